@@ -1,0 +1,167 @@
+/*
+ * qobgpu.h -- C ABI of libqobgpu.so, the GB300 (sm_103a) implementation of
+ * QuantumOpticsBase.jl's operator-application path.
+ *
+ * The library replaces the reference's 5-argument mul!
+ *     mul!(result, a, b, alpha, beta)      result = alpha*a*b + beta*result
+ * for Ket / Bra / Operator results with LazySum, LazyTensor, LazyProduct,
+ * SparseOperator and DenseOperator operands.  A host language (Julia through
+ * ccall, Python through ctypes, C/C++ directly) builds operator handles that
+ * mirror the reference's operator objects, then calls qob_mul on device
+ * buffers.  There is no CPU fallback: every qob_mul runs CUDA kernels.
+ *
+ * Conventions (the reference's):
+ *   - complex data is interleaved (re, im); dtype QOB_C128 = ComplexF64,
+ *     QOB_C64 = ComplexF32;
+ *   - matrices are column-major; CSC index arrays are 1-based (Julia's
+ *     SparseMatrixCSC colptr / rowval) and are converted on upload;
+ *   - composite bases are ordered first subsystem fastest (src/states.jl:105);
+ *   - LazyTensor indices are 1-based and sorted (src/operators_lazytensor.jl:15-36).
+ *
+ * Every function returns a status (QOB_OK = 0); qob_last_error(ctx) gives a
+ * message for the last failure on that context.  All work is stream-ordered
+ * on the stream passed in (NULL = the legacy default stream).  A context is
+ * not thread-safe: use one per host thread.
+ */
+#ifndef QOBGPU_H
+#define QOBGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define QOB_OK 0
+#define QOB_ERR_DIM 1         /* DimensionMismatch (src/operators_lazytensor.jl:695-703) */
+#define QOB_ERR_ALIAS 2       /* ArgumentError: output aliased with input (:704-708) */
+#define QOB_ERR_UNSUPPORTED 3 /* ArgumentError / MethodError: unsupported operand (:640,677) */
+#define QOB_ERR_ARG 4         /* invalid argument: null pointer, malformed CSC, bad index */
+#define QOB_ERR_CUDA 5        /* a CUDA runtime call failed */
+#define QOB_ERR_OOM 6         /* device memory exhausted / admission refused */
+#define QOB_ERR_TIMEOUT 7     /* a bounded device-side wait gave up */
+#define QOB_ERR_STATE 8       /* call not valid in the object's current state */
+
+/* element types */
+#define QOB_C128 0 /* ComplexF64 */
+#define QOB_C64 1  /* ComplexF32 */
+
+/* sides of qob_mul */
+#define QOB_LEFT 0  /* y = alpha * op * x + beta * y   (Ket, or Operator from the left)  */
+#define QOB_RIGHT 1 /* y = alpha * x * op + beta * y   (Bra, or Operator from the right) */
+
+typedef struct qob_ctx qob_ctx;
+typedef struct qob_op qob_op;
+
+int qob_version(void);
+
+/* Context on one CUDA device.  flags: reserved, pass 0. */
+int qob_create(qob_ctx** ctx, int device, unsigned flags);
+int qob_destroy(qob_ctx* ctx);
+const char* qob_last_error(qob_ctx* ctx);
+
+/* ---------------------------------------------------------------------------
+ * Operator handles.  Data is copied from host memory at construction; child
+ * handles may be freed after being used in a parent (the parent keeps its own
+ * reference).
+ * ------------------------------------------------------------------------- */
+
+/* SparseOperator: Operator{BL,BR,<:SparseMatrixCSC} (src/operators_sparse.jl:5-7).
+ * (m, n, colptr[n+1], rowval[nnz], nzval[nnz]) is the stored CSC matrix with
+ * 1-based indices; adjoint != 0 makes the operator its conjugate transpose
+ * (SparseOpAdjType). */
+int qob_op_sparse(qob_ctx* ctx, int64_t m, int64_t n, const int64_t* colptr,
+                  const int64_t* rowval, const void* nzval, int dtype, int adjoint, qob_op** out);
+
+/* DenseOperator: Operator{BL,BR,<:Matrix} (src/operators_dense.jl:12-20,49-52);
+ * column-major m x n with leading dimension ld; adjoint as above. */
+int qob_op_dense(qob_ctx* ctx, int64_t m, int64_t n, const void* data, int64_t ld, int dtype,
+                 int adjoint, qob_op** out);
+
+/* identityoperator data: FillArrays Eye(m, n) (src/operators_sparse.jl:86-88,180-183). */
+int qob_op_eye(qob_ctx* ctx, int64_t m, int64_t n, qob_op** out);
+
+/* LazyTensor(basis_l, basis_r, indices, operators, factor)
+ * (src/operators_lazytensor.jl:15-36).  shape_l / shape_r: the subsystem
+ * lengths of the composite bases (_comp_size, :517-518); indices: nfac
+ * 1-based, strictly increasing subsystem numbers; factors: sparse, dense or
+ * eye handles whose shapes match their subsystems. */
+int qob_op_lazytensor(qob_ctx* ctx, int nsub, const int64_t* shape_l, const int64_t* shape_r,
+                      int nfac, const int64_t* indices, qob_op* const* factors, double factor_re,
+                      double factor_im, qob_op** out);
+
+/* LazySum(basis_l, basis_r, factors, operators) (src/operators_lazysum.jl:41-51);
+ * factors: nterms interleaved complex doubles; an empty sum (nterms == 0) is
+ * allowed and needs (m, n). */
+int qob_op_lazysum(qob_ctx* ctx, int64_t m, int64_t n, int nterms, const double* factors,
+                   qob_op* const* ops, qob_op** out);
+
+/* LazyProduct(operators, factor) (src/operators_lazyproduct.jl:33-52). */
+int qob_op_lazyproduct(qob_ctx* ctx, int nops, qob_op* const* ops, double factor_re,
+                       double factor_im, qob_op** out);
+
+/* Rewrite a LazySum's factors in place, as TimeDependentSum's
+ * update_static_coefficients! does (src/time_dependent_operator.jl:279-290).
+ * The compiled device form is updated without recompiling its structure. */
+int qob_op_set_factors(qob_ctx* ctx, qob_op* sum, const double* factors);
+
+int qob_op_free(qob_ctx* ctx, qob_op* op);
+
+/* Shape of an operator: rows = length(basis_l), cols = length(basis_r). */
+int qob_op_shape(qob_ctx* ctx, const qob_op* op, int64_t* rows, int64_t* cols);
+
+/* Compile (and cache) the device form of op for one side and dtype ahead of
+ * the first qob_mul; qob_mul does this on demand otherwise.  Reports the
+ * compiled structure for diagnostics: info[0] = gather groups, info[1] = 1 if a
+ * merged diagonal is used, info[2] = total stored entries of the groups,
+ * info[3] = number of extra (non-fused) passes.  info may be NULL. */
+int qob_op_prepare(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t* info);
+
+/* ---------------------------------------------------------------------------
+ * Application: the 5-argument mul!.
+ *
+ * side QOB_LEFT : y (m x ncols) = alpha * op * x (n x ncols) + beta * y
+ *   Ket:       mul!(::Ket, op, ::Ket, alpha, beta)        ncols = 1
+ *   Operator:  mul!(::Operator, op, ::Operator, ...)      ncols = columns
+ * side QOB_RIGHT: y (nrows x n) = alpha * x (nrows x m) * op + beta * y
+ *   Bra:       mul!(::Bra, ::Bra, op, alpha, beta)        nrows = 1
+ *   Operator:  mul!(::Operator, ::Operator, op, ...)      nrows = rows
+ *
+ * x and y are DEVICE pointers to column-major arrays with leading dimensions
+ * x_ld, y_ld (elements).  is_vector selects the Ket/Bra form of the
+ * reference's dispatch (gemv! rather than gemm!).  beta == 0 overwrites y
+ * without reading it (NaN in y is ignored, src/operators_lazysum.jl:179-186).
+ * Errors: QOB_ERR_DIM on shape mismatch, QOB_ERR_ALIAS when y overlaps x.
+ * ------------------------------------------------------------------------- */
+int qob_mul(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, double alpha_re,
+            double alpha_im, const void* x, int64_t x_rows, int64_t x_cols, int64_t x_ld,
+            double beta_re, double beta_im, void* y, int64_t y_rows, int64_t y_cols, int64_t y_ld,
+            void* stream);
+
+/* Same as qob_mul for HOST x and y: the library copies x to the device, applies
+ * the operator and copies y back (the path a caller without device buffers
+ * uses).  Synchronous. */
+int qob_mul_host(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, double alpha_re,
+                 double alpha_im, const void* x, int64_t x_rows, int64_t x_cols, double beta_re,
+                 double beta_im, void* y, int64_t y_rows, int64_t y_cols);
+
+/* ---------------------------------------------------------------------------
+ * FP64 reductions (norm, inner product, expectation value) on device vectors;
+ * deterministic order.  Results are written to HOST memory (synchronous).
+ * x of dtype QOB_C128 or QOB_C64; accumulation is always in double.
+ * ------------------------------------------------------------------------- */
+/* norm(x) (src/states.jl:89) */
+int qob_norm(qob_ctx* ctx, int dtype, const void* x, int64_t n, double* result, void* stream);
+/* dot(x, y) = sum conj(x_i) y_i, result interleaved complex */
+int qob_dot(qob_ctx* ctx, int dtype, const void* x, const void* y, int64_t n, double* result,
+            void* stream);
+/* expect(op, psi) = <psi|op|psi> (src/operators.jl:119) */
+int qob_expect(qob_ctx* ctx, qob_op* op, int dtype, const void* psi, int64_t n, double* result,
+               void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QOBGPU_H */

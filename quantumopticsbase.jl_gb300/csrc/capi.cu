@@ -1,0 +1,529 @@
+// capi.cu -- the C ABI (include/qobgpu.h): operator handles, plan cache,
+// execution of compiled plans, and the FP64 reductions.
+#include <algorithm>
+#include <cstring>
+#include <new>
+
+#include "qob_internal.h"
+
+namespace qob {
+
+void fail(int code, const std::string& msg) { throw Error{code, msg}; }
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return;
+  cudaGetLastError();  // clear a sticky-free error so the context stays usable
+  if (e == cudaErrorMemoryAllocation) fail(QOB_ERR_OOM, std::string(what) + ": out of device memory");
+  fail(QOB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+DeviceBuf::~DeviceBuf() {
+  if (p) cudaFree(p);
+}
+void DeviceBuf::alloc(size_t b) {
+  if (p) {
+    cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  QOB_CUDA(cudaMalloc(&p, b));
+  bytes = b;
+}
+void DeviceBuf::upload(const void* host, size_t b) {
+  if (!p || bytes < b) alloc(b);
+  QOB_CUDA(cudaMemcpy(p, host, b, cudaMemcpyHostToDevice));
+}
+
+void* Workspace::get(size_t slot, size_t bytes) {
+  if (slots.size() <= slot) slots.resize(slot + 1);
+  DeviceBuf& d = slots[slot];
+  if (d.bytes < bytes) {
+    // buffers are reused across calls; wait for work that may still use the old one
+    QOB_CUDA(cudaDeviceSynchronize());
+    d.alloc(bytes + bytes / 4);
+  }
+  return d.p;
+}
+
+Context::~Context() {
+  if (reduce_host) cudaFreeHost(reduce_host);
+}
+
+namespace {
+
+c128 coefval(const TermCoef& c, const OpNode* root) {
+  if (c.top < 0) return c.inner;
+  return cmul(root->factors[c.top], c.inner);
+}
+
+int64_t prod_range(const std::vector<int64_t>& v, size_t lo, size_t hi) {
+  int64_t p = 1;
+  for (size_t i = lo; i < hi; ++i) p *= v[i];
+  return p;
+}
+
+}  // namespace
+
+// Runs a compiled plan: y = alpha * op * x + beta * y on ncols vectors whose
+// element e of vector c lives at x[e * xes + c * xcs].
+void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, int64_t xcs,
+                c128 beta, void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s,
+                int ws) {
+  const size_t esz = P.precision == QOB_C128 ? 16 : 8;
+  const c128 one{1.0, 0.0}, zero{0.0, 0.0};
+  if (P.kind == Plan::Kind::Sum) {
+    // LazySum with no terms or alpha == 0: _zero_op_mul! (src/operators_lazysum.jl:190-192)
+    if (is_zero(alpha) || P.nterms_total == 0) {
+      launch_scale(P.precision, y, P.m, ncols, yes, ycs, beta, s);
+      return;
+    }
+    c128 b = beta;  // the first pass applies beta, the rest accumulate (:194-197)
+    if (P.gather) {
+      launch_gather(*P.gather, P.precision, x, xes, xcs, y, yes, ycs, ncols, alpha, b, s);
+      b = one;
+    }
+    for (auto& d : P.dense) {
+      launch_dense(P.precision, d.a.p, d.m, d.n, cmul(alpha, coefval(d.coef, P.root)), x, xes, xcs, b, y,
+                   yes, ycs, ncols, s);
+      b = one;
+    }
+    for (auto& mk : P.modek) {
+      const c128 a = cmul(alpha, coefval(mk.coef, P.root));
+      const size_t nst = mk.steps.size();
+      if (nst == 0) {
+        launch_axpby(P.precision, x, xes, xcs, a, y, yes, ycs, b, P.m, ncols, s);
+        b = one;
+        continue;
+      }
+      std::vector<int64_t> cur = mk.shape_in;
+      const void* src = x;
+      int64_t ses = xes, scs = xcs;
+      for (size_t k = 0; k < nst; ++k) {
+        const ModekStep& st = mk.steps[k];
+        std::vector<int64_t> next = cur;
+        next[st.site] = st.dout;
+        const int64_t s1 = prod_range(cur, 0, st.site), s3 = prod_range(cur, st.site + 1, cur.size());
+        const c128 ak = (k == 0) ? a : one;
+        if (k + 1 == nst) {
+          launch_modek(P.precision, st.a.p, st.eye, s1, st.dout, st.din, s3, ak, src, ses, scs, b, y, yes,
+                       ycs, ncols, s);
+        } else {
+          const int64_t len = prod_range(next, 0, next.size());
+          void* t = ctx.ws.get(ws + (k % 2), (size_t)len * ncols * esz);
+          launch_modek(P.precision, st.a.p, st.eye, s1, st.dout, st.din, s3, ak, src, ses, scs, zero, t, 1,
+                       len, ncols, s);
+          src = t;
+          ses = 1;
+          scs = len;
+        }
+        cur = next;
+      }
+      b = one;
+    }
+    for (auto& sp : P.subs) {
+      apply_plan(ctx, *sp.plan, cmul(alpha, coefval(sp.coef, P.root)), x, xes, xcs, b, y, yes, ycs, ncols, s,
+                 ws + 2);
+      b = one;
+    }
+    return;
+  }
+  // LazyProduct (src/operators_lazyproduct.jl:103-164)
+  if (is_zero(alpha)) {
+    launch_scale(P.precision, y, P.m, ncols, yes, ycs, beta, s);
+    return;
+  }
+  const size_t n = P.chain.size();
+  if (n == 1) {
+    apply_plan(ctx, *P.chain[0], cmul(P.pfactor, alpha), x, xes, xcs, beta, y, yes, ycs, ncols, s, ws);
+    return;
+  }
+  const void* src = x;
+  int64_t ses = xes, scs = xcs;
+  for (size_t i = 0; i < n; ++i) {
+    Plan& Q = *P.chain[i];
+    if (i + 1 == n) {
+      apply_plan(ctx, Q, alpha, src, ses, scs, beta, y, yes, ycs, ncols, s, ws + 2);
+    } else {
+      void* t = ctx.ws.get(ws + (i % 2), (size_t)Q.m * ncols * esz);
+      apply_plan(ctx, Q, i == 0 ? P.pfactor : one, src, ses, scs, zero, t, 1, Q.m, ncols, s, ws + 2);
+      src = t;
+      ses = 1;
+      scs = Q.m;
+    }
+  }
+}
+
+}  // namespace qob
+
+using namespace qob;
+
+namespace {
+
+template <class F>
+int guard(qob_ctx* ctx, F&& f) {
+  try {
+    if (ctx) QOB_CUDA(cudaSetDevice(ctx->c.device));
+    f();
+    return QOB_OK;
+  } catch (const Error& e) {
+    if (ctx) ctx->c.err = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    if (ctx) ctx->c.err = "host out of memory";
+    return QOB_ERR_OOM;
+  } catch (const std::exception& e) {
+    if (ctx) ctx->c.err = e.what();
+    return QOB_ERR_ARG;
+  }
+}
+
+c128 read_c(const void* p, int dtype, int64_t i) {
+  if (dtype == QOB_C128) {
+    const double* d = static_cast<const double*>(p);
+    return {d[2 * i], d[2 * i + 1]};
+  }
+  const float* f = static_cast<const float*>(p);
+  return {(double)f[2 * i], (double)f[2 * i + 1]};
+}
+
+void check_dtype(int dtype) {
+  if (dtype != QOB_C128 && dtype != QOB_C64) fail(QOB_ERR_ARG, "dtype must be QOB_C128 or QOB_C64");
+}
+
+qob_op* wrap(NodeP n) {
+  auto* h = new qob_op;
+  h->node = std::move(n);
+  return h;
+}
+
+bool is_leaf(const OpNode& n) { return n.kind == Kind::Sparse || n.kind == Kind::Dense || n.kind == Kind::Eye; }
+
+Plan& get_plan(Context& ctx, qob_op* op, int side, int prec) {
+  auto& slot = op->plans[side][prec];
+  if (slot && !plan_is_current(*slot)) {
+    bool only_root = true;
+    for (auto& d : slot->deps)
+      if (d.first != op->node.get() && d.first->factors_version != d.second) only_root = false;
+    if (only_root && op->node->kind == Kind::LazySum)
+      refresh_coefficients(*slot, *op->node);
+    else
+      slot.reset();
+  }
+  if (!slot) slot = compile_plan(ctx, op->node, side, prec);
+  return *slot;
+}
+
+bool overlaps(const void* a, size_t abytes, const void* b, size_t bbytes) {
+  const char* pa = static_cast<const char*>(a);
+  const char* pb = static_cast<const char*>(b);
+  return pa < pb + bbytes && pb < pa + abytes;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qob_version(void) { return 10000; }
+
+int qob_create(qob_ctx** ctx, int device, unsigned flags) {
+  (void)flags;
+  if (!ctx) return QOB_ERR_ARG;
+  *ctx = nullptr;
+  auto* c = new qob_ctx;
+  c->c.device = device;
+  int rc = guard(c, [&] {
+    int n = 0;
+    QOB_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) fail(QOB_ERR_ARG, "no such CUDA device");
+    QOB_CUDA(cudaDeviceGetAttribute(&c->c.num_sms, cudaDevAttrMultiProcessorCount, device));
+  });
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  *ctx = c;
+  return QOB_OK;
+}
+
+int qob_destroy(qob_ctx* ctx) {
+  if (!ctx) return QOB_ERR_ARG;
+  cudaSetDevice(ctx->c.device);
+  delete ctx;
+  return QOB_OK;
+}
+
+const char* qob_last_error(qob_ctx* ctx) { return ctx ? ctx->c.err.c_str() : "null context"; }
+
+int qob_op_sparse(qob_ctx* ctx, int64_t m, int64_t n, const int64_t* colptr, const int64_t* rowval,
+                  const void* nzval, int dtype, int adjoint, qob_op** out) {
+  return guard(ctx, [&] {
+    if (!out || !colptr || m < 0 || n < 0) fail(QOB_ERR_ARG, "qob_op_sparse: bad arguments");
+    check_dtype(dtype);
+    auto nd = std::make_shared<OpNode>();
+    nd->kind = Kind::Sparse;
+    nd->sm = m;
+    nd->sn = n;
+    nd->adjoint = adjoint != 0;
+    nd->m = nd->adjoint ? n : m;
+    nd->n = nd->adjoint ? m : n;
+    nd->src_dtype = dtype;
+    if (colptr[0] != 1) fail(QOB_ERR_ARG, "CSC colptr must start at 1");
+    nd->colptr.resize(n + 1);
+    for (int64_t c = 0; c <= n; ++c) {
+      nd->colptr[c] = colptr[c] - 1;
+      if (c > 0 && nd->colptr[c] < nd->colptr[c - 1]) fail(QOB_ERR_ARG, "CSC colptr must be non-decreasing");
+    }
+    const int64_t nnz = nd->colptr[n];
+    if (nnz > 0 && (!rowval || !nzval)) fail(QOB_ERR_ARG, "CSC with entries needs rowval and nzval");
+    nd->rowval.resize(nnz);
+    nd->vals.resize(nnz);
+    for (int64_t p = 0; p < nnz; ++p) {
+      if (rowval[p] < 1 || rowval[p] > m) fail(QOB_ERR_ARG, "CSC row index out of range");
+      nd->rowval[p] = rowval[p] - 1;
+      nd->vals[p] = read_c(nzval, dtype, p);
+    }
+    *out = wrap(nd);
+  });
+}
+
+int qob_op_dense(qob_ctx* ctx, int64_t m, int64_t n, const void* data, int64_t ld, int dtype, int adjoint,
+                 qob_op** out) {
+  return guard(ctx, [&] {
+    if (!out || (m * n > 0 && !data) || m < 0 || n < 0 || ld < std::max<int64_t>(m, 1))
+      fail(QOB_ERR_ARG, "qob_op_dense: bad arguments");
+    check_dtype(dtype);
+    auto nd = std::make_shared<OpNode>();
+    nd->kind = Kind::Dense;
+    nd->sm = m;
+    nd->sn = n;
+    nd->adjoint = adjoint != 0;
+    nd->m = nd->adjoint ? n : m;
+    nd->n = nd->adjoint ? m : n;
+    nd->src_dtype = dtype;
+    nd->vals.resize(m * n);
+    for (int64_t c = 0; c < n; ++c)
+      for (int64_t r = 0; r < m; ++r) nd->vals[r + c * m] = read_c(data, dtype, r + c * ld);
+    *out = wrap(nd);
+  });
+}
+
+int qob_op_eye(qob_ctx* ctx, int64_t m, int64_t n, qob_op** out) {
+  return guard(ctx, [&] {
+    if (!out || m < 0 || n < 0) fail(QOB_ERR_ARG, "qob_op_eye: bad arguments");
+    auto nd = std::make_shared<OpNode>();
+    nd->kind = Kind::Eye;
+    nd->sm = nd->m = m;
+    nd->sn = nd->n = n;
+    *out = wrap(nd);
+  });
+}
+
+int qob_op_lazytensor(qob_ctx* ctx, int nsub, const int64_t* shape_l, const int64_t* shape_r, int nfac,
+                      const int64_t* indices, qob_op* const* factors, double factor_re, double factor_im,
+                      qob_op** out) {
+  return guard(ctx, [&] {
+    if (!out || nsub < 1 || !shape_l || !shape_r || nfac < 0 || (nfac > 0 && (!indices || !factors)))
+      fail(QOB_ERR_ARG, "qob_op_lazytensor: bad arguments");
+    auto nd = std::make_shared<OpNode>();
+    nd->kind = Kind::LazyTensor;
+    nd->shape_l.assign(shape_l, shape_l + nsub);
+    nd->shape_r.assign(shape_r, shape_r + nsub);
+    nd->m = nd->n = 1;
+    for (int i = 0; i < nsub; ++i) {
+      if (shape_l[i] < 1 || shape_r[i] < 1) fail(QOB_ERR_ARG, "subsystem lengths must be positive");
+      nd->m *= shape_l[i];
+      nd->n *= shape_r[i];
+    }
+    nd->factor = {factor_re, factor_im};
+    for (int k = 0; k < nfac; ++k) {
+      const int64_t idx = indices[k];
+      if (idx < 1 || idx > nsub) fail(QOB_ERR_ARG, "LazyTensor index out of range");
+      if (k > 0 && idx <= indices[k - 1]) fail(QOB_ERR_ARG, "LazyTensor indices must be sorted and unique");
+      if (!factors[k]) fail(QOB_ERR_ARG, "null factor");
+      const NodeP& f = factors[k]->node;
+      if (!is_leaf(*f))
+        fail(QOB_ERR_UNSUPPORTED, "gemm! of LazyTensor is not implemented for a non-data operator factor");
+      if (f->m != shape_l[idx - 1] || f->n != shape_r[idx - 1])
+        fail(QOB_ERR_DIM, "factor shape does not match its subsystem");
+      nd->sites.push_back((int)(idx - 1));
+      nd->ops.push_back(f);
+    }
+    *out = wrap(nd);
+  });
+}
+
+int qob_op_lazysum(qob_ctx* ctx, int64_t m, int64_t n, int nterms, const double* factors, qob_op* const* ops,
+                   qob_op** out) {
+  return guard(ctx, [&] {
+    if (!out || nterms < 0 || (nterms > 0 && (!factors || !ops)) || m < 0 || n < 0)
+      fail(QOB_ERR_ARG, "qob_op_lazysum: bad arguments");
+    auto nd = std::make_shared<OpNode>();
+    nd->kind = Kind::LazySum;
+    nd->m = m;
+    nd->n = n;
+    for (int k = 0; k < nterms; ++k) {
+      if (!ops[k]) fail(QOB_ERR_ARG, "null term");
+      const NodeP& t = ops[k]->node;
+      if (t->m != m || t->n != n) fail(QOB_ERR_DIM, "LazySum term shape does not match the sum (IncompatibleBases)");
+      nd->ops.push_back(t);
+      nd->factors.push_back({factors[2 * k], factors[2 * k + 1]});
+    }
+    *out = wrap(nd);
+  });
+}
+
+int qob_op_lazyproduct(qob_ctx* ctx, int nops, qob_op* const* ops, double factor_re, double factor_im,
+                       qob_op** out) {
+  return guard(ctx, [&] {
+    if (!out || nops < 1 || !ops) fail(QOB_ERR_ARG, "LazyProduct needs at least one operator");
+    auto nd = std::make_shared<OpNode>();
+    nd->kind = Kind::LazyProduct;
+    for (int k = 0; k < nops; ++k) {
+      if (!ops[k]) fail(QOB_ERR_ARG, "null operator");
+      if (k > 0 && ops[k - 1]->node->n != ops[k]->node->m)
+        fail(QOB_ERR_DIM, "LazyProduct operators are not multiplicable");
+      nd->ops.push_back(ops[k]->node);
+    }
+    nd->m = nd->ops.front()->m;
+    nd->n = nd->ops.back()->n;
+    nd->factor = {factor_re, factor_im};
+    *out = wrap(nd);
+  });
+}
+
+int qob_op_set_factors(qob_ctx* ctx, qob_op* op, const double* factors) {
+  return guard(ctx, [&] {
+    if (!op || (!factors && !op->node->factors.empty())) fail(QOB_ERR_ARG, "qob_op_set_factors: bad arguments");
+    if (op->node->kind != Kind::LazySum) fail(QOB_ERR_ARG, "set_factors needs a LazySum");
+    for (size_t k = 0; k < op->node->factors.size(); ++k) op->node->factors[k] = {factors[2 * k], factors[2 * k + 1]};
+    op->node->factors_version++;
+  });
+}
+
+int qob_op_free(qob_ctx* ctx, qob_op* op) {
+  return guard(ctx, [&] { delete op; });
+}
+
+int qob_op_shape(qob_ctx* ctx, const qob_op* op, int64_t* rows, int64_t* cols) {
+  return guard(ctx, [&] {
+    if (!op) fail(QOB_ERR_ARG, "null operator");
+    if (rows) *rows = op->node->m;
+    if (cols) *cols = op->node->n;
+  });
+}
+
+int qob_op_prepare(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t* info) {
+  return guard(ctx, [&] {
+    if (!ctx || !op || (side != QOB_LEFT && side != QOB_RIGHT)) fail(QOB_ERR_ARG, "qob_op_prepare: bad arguments");
+    check_dtype(dtype);
+    Plan& P = get_plan(ctx->c, op, side, dtype);
+    if (info) {
+      info[0] = P.gather ? P.gather->ngroups : 0;
+      info[1] = P.gather && P.gather->has_diag ? 1 : 0;
+      info[2] = P.gather ? P.gather->nentries : 0;
+      info[3] = (int64_t)(P.dense.size() + P.modek.size() + P.subs.size() + P.chain.size());
+    }
+  });
+}
+
+int qob_mul(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, double alpha_re, double alpha_im,
+            const void* x, int64_t x_rows, int64_t x_cols, int64_t x_ld, double beta_re, double beta_im, void* y,
+            int64_t y_rows, int64_t y_cols, int64_t y_ld, void* stream) {
+  return guard(ctx, [&] {
+    if (!ctx || !op) fail(QOB_ERR_ARG, "null context or operator");
+    if (side != QOB_LEFT && side != QOB_RIGHT) fail(QOB_ERR_ARG, "side must be QOB_LEFT or QOB_RIGHT");
+    check_dtype(dtype);
+    const int64_t m = op->node->m, n = op->node->n;
+    int64_t ncols, xes, xcs, yes, ycs;
+    if (side == QOB_LEFT) {
+      if (x_rows != n) fail(QOB_ERR_DIM, "A and B dimensions do not match. Can't do `A*B`");
+      if (y_rows != m || y_cols != x_cols) fail(QOB_ERR_DIM, "Output dimensions do not match A*B. Can't do `R.=A*B`");
+      if (is_vector && x_cols != 1) fail(QOB_ERR_ARG, "a Ket has one column");
+      if (x_ld < std::max<int64_t>(x_rows, 1) || y_ld < std::max<int64_t>(y_rows, 1))
+        fail(QOB_ERR_ARG, "leading dimension smaller than the number of rows");
+      ncols = x_cols;
+      xes = 1;
+      xcs = x_ld;
+      yes = 1;
+      ycs = y_ld;
+    } else {
+      if (x_cols != m) fail(QOB_ERR_DIM, "A and B dimensions do not match. Can't do `A*B`");
+      if (y_cols != n || y_rows != x_rows) fail(QOB_ERR_DIM, "Output dimensions do not match A*B. Can't do `R.=A*B`");
+      if (is_vector && x_rows != 1) fail(QOB_ERR_ARG, "a Bra has one row");
+      if (x_ld < std::max<int64_t>(x_rows, 1) || y_ld < std::max<int64_t>(y_rows, 1))
+        fail(QOB_ERR_ARG, "leading dimension smaller than the number of rows");
+      ncols = x_rows;
+      xes = x_ld;
+      xcs = 1;
+      yes = y_ld;
+      ycs = 1;
+    }
+    if (ncols == 0 || (side == QOB_LEFT ? m : n) == 0) return;
+    if (!x || !y) fail(QOB_ERR_ARG, "null data pointer");
+    const size_t esz = dtype == QOB_C128 ? 16 : 8;
+    const size_t xbytes = (size_t)(x_ld * (x_cols - 1) + x_rows) * esz;
+    const size_t ybytes = (size_t)(y_ld * (y_cols - 1) + y_rows) * esz;
+    if (overlaps(x, xbytes, y, ybytes)) fail(QOB_ERR_ALIAS, "output matrix must not be aliased with input matrix");
+    if (ncols > 65535 && side == QOB_RIGHT) fail(QOB_ERR_UNSUPPORTED, "more than 65535 rows");
+    Plan& P = get_plan(ctx->c, op, side, dtype);
+    apply_plan(ctx->c, P, {alpha_re, alpha_im}, x, xes, xcs, {beta_re, beta_im}, y, yes, ycs, ncols,
+               (cudaStream_t)stream, 0);
+  });
+}
+
+int qob_mul_host(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, double alpha_re, double alpha_im,
+                 const void* x, int64_t x_rows, int64_t x_cols, double beta_re, double beta_im, void* y,
+                 int64_t y_rows, int64_t y_cols) {
+  int rc = guard(ctx, [&] {
+    if (!ctx || !op || !x || !y) fail(QOB_ERR_ARG, "null argument");
+    check_dtype(dtype);
+    const size_t esz = dtype == QOB_C128 ? 16 : 8;
+    const size_t xb = (size_t)x_rows * x_cols * esz, yb = (size_t)y_rows * y_cols * esz;
+    if (ctx->c.host_x.bytes < xb) ctx->c.host_x.alloc(xb);
+    if (ctx->c.host_y.bytes < yb) ctx->c.host_y.alloc(yb);
+    QOB_CUDA(cudaMemcpyAsync(ctx->c.host_x.p, x, xb, cudaMemcpyHostToDevice, 0));
+    if (beta_re != 0.0 || beta_im != 0.0)
+      QOB_CUDA(cudaMemcpyAsync(ctx->c.host_y.p, y, yb, cudaMemcpyHostToDevice, 0));
+  });
+  if (rc) return rc;
+  rc = qob_mul(ctx, side, is_vector, op, dtype, alpha_re, alpha_im, ctx->c.host_x.p, x_rows, x_cols,
+               std::max<int64_t>(x_rows, 1), beta_re, beta_im, ctx->c.host_y.p, y_rows, y_cols,
+               std::max<int64_t>(y_rows, 1), nullptr);
+  if (rc) return rc;
+  return guard(ctx, [&] {
+    const size_t esz = dtype == QOB_C128 ? 16 : 8;
+    QOB_CUDA(cudaMemcpyAsync(y, ctx->c.host_y.p, (size_t)y_rows * y_cols * esz, cudaMemcpyDeviceToHost, 0));
+    QOB_CUDA(cudaStreamSynchronize(0));
+  });
+}
+
+int qob_norm(qob_ctx* ctx, int dtype, const void* x, int64_t n, double* result, void* stream) {
+  return guard(ctx, [&] {
+    if (!ctx || !x || !result || n < 0) fail(QOB_ERR_ARG, "qob_norm: bad arguments");
+    check_dtype(dtype);
+    reduce_dot(ctx->c, dtype, x, x, n, true, result, (cudaStream_t)stream);
+  });
+}
+
+int qob_dot(qob_ctx* ctx, int dtype, const void* x, const void* y, int64_t n, double* result, void* stream) {
+  return guard(ctx, [&] {
+    if (!ctx || !x || !y || !result || n < 0) fail(QOB_ERR_ARG, "qob_dot: bad arguments");
+    check_dtype(dtype);
+    reduce_dot(ctx->c, dtype, x, y, n, false, result, (cudaStream_t)stream);
+  });
+}
+
+int qob_expect(qob_ctx* ctx, qob_op* op, int dtype, const void* psi, int64_t n, double* result, void* stream) {
+  return guard(ctx, [&] {
+    if (!ctx || !op || !psi || !result) fail(QOB_ERR_ARG, "qob_expect: bad arguments");
+    check_dtype(dtype);
+    if (op->node->m != n || op->node->n != n) fail(QOB_ERR_DIM, "expect needs a square operator matching the state");
+    const size_t esz = dtype == QOB_C128 ? 16 : 8;
+    void* t = ctx->c.ws.get(15, (size_t)n * esz);
+    Plan& P = get_plan(ctx->c, op, QOB_LEFT, dtype);
+    apply_plan(ctx->c, P, {1.0, 0.0}, psi, 1, n, {0.0, 0.0}, t, 1, n, 1, (cudaStream_t)stream, 16);
+    reduce_dot(ctx->c, dtype, psi, t, n, false, result, (cudaStream_t)stream);
+  });
+}
+
+}  // extern "C"

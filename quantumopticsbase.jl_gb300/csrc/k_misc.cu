@@ -1,0 +1,314 @@
+// k_misc.cu -- the smaller kernels of the application path:
+//   * beta scaling / zero fill            (_zero_op_mul!, src/operators_lazysum.jl:179-186)
+//   * y = alpha x + beta y                (_tp_sum_matmul! with no factors, :453-458)
+//   * dense operator times vectors        (mul! -> BLAS, src/operators_dense.jl:394-396)
+//   * one mode product of a factor        (_tp_matmul_first!/_mid!/_last!,
+//                                          src/operators_lazytensor.jl:281-428)
+//   * FP64 reductions: norm, dot          (src/states.jl:89, src/operators.jl:119)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "qob_internal.h"
+
+namespace qob {
+
+namespace {
+
+template <typename R>
+struct Cx;
+template <>
+struct Cx<double> {
+  using T = double2;
+};
+template <>
+struct Cx<float> {
+  using T = float2;
+};
+
+template <typename CT>
+__device__ __forceinline__ CT mk(double re, double im) {
+  CT o;
+  o.x = (decltype(o.x))re;
+  o.y = (decltype(o.y))im;
+  return o;
+}
+
+// ---------------------------------------------------------------------------
+template <typename CT>
+__global__ void k_scale(CT* y, int64_t rows, int64_t cols, int64_t lr, int64_t lc, double br,
+                        double bi) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= rows * cols) return;
+  const int64_t r = i % rows, c = i / rows;
+  CT* p = y + r * lr + c * lc;
+  if (br == 0.0 && bi == 0.0) {
+    *p = mk<CT>(0.0, 0.0);
+  } else {
+    CT o = *p;
+    double re = br * (double)o.x - bi * (double)o.y;
+    double im = br * (double)o.y + bi * (double)o.x;
+    *p = mk<CT>(re, im);
+  }
+}
+
+// y[e, c] = alpha * x[e, c] + beta * y[e, c]   (beta == 0: y not read)
+template <typename CT, typename R>
+__global__ void k_axpby(const CT* __restrict__ x, int64_t xes, int64_t xcs, CT* __restrict__ y,
+                        int64_t yes, int64_t ycs, int64_t len, int64_t ncols, double ar, double ai,
+                        double br, double bi) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= len * ncols) return;
+  const int64_t e = i % len, c = i / len;
+  CT xv = x[e * xes + c * xcs];
+  R re = (R)ar * xv.x - (R)ai * xv.y;
+  R im = (R)ar * xv.y + (R)ai * xv.x;
+  CT* yp = y + e * yes + c * ycs;
+  if (br != 0.0 || bi != 0.0) {
+    CT o = *yp;
+    re += (R)br * o.x - (R)bi * o.y;
+    im += (R)br * o.y + (R)bi * o.x;
+  }
+  *yp = mk<CT>(re, im);
+}
+
+// Dense operator (m x n, column-major) times ncols vectors: one thread per
+// output (i, c); the operator column reads are coalesced across i.
+template <typename CT, typename R>
+__global__ void k_dense(const CT* __restrict__ a, int64_t m, int64_t n, const CT* __restrict__ x,
+                        int64_t xes, int64_t xcs, CT* __restrict__ y, int64_t yes, int64_t ycs,
+                        int64_t ncols, double ar, double ai, double br, double bi) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t c = blockIdx.y;
+  if (i >= m || c >= ncols) return;
+  R sre = 0, sim = 0;
+  const CT* xc = x + c * xcs;
+  for (int64_t k = 0; k < n; ++k) {
+    CT av = a[i + k * m];
+    CT xv = xc[k * xes];
+    sre = fma(av.x, xv.x, sre);
+    sre = fma(-av.y, xv.y, sre);
+    sim = fma(av.x, xv.y, sim);
+    sim = fma(av.y, xv.x, sim);
+  }
+  R re = (R)ar * sre - (R)ai * sim;
+  R im = (R)ar * sim + (R)ai * sre;
+  CT* yp = y + i * yes + c * ycs;
+  if (br != 0.0 || bi != 0.0) {
+    CT o = *yp;
+    re += (R)br * o.x - (R)bi * o.y;
+    im += (R)br * o.y + (R)bi * o.x;
+  }
+  *yp = mk<CT>(re, im);
+}
+
+// One mode product: out[a, j, b] = alpha * sum_k A[j, k] in[a, k, b] + beta * out,
+// a < s1, j < dout, b < s3; element e of vector c at x[e * xes + c * xcs].
+// A non-square Eye is the truncated identity (src/operators_lazytensor.jl:348-371).
+template <typename CT, typename R, bool EYE>
+__global__ void k_modek(const CT* __restrict__ A, int64_t s1, int64_t dout, int64_t din, int64_t s3,
+                        const CT* __restrict__ x, int64_t xes, int64_t xcs, CT* __restrict__ y,
+                        int64_t yes, int64_t ycs, int64_t ncols, double ar, double ai, double br,
+                        double bi) {
+  const int64_t len = s1 * dout * s3;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t c = blockIdx.y;
+  if (i >= len || c >= ncols) return;
+  const int64_t a = i % s1, t = i / s1, j = t % dout, b = t / dout;
+  const CT* xc = x + c * xcs;
+  R sre = 0, sim = 0;
+  if (EYE) {
+    if (j < din) {
+      CT xv = xc[(a + s1 * (j + din * b)) * xes];
+      sre = xv.x;
+      sim = xv.y;
+    }
+  } else {
+    for (int64_t k = 0; k < din; ++k) {
+      CT av = A[j + k * dout];
+      CT xv = xc[(a + s1 * (k + din * b)) * xes];
+      sre = fma(av.x, xv.x, sre);
+      sre = fma(-av.y, xv.y, sre);
+      sim = fma(av.x, xv.y, sim);
+      sim = fma(av.y, xv.x, sim);
+    }
+  }
+  R re = (R)ar * sre - (R)ai * sim;
+  R im = (R)ar * sim + (R)ai * sre;
+  CT* yp = y + i * yes + c * ycs;
+  if (br != 0.0 || bi != 0.0) {
+    CT o = *yp;
+    re += (R)br * o.x - (R)bi * o.y;
+    im += (R)br * o.y + (R)bi * o.x;
+  }
+  *yp = mk<CT>(re, im);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 reductions in a fixed order: block partials (strided per thread, then a
+// shared-memory tree), then one block sums the partials in index order.
+constexpr int kRedThreads = 256;
+constexpr int kRedBlocks = 304;  // 2 x 152 SMs
+
+template <typename CT>
+__global__ void k_dot_partial(const CT* __restrict__ x, const CT* __restrict__ y, int64_t n,
+                              double2* __restrict__ part) {
+  __shared__ double sre[kRedThreads], sim[kRedThreads];
+  double re = 0.0, im = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)kRedThreads + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kRedThreads) {
+    CT a = x[i], b = y[i];
+    const double ax = a.x, ay = a.y, bx = b.x, by = b.y;
+    // conj(a) * b
+    re = fma(ax, bx, re);
+    re = fma(ay, by, re);
+    im = fma(ax, by, im);
+    im = fma(-ay, bx, im);
+  }
+  sre[threadIdx.x] = re;
+  sim[threadIdx.x] = im;
+  __syncthreads();
+  for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      sre[threadIdx.x] += sre[threadIdx.x + w];
+      sim[threadIdx.x] += sim[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = make_double2(sre[0], sim[0]);
+}
+
+__global__ void k_dot_final(const double2* __restrict__ part, int nparts, double2* out) {
+  __shared__ double sre[kRedThreads], sim[kRedThreads];
+  double re = 0.0, im = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += kRedThreads) {
+    re += part[i].x;
+    im += part[i].y;
+  }
+  sre[threadIdx.x] = re;
+  sim[threadIdx.x] = im;
+  __syncthreads();
+  for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      sre[threadIdx.x] += sre[threadIdx.x + w];
+      sim[threadIdx.x] += sim[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = make_double2(sre[0], sim[0]);
+}
+
+inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+}  // namespace
+
+void launch_scale(int precision, void* y, int64_t rows, int64_t cols, int64_t lr, int64_t lc,
+                  c128 beta, cudaStream_t s) {
+  if (beta.re == 1.0 && beta.im == 0.0) return;
+  const int64_t n = rows * cols;
+  if (n == 0) return;
+  if (precision == QOB_C128)
+    k_scale<double2><<<blocks_for(n, 256), 256, 0, s>>>((double2*)y, rows, cols, lr, lc, beta.re, beta.im);
+  else
+    k_scale<float2><<<blocks_for(n, 256), 256, 0, s>>>((float2*)y, rows, cols, lr, lc, beta.re, beta.im);
+  QOB_CUDA(cudaGetLastError());
+}
+
+void launch_axpby(int precision, const void* x, int64_t xes, int64_t xcs, c128 alpha, void* y,
+                  int64_t yes, int64_t ycs, c128 beta, int64_t len, int64_t ncols, cudaStream_t s) {
+  const int64_t n = len * ncols;
+  if (n == 0) return;
+  if (precision == QOB_C128)
+    k_axpby<double2, double><<<blocks_for(n, 256), 256, 0, s>>>(
+        (const double2*)x, xes, xcs, (double2*)y, yes, ycs, len, ncols, alpha.re, alpha.im, beta.re, beta.im);
+  else
+    k_axpby<float2, float><<<blocks_for(n, 256), 256, 0, s>>>(
+        (const float2*)x, xes, xcs, (float2*)y, yes, ycs, len, ncols, alpha.re, alpha.im, beta.re, beta.im);
+  QOB_CUDA(cudaGetLastError());
+}
+
+void launch_dense(int precision, const void* a, int64_t m, int64_t n, c128 alpha, const void* x,
+                  int64_t xes, int64_t xcs, c128 beta, void* y, int64_t yes, int64_t ycs,
+                  int64_t ncols, cudaStream_t s) {
+  if (m == 0 || ncols == 0) return;
+  const size_t esz = precision == QOB_C128 ? 16 : 8;
+  if (ncols > 65535) {  // grid.y limit: split the vectors
+    for (int64_t c0 = 0; c0 < ncols; c0 += 65535)
+      launch_dense(precision, a, m, n, alpha, (const char*)x + c0 * xcs * esz, xes, xcs, beta,
+                   (char*)y + c0 * ycs * esz, yes, ycs, std::min<int64_t>(65535, ncols - c0), s);
+    return;
+  }
+  dim3 grid(blocks_for(m, 128), (unsigned)ncols);
+  if (precision == QOB_C128)
+    k_dense<double2, double><<<grid, 128, 0, s>>>((const double2*)a, m, n, (const double2*)x, xes, xcs,
+                                                  (double2*)y, yes, ycs, ncols, alpha.re, alpha.im,
+                                                  beta.re, beta.im);
+  else
+    k_dense<float2, float><<<grid, 128, 0, s>>>((const float2*)a, m, n, (const float2*)x, xes, xcs,
+                                                (float2*)y, yes, ycs, ncols, alpha.re, alpha.im,
+                                                beta.re, beta.im);
+  QOB_CUDA(cudaGetLastError());
+}
+
+void launch_modek(int precision, const void* a, bool eye, int64_t s1, int64_t dout, int64_t din,
+                  int64_t s3, c128 alpha, const void* x, int64_t xes, int64_t xcs, c128 beta,
+                  void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s) {
+  const int64_t len = s1 * dout * s3;
+  if (len == 0 || ncols == 0) return;
+  const size_t esz = precision == QOB_C128 ? 16 : 8;
+  if (ncols > 65535) {  // grid.y limit: split the vectors
+    for (int64_t c0 = 0; c0 < ncols; c0 += 65535)
+      launch_modek(precision, a, eye, s1, dout, din, s3, alpha, (const char*)x + c0 * xcs * esz, xes, xcs,
+                   beta, (char*)y + c0 * ycs * esz, yes, ycs, std::min<int64_t>(65535, ncols - c0), s);
+    return;
+  }
+  dim3 grid(blocks_for(len, 256), (unsigned)ncols);
+  if (precision == QOB_C128) {
+    if (eye)
+      k_modek<double2, double, true><<<grid, 256, 0, s>>>(nullptr, s1, dout, din, s3, (const double2*)x, xes,
+                                                          xcs, (double2*)y, yes, ycs, ncols, alpha.re,
+                                                          alpha.im, beta.re, beta.im);
+    else
+      k_modek<double2, double, false><<<grid, 256, 0, s>>>((const double2*)a, s1, dout, din, s3,
+                                                           (const double2*)x, xes, xcs, (double2*)y, yes,
+                                                           ycs, ncols, alpha.re, alpha.im, beta.re, beta.im);
+  } else {
+    if (eye)
+      k_modek<float2, float, true><<<grid, 256, 0, s>>>(nullptr, s1, dout, din, s3, (const float2*)x, xes, xcs,
+                                                        (float2*)y, yes, ycs, ncols, alpha.re, alpha.im,
+                                                        beta.re, beta.im);
+    else
+      k_modek<float2, float, false><<<grid, 256, 0, s>>>((const float2*)a, s1, dout, din, s3,
+                                                         (const float2*)x, xes, xcs, (float2*)y, yes, ycs,
+                                                         ncols, alpha.re, alpha.im, beta.re, beta.im);
+  }
+  QOB_CUDA(cudaGetLastError());
+}
+
+// result: interleaved complex dot (norm: sqrt of the real part in out[0]).
+void reduce_dot(Context& ctx, int precision, const void* x, const void* y, int64_t n, bool norm,
+                double* out, cudaStream_t s) {
+  if (ctx.reduce_buf.bytes < (kRedBlocks + 1) * sizeof(double2))
+    ctx.reduce_buf.alloc((kRedBlocks + 1) * sizeof(double2));
+  if (!ctx.reduce_host) QOB_CUDA(cudaMallocHost(&ctx.reduce_host, sizeof(double2)));
+  double2* part = (double2*)ctx.reduce_buf.p;
+  double2* res = part + kRedBlocks;
+  if (precision == QOB_C128)
+    k_dot_partial<double2><<<kRedBlocks, kRedThreads, 0, s>>>((const double2*)x, (const double2*)y, n, part);
+  else
+    k_dot_partial<float2><<<kRedBlocks, kRedThreads, 0, s>>>((const float2*)x, (const float2*)y, n, part);
+  QOB_CUDA(cudaGetLastError());
+  k_dot_final<<<1, kRedThreads, 0, s>>>(part, kRedBlocks, res);
+  QOB_CUDA(cudaGetLastError());
+  QOB_CUDA(cudaMemcpyAsync(ctx.reduce_host, res, sizeof(double2), cudaMemcpyDeviceToHost, s));
+  QOB_CUDA(cudaStreamSynchronize(s));
+  const double2 r = *(const double2*)ctx.reduce_host;
+  if (norm) {
+    out[0] = sqrt(r.x);
+  } else {
+    out[0] = r.x;
+    out[1] = r.y;
+  }
+}
+
+}  // namespace qob

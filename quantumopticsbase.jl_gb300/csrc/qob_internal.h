@@ -1,0 +1,281 @@
+// qob_internal.h -- internal types of libqobgpu: the operator tree mirrored
+// from the reference's operator objects, and the compiled device form
+// ("plan") that the kernels execute.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "qobgpu.h"
+
+namespace qob {
+
+// ---------------------------------------------------------------------------
+// complex scalars (interleaved re, im), usable on host and device
+// ---------------------------------------------------------------------------
+struct c128 {
+  double re, im;
+};
+struct c64 {
+  float re, im;
+};
+
+__host__ __device__ inline c128 cmul(c128 a, c128 b) {
+  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+__host__ __device__ inline c128 cadd(c128 a, c128 b) { return {a.re + b.re, a.im + b.im}; }
+inline bool is_zero(c128 a) { return a.re == 0.0 && a.im == 0.0; }
+inline bool is_one(c128 a) { return a.re == 1.0 && a.im == 0.0; }
+inline c128 cconj(c128 a) { return {a.re, -a.im}; }
+
+// ---------------------------------------------------------------------------
+// errors: thrown inside the library, turned into status codes at the C ABI
+// ---------------------------------------------------------------------------
+struct Error {
+  int code;
+  std::string msg;
+};
+[[noreturn]] void fail(int code, const std::string& msg);
+void cuda_check(cudaError_t e, const char* what);
+#define QOB_CUDA(call) ::qob::cuda_check((call), #call)
+
+// ---------------------------------------------------------------------------
+// operator tree (host)
+// ---------------------------------------------------------------------------
+enum class Kind { Sparse, Dense, Eye, LazyTensor, LazySum, LazyProduct };
+
+struct OpNode {
+  Kind kind;
+  int64_t m = 0, n = 0;  // shape after adjoint: length(basis_l) x length(basis_r)
+  bool adjoint = false;
+  int src_dtype = QOB_C128;
+  // Sparse: stored CSC (0-based), pre-adjoint; Dense: stored column-major.
+  int64_t sm = 0, sn = 0;
+  std::vector<int64_t> colptr, rowval;
+  std::vector<c128> vals;
+  // lazy operators
+  std::vector<int64_t> shape_l, shape_r;  // composite shapes (LazyTensor)
+  std::vector<int> sites;                 // 0-based subsystem of each factor
+  std::vector<std::shared_ptr<OpNode>> ops;
+  c128 factor{1.0, 0.0};
+  std::vector<c128> factors;  // LazySum
+  uint64_t factors_version = 0;
+};
+using NodeP = std::shared_ptr<OpNode>;
+
+// ---------------------------------------------------------------------------
+// compiled device form
+// ---------------------------------------------------------------------------
+constexpr int kMaxBlocks = 4;   // runs of consecutive subsystems per group
+constexpr int kMaxSites = 32;   // subsystems of a composite basis on the device
+
+// One merged local operator: all LazyTensor terms with the same support.
+// The local row of output index J is sum_b ((J / div_b) % mod_b) * lstride_b;
+// its stored entries give input offsets relative to the row's base index.
+struct GGroup {
+  int32_t nblk;
+  int32_t nrows;
+  int32_t rowptr_off;  // into rowptr[]; rowptr values are absolute entry indices
+  int32_t support_lo;  // bit mask of support subsystems (non-square bases)
+  uint32_t div[kMaxBlocks];
+  uint32_t mod[kMaxBlocks];
+  uint32_t lstride[kMaxBlocks];
+  uint32_t support_hi;
+  uint32_t pad_;
+  uint64_t mdiv[kMaxBlocks];  // Lemire magic numbers of div / mod
+  uint64_t mmod[kMaxBlocks];
+};
+
+static_assert(sizeof(GGroup) % 8 == 0, "GGroup is copied to shared memory in 8-byte words");
+
+// Per-subsystem data for bases whose left and right shapes differ.
+struct SiteTable {
+  int32_t nsites;
+  uint32_t dout[kMaxSites];
+  uint32_t sout[kMaxSites];
+  uint32_t din[kMaxSites];
+  uint32_t sin[kMaxSites];
+  uint64_t msout[kMaxSites];
+  uint64_t mdout[kMaxSites];
+};
+
+// Kernel-side view of a gather plan for one scalar type.
+struct GatherView {
+  int64_t m;  // output length
+  int64_t n;  // input length
+  int32_t ngroups;
+  int32_t square;
+  int32_t real_vals;
+  int32_t has_diag;
+  const GGroup* groups;
+  const int32_t* rowptr;
+  const int32_t* coloff;
+  const void* vals;  // double / double2 / float / float2 by precision and real_vals
+  const void* diag;  // same element type as vals, length m
+};
+
+// A host-side record of how each stored entry is made from the terms, so a
+// change of the LazySum factors only re-evaluates values (set_factors).
+struct Contribution {
+  int32_t term;   // flattened term index
+  int32_t slot;   // entry index (>= 0) or -(diag slot + 1)
+  c128 pv;        // product of factor values (without the term coefficient)
+};
+
+struct TermCoef {
+  int32_t top;    // index into the root LazySum's factors, or -1
+  c128 inner;     // product of inner factors (LazyTensor factor, nested sums)
+};
+
+struct DeviceBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DeviceBuf() = default;
+  DeviceBuf(const DeviceBuf&) = delete;
+  DeviceBuf& operator=(const DeviceBuf&) = delete;
+  DeviceBuf(DeviceBuf&& o) noexcept : p(o.p), bytes(o.bytes) {
+    o.p = nullptr;
+    o.bytes = 0;
+  }
+  DeviceBuf& operator=(DeviceBuf&& o) noexcept {
+    std::swap(p, o.p);
+    std::swap(bytes, o.bytes);
+    return *this;
+  }
+  ~DeviceBuf();
+  void alloc(size_t b);
+  void upload(const void* host, size_t b);
+};
+
+struct GatherPlan {
+  int64_t m = 0, n = 0;
+  bool square = true;
+  bool real_vals = true;
+  bool has_diag = false;
+  int precision = QOB_C128;
+  int ngroups = 0;
+  int64_t nentries = 0;
+  // device arrays
+  DeviceBuf groups, rowptr, coloff, vals, diag;
+  DeviceBuf dgroups, dvals;  // diagonal sources: groups + local diagonal tables
+  int ndgroups = 0;
+  SiteTable sites{};
+  // host record for coefficient updates
+  std::vector<TermCoef> terms;
+  std::vector<Contribution> contrib;
+  std::vector<int64_t> dslot_count;
+  int64_t ndslots = 0;
+  std::shared_ptr<void> host_rec;  // merged-slot record used by set_factors
+  GatherView view() const;
+};
+
+// Dense full-space term (GEMM / GEMV pass) or a mode-k sequence.
+struct DensePass {
+  TermCoef coef;
+  int64_t m, n;
+  DeviceBuf a;  // m x n column-major in the plan's precision (already transposed for RIGHT)
+};
+
+struct ModekStep {
+  int site;
+  int64_t dout, din;
+  DeviceBuf a;  // dout x din column-major
+  bool eye = false;
+};
+struct ModekPass {
+  TermCoef coef;
+  std::vector<int64_t> shape_in, shape_out;
+  std::vector<ModekStep> steps;
+};
+
+struct Plan;
+struct SubPass {
+  TermCoef coef;
+  std::unique_ptr<Plan> plan;
+};
+
+struct Plan {
+  enum class Kind { Sum, Product } kind = Kind::Sum;
+  int side = QOB_LEFT;
+  int precision = QOB_C128;
+  int64_t m = 0, n = 0;  // rows of the output vectors / of the input vectors
+  // Sum
+  std::unique_ptr<GatherPlan> gather;
+  std::vector<DensePass> dense;
+  std::vector<ModekPass> modek;
+  std::vector<SubPass> subs;
+  int nterms_total = 0;
+  // Product
+  c128 pfactor{1.0, 0.0};
+  std::vector<std::unique_ptr<Plan>> chain;  // in application order
+  // dependency record: (node, factors_version) of every LazySum inside
+  std::vector<std::pair<const OpNode*, uint64_t>> deps;
+  const OpNode* root = nullptr;
+};
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct Workspace {
+  std::vector<DeviceBuf> slots;
+  void* get(size_t slot, size_t bytes);
+};
+
+struct Context {
+  int device = 0;
+  int num_sms = 0;
+  std::string err;
+  Workspace ws;
+  DeviceBuf reduce_buf;
+  void* reduce_host = nullptr;  // pinned
+  DeviceBuf host_x, host_y;     // staging for qob_mul_host
+  ~Context();
+};
+
+// plan.cu
+std::unique_ptr<Plan> compile_plan(Context& ctx, const NodeP& op, int side, int precision);
+void refresh_coefficients(Plan& plan, const OpNode& root);
+bool plan_is_current(const Plan& plan);
+
+// kernels (launchers)
+void launch_gather(const GatherPlan& g, int precision, const void* x, int64_t xes, int64_t xcs,
+                   void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta,
+                   cudaStream_t s);
+void launch_build_diag(const GatherPlan& g, cudaStream_t s);
+void launch_scale(int precision, void* y, int64_t rows, int64_t cols, int64_t ld_row,
+                  int64_t ld_col, c128 beta, cudaStream_t s);
+void launch_dense(int precision, const void* a, int64_t m, int64_t n, c128 alpha, const void* x,
+                  int64_t xes, int64_t xcs, c128 beta, void* y, int64_t yes, int64_t ycs,
+                  int64_t ncols, cudaStream_t s);
+void launch_modek(int precision, const void* a, bool eye, int64_t s1, int64_t dout, int64_t din,
+                  int64_t s3, c128 alpha, const void* x, int64_t xes, int64_t xcs, c128 beta,
+                  void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s);
+void launch_axpby(int precision, const void* x, int64_t xes, int64_t xcs, c128 alpha, void* y,
+                  int64_t yes, int64_t ycs, c128 beta, int64_t len, int64_t ncols,
+                  cudaStream_t s);
+void reduce_dot(Context& ctx, int precision, const void* x, const void* y, int64_t n, bool norm,
+                double* out, cudaStream_t s);
+
+// execution (apply.cu)
+void apply_plan(Context& ctx, Plan& plan, c128 alpha, const void* x, int64_t xes, int64_t xcs,
+                c128 beta, void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s,
+                int ws_base);
+
+// Lemire, Kaser & Kurz (2019) "Faster remainder by direct computation":
+// for 32-bit n and d > 1, n / d == umulhi64(M, n) and n % d ==
+// umulhi64((M * n) mod 2^64, d) with M = floor((2^64 - 1) / d) + 1.
+inline uint64_t lemire_magic(uint32_t d) { return d <= 1 ? 0 : (~uint64_t(0)) / d + 1; }
+
+}  // namespace qob
+
+struct qob_ctx {
+  qob::Context c;
+};
+struct qob_op {
+  qob::NodeP node;
+  std::unique_ptr<qob::Plan> plans[2][2];  // [side][precision]
+};

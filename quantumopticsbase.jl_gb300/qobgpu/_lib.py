@@ -1,0 +1,79 @@
+"""ctypes binding of libqobgpu.so (declared in include/qobgpu.h).
+
+There is no fallback: if the library is missing the import of the device layer
+fails with an error that says how to build it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libqobgpu.so")
+
+QOB_OK = 0
+QOB_ERR_DIM = 1
+QOB_ERR_ALIAS = 2
+QOB_ERR_UNSUPPORTED = 3
+QOB_ERR_ARG = 4
+QOB_ERR_CUDA = 5
+QOB_ERR_OOM = 6
+QOB_ERR_TIMEOUT = 7
+QOB_ERR_STATE = 8
+QOB_C128 = 0
+QOB_C64 = 1
+QOB_LEFT = 0
+QOB_RIGHT = 1
+
+VP = C.c_void_p
+I64 = C.c_int64
+I64P = C.POINTER(C.c_int64)
+DP = C.POINTER(C.c_double)
+D = C.c_double
+I = C.c_int
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "qob_version": (I, []),
+    "qob_create": (I, [C.POINTER(VP), I, C.c_uint]),
+    "qob_destroy": (I, [VP]),
+    "qob_last_error": (C.c_char_p, [VP]),
+    "qob_op_sparse": (I, [VP, I64, I64, I64P, I64P, VP, I, I, C.POINTER(VP)]),
+    "qob_op_dense": (I, [VP, I64, I64, VP, I64, I, I, C.POINTER(VP)]),
+    "qob_op_eye": (I, [VP, I64, I64, C.POINTER(VP)]),
+    "qob_op_lazytensor": (I, [VP, I, I64P, I64P, I, I64P, C.POINTER(VP), D, D, C.POINTER(VP)]),
+    "qob_op_lazysum": (I, [VP, I64, I64, I, DP, C.POINTER(VP), C.POINTER(VP)]),
+    "qob_op_lazyproduct": (I, [VP, I, C.POINTER(VP), D, D, C.POINTER(VP)]),
+    "qob_op_set_factors": (I, [VP, VP, DP]),
+    "qob_op_free": (I, [VP, VP]),
+    "qob_op_shape": (I, [VP, VP, I64P, I64P]),
+    "qob_op_prepare": (I, [VP, VP, I, I, I64P]),
+    "qob_mul": (I, [VP, I, I, VP, I, D, D, VP, I64, I64, I64, D, D, VP, I64, I64, I64, VP]),
+    "qob_mul_host": (I, [VP, I, I, VP, I, D, D, VP, I64, I64, D, D, VP, I64, I64]),
+    "qob_norm": (I, [VP, I, VP, I64, DP, VP]),
+    "qob_dot": (I, [VP, I, VP, VP, I64, DP, VP]),
+    "qob_expect": (I, [VP, VP, I, VP, I64, DP, VP]),
+}
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with `python -c \"import __graft_entry__ as g; g.build()\"` "
+                "(nvcc, sm_103a). There is no CPU fallback."
+            )
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return list(SIGNATURES)

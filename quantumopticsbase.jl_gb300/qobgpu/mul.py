@@ -1,0 +1,210 @@
+"""``mul_`` -- the reference's 5-argument ``mul!(result, a, b, alpha, beta)``.
+
+Dispatch follows the reference:
+* ``mul_(::Ket, op, ::Ket, α, β)``            op applied from the left to a ket
+* ``mul_(::Bra, ::Bra, op, α, β)``            a bra times op
+* ``mul_(::Operator, op, ::Operator, α, β)``  op times a dense operator (its columns)
+* ``mul_(::Operator, ::Operator, op, α, β)``  a dense operator times op (its rows)
+
+States whose data are CUDA ``torch`` tensors stay on the device (the path an
+ODE right-hand side uses); numpy data are copied to the device and back
+around the call.  Every call runs the CUDA kernels of libqobgpu.so; there is
+no host arithmetic on this path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from . import operators as O
+from .device import dtype_code, get_context, handle, raise_for
+from .states import Bra, Ket, StateVector
+
+
+def _is_torch(a) -> bool:
+    return type(a).__module__.startswith("torch")
+
+
+def _state_like(o) -> bool:
+    return isinstance(o, O.Operator) and (isinstance(o.data, np.ndarray) or _is_torch(o.data))
+
+
+def _np_dtype(a):
+    if _is_torch(a):
+        import torch
+
+        return np.complex64 if a.dtype == torch.complex64 else np.complex128
+    return np.complex64 if a.dtype == np.complex64 else np.complex128
+
+
+def _stream_ptr(device: int):
+    import torch
+
+    return C.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def _matrix_view(a):
+    """(rows, cols, ld) of a 1-D or column-major 2-D array/tensor."""
+    if a.ndim == 1:
+        return a.shape[0], 1, max(1, a.shape[0])
+    r, c = a.shape
+    if _is_torch(a):
+        st = a.stride()
+        if st[0] != 1 and r > 1:
+            raise O.ArgumentError("device operator data must be column-major (stride (1, ld))")
+        return r, c, max(1, st[1] if c > 1 else r)
+    if not a.flags.f_contiguous:
+        raise O.ArgumentError("host operator data must be Fortran-ordered")
+    return r, c, max(1, r)
+
+
+def _classify(result, a, b):
+    """(side, is_vector, op, x, y)"""
+    if isinstance(b, StateVector):
+        if not isinstance(b, Ket) or not isinstance(result, Ket):
+            raise O.ArgumentError("mul_(result::Ket, op, b::Ket) expected")
+        if result.basis != a.basis_l or b.basis != a.basis_r:
+            raise O.IncompatibleBases()
+        return L.QOB_LEFT, True, a, b.data, result.data
+    if isinstance(a, StateVector):
+        if not isinstance(a, Bra) or not isinstance(result, Bra):
+            raise O.ArgumentError("mul_(result::Bra, a::Bra, op) expected")
+        if a.basis != b.basis_l or result.basis != b.basis_r:
+            raise O.IncompatibleBases()
+        return L.QOB_RIGHT, True, b, a.data, result.data
+    if not isinstance(result, O.Operator) or not _state_like(result):
+        raise O.ArgumentError("result must be an Operator with dense data")
+    if a.basis_r != b.basis_l or result.basis_l != a.basis_l or result.basis_r != b.basis_r:
+        raise O.IncompatibleBases()
+    # the dense data operand is the state; the other one is applied to it
+    if _state_like(b) or not _state_like(a):
+        return L.QOB_LEFT, False, a, b.data, result.data
+    return L.QOB_RIGHT, False, b, a.data, result.data
+
+
+def mul_(result, a, b, alpha=1.0, beta=0.0, device: int | None = None):
+    """In place ``result = alpha * a * b + beta * result``; returns ``result``."""
+    side, is_vec, op, x, y = _classify(result, a, b)
+    alpha, beta = complex(alpha), complex(beta)
+    lib = L.lib()
+    if _is_torch(y):
+        import torch
+
+        dev = y.device.index if device is None else device
+        ctx = get_context(dev)
+        h = handle(ctx, op)
+        ydt = _np_dtype(y)
+        if not _is_torch(x) or x.device != y.device or _np_dtype(x) != ydt:
+            xt = torch.as_tensor(np.asarray(x) if not _is_torch(x) else x, device=y.device)
+            x = xt.to(torch.complex64 if ydt == np.complex64 else torch.complex128)
+            if x.ndim == 2 and x.stride(0) != 1 and x.shape[0] > 1:
+                x = x.t().contiguous().t()
+        xr, xc, xld = _matrix_view(x)
+        yr, yc, yld = _matrix_view(y)
+        if side == L.QOB_RIGHT and x.ndim == 1:
+            xr, xc, xld = 1, x.shape[0], 1
+            yr, yc, yld = 1, y.shape[0], 1
+        rc = lib.qob_mul(ctx.ptr, side, int(is_vec), h.ptr, dtype_code(ydt), alpha.real, alpha.imag,
+                         C.c_void_p(x.data_ptr()), xr, xc, xld, beta.real, beta.imag, C.c_void_p(y.data_ptr()),
+                         yr, yc, yld, _stream_ptr(dev))
+        raise_for(rc, ctx)
+        return result
+    # host arrays: copy in, apply on the device, copy back
+    dev = 0 if device is None else device
+    ctx = get_context(dev)
+    h = handle(ctx, op)
+    ydt = _np_dtype(y)
+    xh = np.asfortranarray(np.asarray(x.detach().cpu().numpy() if _is_torch(x) else x), dtype=ydt)
+    if not (isinstance(y, np.ndarray) and (y.flags.f_contiguous or y.ndim == 1)):
+        raise O.ArgumentError("host result data must be a Fortran-ordered numpy array")
+    if side == L.QOB_LEFT:
+        xr, xc = (xh.shape[0], 1) if xh.ndim == 1 else xh.shape
+        yr, yc = (y.shape[0], 1) if y.ndim == 1 else y.shape
+    else:
+        xr, xc = (1, xh.shape[0]) if xh.ndim == 1 else xh.shape
+        yr, yc = (1, y.shape[0]) if y.ndim == 1 else y.shape
+    rc = lib.qob_mul_host(ctx.ptr, side, int(is_vec), h.ptr, dtype_code(ydt), alpha.real, alpha.imag,
+                          xh.ctypes.data_as(C.c_void_p), xr, xc, beta.real, beta.imag, y.ctypes.data_as(C.c_void_p),
+                          yr, yc)
+    raise_for(rc, ctx)
+    return result
+
+
+def apply_alloc(op, psi: Ket) -> Ket:
+    """``op * psi`` (src/operators_dense.jl:111-115): allocate, then mul_."""
+    if _is_torch(psi.data):
+        import torch
+
+        out = torch.zeros(len(op.basis_l), dtype=psi.data.dtype, device=psi.data.device)
+    else:
+        out = np.zeros(len(op.basis_l), dtype=_np_dtype(psi.data))
+    return mul_(Ket(op.basis_l, out), op, psi)
+
+
+def apply_alloc_bra(psi: Bra, op) -> Bra:
+    if _is_torch(psi.data):
+        import torch
+
+        out = torch.zeros(len(op.basis_r), dtype=psi.data.dtype, device=psi.data.device)
+    else:
+        out = np.zeros(len(op.basis_r), dtype=_np_dtype(psi.data))
+    return mul_(Bra(op.basis_r, out), psi, op)
+
+
+def to_device(obj, device: int = 0, dtype=None):
+    """Copy of a Ket/Bra/Operator(dense) with column-major CUDA tensor data."""
+    import torch
+
+    d = obj.data
+    a = d.detach().cpu().numpy() if _is_torch(d) else O._to_dense_array(d) if isinstance(obj, O.Operator) else d
+    if dtype is not None:
+        a = a.astype(dtype)
+    t = torch.as_tensor(np.ascontiguousarray(a.T) if a.ndim == 2 else np.ascontiguousarray(a),
+                        device=f"cuda:{device}")
+    if a.ndim == 2:
+        t = t.t()  # column-major view of shape (m, n)
+    if isinstance(obj, O.Operator):
+        return O.Operator(obj.basis_l, obj.basis_r, t)
+    return type(obj)(obj.basis, t)
+
+
+def _vec_ptr(x):
+    if _is_torch(x):
+        if not x.is_contiguous():
+            raise O.ArgumentError("device state must be contiguous")
+        return C.c_void_p(x.data_ptr()), x.device.index
+    raise O.ArgumentError("norm/dot/expect on the device need CUDA tensor data")
+
+
+def norm(psi: StateVector) -> float:
+    """FP64 norm (src/states.jl:89), accumulated in double even for ComplexF32 data."""
+    p, dev = _vec_ptr(psi.data)
+    ctx = get_context(dev)
+    out = (C.c_double * 1)()
+    raise_for(L.lib().qob_norm(ctx.ptr, dtype_code(_np_dtype(psi.data)), p, psi.data.shape[0], out,
+                               _stream_ptr(dev)), ctx)
+    return out[0]
+
+
+def dot(x: StateVector, y: StateVector) -> complex:
+    """sum(conj(x) .* y) in FP64."""
+    px, dev = _vec_ptr(x.data)
+    py, _ = _vec_ptr(y.data)
+    ctx = get_context(dev)
+    out = (C.c_double * 2)()
+    raise_for(L.lib().qob_dot(ctx.ptr, dtype_code(_np_dtype(x.data)), px, py, x.data.shape[0], out,
+                              _stream_ptr(dev)), ctx)
+    return complex(out[0], out[1])
+
+
+def expect(op, psi: Ket) -> complex:
+    """``expect(op, psi) = <psi|op|psi>`` (src/operators.jl:119) in FP64."""
+    p, dev = _vec_ptr(psi.data)
+    ctx = get_context(dev)
+    h = handle(ctx, op)
+    out = (C.c_double * 2)()
+    raise_for(L.lib().qob_expect(ctx.ptr, h.ptr, dtype_code(_np_dtype(psi.data)), p, psi.data.shape[0], out,
+                                 _stream_ptr(dev)), ctx)
+    return complex(out[0], out[1])

@@ -1,0 +1,245 @@
+"""GPU parity: libqobgpu (through the C ABI via the qobgpu mirror) against the
+oracle (restated reference mul!) on the same seeded inputs.
+
+Tolerances (relative l2, stated per test): 1e-12 for ComplexF64, 1e-5 for the
+ComplexF32 mode, as the plain form and the precision mode require.
+"""
+import numpy as np
+import pytest
+
+import oracle as OR
+import qobgpu as Q
+from helpers import host_copy, rand_op, rand_state, rel_l2
+from qobgpu import operators as O
+from qobgpu.hamiltonians import (heisenberg_chain, jaynes_cummings, jaynes_cummings_sparse,
+                                 random_density_columns, two_mode_cavity)
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 1e-5
+AL, BE = 0.7 - 0.2j, 0.3
+
+
+def _is_state(x):
+    return isinstance(x, Q.states.StateVector) or (isinstance(x, O.Operator) and isinstance(x.data, np.ndarray))
+
+
+def gpu_mul(result, a, b, alpha=1.0, beta=0.0, dtype=np.complex128):
+    """mul_ on device copies of the state operands; returns the host result data."""
+    from qobgpu.mul import mul_, to_device
+
+    r = to_device(result, dtype=dtype)
+    if isinstance(b, Q.states.StateVector) or (_is_state(b) and not isinstance(a, Q.states.StateVector)):
+        b = to_device(b, dtype=dtype)
+    else:
+        a = to_device(a, dtype=dtype)
+    mul_(r, a, b, alpha, beta)
+    return host_copy(r)
+
+
+def check(result, a, b, alpha, beta, tol=TOL64, dtype=np.complex128):
+    ref = OR.mul(result, a, b, alpha, beta)
+    got = gpu_mul(result, a, b, alpha, beta, dtype)
+    err = rel_l2(got, ref)
+    assert err < tol, f"relative l2 error {err:.3e} >= {tol:g}"
+    return err
+
+
+# ---------------------------------------------------------------- benchmark Hamiltonians
+def test_jaynes_cummings_ket_fp64_and_fp32():
+    H = jaynes_cummings(15, 15, seed=1)
+    rng = Q.Rng(100)
+    psi, out = rand_state(rng, H.basis_r), rand_state(rng, H.basis_l)
+    check(out, H, psi, AL, BE, TOL64)
+    check(out, H, psi, AL, BE, TOL32, np.complex64)
+    check(out, H, psi, AL, 0.0, TOL64)
+    check(out, H, psi, AL, 1.0, TOL64)
+
+
+def test_heisenberg_14_spins_batch():
+    H = heisenberg_chain(14, seed=3)
+    rng = Q.Rng(101)
+    nb = 8
+    X = O.Operator(H.basis_r, Q.GenericBasis(nb), rng.kets_data(len(H.basis_r), nb))
+    Y = O.Operator(H.basis_l, Q.GenericBasis(nb), rng.kets_data(len(H.basis_l), nb))
+    check(Y, H, X, AL, BE, TOL64)
+    check(Y, H, X, AL, BE, TOL32, np.complex64)
+    psi, out = rand_state(rng, H.basis_r), rand_state(rng, H.basis_l)
+    check(out, H, psi, AL, BE, TOL64)
+
+
+def test_heisenberg_operator_both_sides_8_spins():
+    H = heisenberg_chain(8, seed=4)
+    rng = Q.Rng(102)
+    rho = rand_op(rng, H.basis_r, H.basis_r)
+    r0 = rand_op(rng, H.basis_l, H.basis_r)
+    check(r0, H, rho, AL, BE, TOL64)
+    check(r0, rho, H, AL, BE, TOL64)
+    check(r0, rho, H, AL, BE, TOL32, np.complex64)
+    bra, rb = rand_state(rng, H.basis_l, Q.Bra), rand_state(rng, H.basis_r, Q.Bra)
+    check(rb, bra, H, AL, BE, TOL64)
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, TOL64), (np.complex64, TOL32)])
+def test_sparse_operator_spmv_spmm(dtype, tol):
+    S = jaynes_cummings_sparse(31, 63, seed=1)
+    rng = Q.Rng(103)
+    n = len(S.basis_l)
+    psi, out = rand_state(rng, S.basis_r), rand_state(rng, S.basis_l)
+    check(out, S, psi, AL, BE, tol, dtype)
+    rho = O.Operator(S.basis_r, Q.GenericBasis(256), random_density_columns(n, 256, seed=5))
+    r0 = O.Operator(S.basis_l, Q.GenericBasis(256), np.asfortranarray(rng.complex_normal(n * 256).reshape(n, 256, order="F")))
+    check(r0, S, rho, AL, BE, tol, dtype)
+
+
+def test_two_mode_cavities():
+    rng = Q.Rng(104)
+    for k in range(4):
+        n1, n2 = rng.integers(2, 8, 64)
+        H = two_mode_cavity(int(n1), int(n2), seed=10 + k)
+        psi, out = rand_state(rng, H.basis_r), rand_state(rng, H.basis_l)
+        check(out, H, psi, AL, BE, TOL64)
+        check(out, H, psi, AL, BE, TOL32, np.complex64)
+
+
+# ---------------------------------------------------------------- reference test identities
+def lt_bases():
+    b1a, b1b = Q.GenericBasis(2), Q.GenericBasis(3)
+    b2a, b2b = Q.GenericBasis(1), Q.GenericBasis(4)
+    b3a, b3b = Q.GenericBasis(6), Q.GenericBasis(5)
+    return (b1a, b1b, b2a, b2b, b3a, b3b), Q.tensor_basis(b1a, b2a, b3a), Q.tensor_basis(b1b, b2b, b3b)
+
+
+@pytest.mark.parametrize("sparse_factors", [False, True])
+def test_lazytensor_mixed_precision_adjoint(sparse_factors):
+    rng = Q.Rng(105)
+    (b1a, b1b, b2a, b2b, b3a, b3b), bl, br = lt_bases()
+    facs = (rand_op(rng, b1a, b1b, np.complex64), O.dagger(rand_op(rng, b2b, b2a)), O.dagger(rand_op(rng, b3b, b3a)))
+    if sparse_factors:
+        facs = tuple(O.sparse(f) for f in facs)
+    op = O.LazyTensor(bl, br, (1, 2, 3), facs, 0.1)
+    psi, out = rand_state(rng, br), rand_state(rng, bl)
+    check(out, op, psi, 1.0, 0.0, TOL64)
+    check(out, op, psi, 1.5, 2.1, TOL64)
+    bra, rb = rand_state(rng, bl, Q.Bra), rand_state(rng, br, Q.Bra)
+    check(rb, bra, op, 1.5, 2.1, TOL64)
+    st, r0 = rand_op(rng, br, Q.GenericBasis(13)), rand_op(rng, bl, Q.GenericBasis(13))
+    check(r0, op, st, 1.5, 2.1, TOL64)
+    st, r0 = rand_op(rng, Q.GenericBasis(17), bl), rand_op(rng, Q.GenericBasis(17), br)
+    check(r0, st, op, 1.5, 2.1, TOL64)
+
+
+def test_explicit_isometries_nan_alpha_beta():
+    from test_oracle import iso_ops
+
+    rng = Q.Rng(106)
+    bl, br, n1, n1_sp, n1_de = iso_ops()
+    state, out = rand_op(rng, br, br), rand_op(rng, bl, br)
+    nan_out = O.Operator(bl, br, np.full(out.data.shape, np.nan + 0j, order="F"))
+    for op in (n1, n1_sp, n1_de):
+        check(out, op, state, -0.8, 1.3, TOL64)
+        got = gpu_mul(nan_out, op, state, -0.8, 0.0)
+        assert np.all(np.isfinite(got))
+        assert rel_l2(got, OR.mul(nan_out, op, state, -0.8, 0.0)) < TOL64
+        assert np.array_equal(gpu_mul(out, op, state, 0.0, 1.3), OR.mul(out, op, state, 0.0, 1.3))
+        assert np.all(gpu_mul(nan_out, op, state, 0.0, 0.0) == 0)
+    st2 = rand_op(rng, bl, bl)
+    for op in (n1, n1_sp, n1_de):
+        check(out, st2, op, -0.8, 1.3, TOL64)
+
+
+def test_lazysum_dense_terms_and_empty():
+    rng = Q.Rng(107)
+    _, bl, br = lt_bases()
+    ops = tuple(rand_op(rng, bl, br) for _ in range(3))
+    op = O.LazySum([0.1, 0.3, 1.2], ops)
+    psi, out = rand_state(rng, br), rand_state(rng, bl)
+    check(out, op, psi, 1.5, 2.1, TOL64)
+    zero = O.LazySum(bl, br)
+    assert rel_l2(gpu_mul(out, zero, psi, 1.5, 2.1), 2.1 * out.data) < 1e-15
+    nan_out = Q.Ket(bl, np.full(len(bl), np.nan + 0j))
+    assert np.all(gpu_mul(nan_out, zero, psi, 1.0, 0.0) == 0)
+    st = rand_op(rng, br, br)
+    res = O.Operator(bl, br, np.full((len(bl), len(br)), np.nan + 0j, order="F"))
+    got = gpu_mul(res, op, st, 1.0, 0.0)
+    assert rel_l2(got, OR.mul(res, op, st, 1.0, 0.0)) < TOL64
+
+
+@pytest.mark.parametrize("nops", [1, 2, 3])
+def test_lazyproduct(nops):
+    rng = Q.Rng(108 + nops)
+    bs = [Q.GenericBasis(k) for k in (3, 5, 4, 6)]
+    ops = [rand_op(rng, bs[i], bs[i + 1]) for i in range(nops)]
+    op = O.LazyProduct(tuple(ops), factor=0.5 - 0.1j)
+    psi, out = rand_state(rng, bs[nops]), rand_state(rng, bs[0])
+    check(out, op, psi, 1.5, 2.1, TOL64)
+    bra, rb = rand_state(rng, bs[0], Q.Bra), rand_state(rng, bs[nops], Q.Bra)
+    check(rb, bra, op, 1.5, 2.1, TOL64)
+
+
+def test_sparse_adjoint_and_big_dense():
+    rng = Q.Rng(110)
+    b = Q.GenericBasis(300)
+    S = O.sparse(rand_op(rng, b, b, density=0.05))
+    psi, out = rand_state(rng, b), rand_state(rng, b)
+    check(out, O.dagger(S), psi, 1.5, 2.1, TOL64)
+    Dn = rand_op(rng, b, b)  # > 256: the dense pass
+    check(out, Dn, psi, 1.5, 2.1, TOL64)
+    check(out, O.dagger(Dn), psi, 1.5, 2.1, TOL64)
+
+
+def test_large_dense_factor_mode_products():
+    """LazyTensor with two 200x200 dense factors: too large to merge, runs as
+    the mode-product chain of _tp_sum_matmul!."""
+    rng = Q.Rng(111)
+    b1, b2, b3 = Q.GenericBasis(200), Q.GenericBasis(3), Q.GenericBasis(200)
+    b = Q.tensor_basis(b1, b2, b3)
+    op = O.LazyTensor(b, b, (1, 3), (rand_op(rng, b1, b1), rand_op(rng, b3, b3)), 0.3)
+    from qobgpu.device import prepare
+
+    info = prepare(op)
+    assert info["extra_passes"] == 1
+    psi, out = rand_state(rng, b), rand_state(rng, b)
+    check(out, op, psi, 1.5, 2.1, TOL64)
+
+
+# ---------------------------------------------------------------- errors and state
+def test_dimension_and_alias_errors():
+    from qobgpu.mul import mul_, to_device
+
+    H = jaynes_cummings(3, 3)
+    rng = Q.Rng(112)
+    psi = to_device(rand_state(rng, H.basis_r))
+    with pytest.raises(O.ArgumentError):
+        mul_(psi, H, psi, 1.0, 0.0)  # output aliased with input
+    wrong = to_device(Q.Ket(Q.GenericBasis(len(H.basis_l)), np.zeros(len(H.basis_l), complex)))
+    with pytest.raises(O.IncompatibleBases):
+        mul_(wrong, H, psi)
+
+
+def test_set_factors_time_dependent_sum():
+    H = heisenberg_chain(6, seed=7)
+    td = O.TimeDependentSum([(lambda t, k=k: np.cos(t + k)) for k in range(len(H.operators))], H.operators)
+    rng = Q.Rng(113)
+    psi, out = rand_state(rng, H.basis_r), rand_state(rng, H.basis_l)
+    for t in (0.0, 0.3, 1.1):
+        td.set_time(t)
+        ref = OR.mul(out, td.static_op, psi, AL, BE)
+        got = gpu_mul(out, td, psi, AL, BE)
+        assert rel_l2(got, ref) < TOL64
+
+
+def test_norm_dot_expect_fp64():
+    from qobgpu.mul import dot, expect, norm, to_device
+
+    H = jaynes_cummings(15, 15)
+    rng = Q.Rng(114)
+    a, b = rand_state(rng, H.basis_r), rand_state(rng, H.basis_r)
+    da, db = to_device(a), to_device(b)
+    assert abs(norm(da) - np.linalg.norm(a.data)) < 1e-14
+    assert abs(dot(da, db) - np.vdot(a.data, b.data)) < 1e-14
+    D = O.dense(H).data
+    assert abs(expect(H, da) - np.vdot(a.data, D @ a.data)) < 1e-12 * abs(np.vdot(a.data, D @ a.data))
+    f = to_device(a, dtype=np.complex64)
+    assert abs(norm(f) - np.linalg.norm(a.data.astype(np.complex64).astype(np.complex128))) < 1e-12

@@ -1,0 +1,74 @@
+"""CPU tests of the host side: the C-ABI library loads and exports every symbol
+the header declares, the seeded generator is stable, and the magic-number
+division used by the kernels' index arithmetic is exact."""
+import os
+import re
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", f)).read()
+            names |= set(re.findall(r"^\s*(?:int|const char\*|void)\s+(qob_\w+)\s*\(", txt, re.M))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    import ctypes
+
+    import __graft_entry__ as g
+
+    g.build()
+    from qobgpu import _lib
+
+    lib = ctypes.CDLL(_lib.LIB_PATH)
+    names = declared_symbols()
+    assert len(names) >= 19
+    for n in sorted(names):
+        assert hasattr(lib, n), f"{n} declared in include/ but not exported"
+    assert set(_lib.SIGNATURES) == names
+
+
+def test_library_without_gpu_reports_cuda_error_not_crash():
+    import ctypes
+
+    import torch
+    from qobgpu import _lib
+
+    if torch.cuda.is_available():
+        return
+    p = ctypes.c_void_p()
+    assert _lib.lib().qob_create(ctypes.byref(p), 0, 0) == _lib.QOB_ERR_CUDA
+
+
+def test_rng_is_stable():
+    import qobgpu as Q
+
+    r = Q.Rng(1)
+    u = r.uniform(3)
+    assert np.allclose(u, Q.Rng(1).uniform(3))
+    assert 0 <= u.min() and u.max() < 1
+    k = Q.Rng(5).ket_data(64)
+    assert abs(np.linalg.norm(k) - 1) < 1e-14
+
+
+def test_lemire_division_exact():
+    """n / d and n % d via M = floor((2^64-1)/d) + 1 (Lemire, Kaser & Kurz 2019),
+    as the kernels compute them, for 32-bit n and d > 1."""
+    rng = np.random.default_rng(0)
+    ds = list(range(2, 70)) + [2 ** k for k in range(1, 31)] + list(rng.integers(2, 2 ** 31, 200))
+    ns = list(range(0, 300)) + [2 ** 31 - 1, 2 ** 32 - 1] + list(rng.integers(0, 2 ** 32, 300))
+    for d in ds:
+        d = int(d)
+        M = (2 ** 64 - 1) // d + 1
+        for n in ns:
+            n = int(n)
+            q = (M * n) >> 64
+            low = (M * n) & (2 ** 64 - 1)
+            r = (low * d) >> 64
+            assert q == n // d and r == n % d, (n, d)
