@@ -1,0 +1,413 @@
+#!/usr/bin/env python3
+"""LazySum·ket applies/s on GB300 for QuantumOpticsBase.jl's mul! hot path.
+
+Workload: the 14-spin open Heisenberg chain, H = Σ J(σxσx + σyσy + σzσz) +
+Σ h_i σz_i (dim 16384, 53 LazyTensor terms, J = 1, h_i ~ U(-1, 1)), applied as
+mul!(Y, H, X, α = 0.7 - 0.2i, β = 0.3) to batches of 64 normalised
+complex-Gaussian kets.  One step = one application to one 64-ket batch.
+Twenty distinct batches rotate (1280 kets, 640 MiB of input + output in
+ComplexF64, more than twice the 129 MB L2), so every step streams its kets from
+HBM.
+
+`value` is the plain ComplexF64 form, device-resident, replayed from a CUDA
+graph and timed with CUDA events on the launching stream.  `e2e` is the same
+metric through the C ABI's host-buffer call (qob_mul_host) with the kets copied
+from pinned host memory and the results copied back every step.  The
+ComplexF32 mode is reported beside it, with its error against the oracle.
+
+`--impl reference` times the CPU restatement of the reference mul! (the
+oracle port; Julia is not available) on all host threads, same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "quantumopticsbase.jl_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "LazySum·ket applies/s (14-spin Heisenberg, batch 64)"
+UNIT = "applies/s"
+NSPINS, BATCH, ROTATE = 14, 64, 20
+ALPHA, BETA = 0.7 - 0.2j, 0.3
+SEED_H = 3
+L2_NOTE = "20 distinct 64-ket batches rotate: 640 MiB (c128) / 320 MiB (c64) of in+out per rotation, > 2x the 129 MB L2"
+
+
+def config():
+    return {
+        "workload": "heisenberg14_lazysum_ket_batch64",
+        "dim": 2 ** NSPINS,
+        "terms": 3 * (NSPINS - 1) + NSPINS,
+        "batch_kets": BATCH,
+        "alpha": [ALPHA.real, ALPHA.imag],
+        "beta": [BETA, 0.0],
+        "l2": L2_NOTE,
+        "parallelism": "replicas",
+    }
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10000)
+    p.add_argument("--warmup", type=int, default=20)
+    p.add_argument("--impl", default="own", choices=["own", "reference"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-graph", action="store_true", help="direct launches (used for ncu captures)")
+    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    return p.parse_args()
+
+
+def read_json(path):
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples (SM clock, throttle reasons) tagged with host time."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.samples = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append((time.time(), [x.strip() for x in line.split(",")]))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        if not self.samples:
+            return None
+        inside = [s for t, s in self.samples if t0 <= t <= t1 + 0.15]
+        note = None
+        if not inside:  # timed region shorter than the sampling period: nearest samples
+            inside = [min(self.samples, key=lambda ts: abs(ts[0] - (t0 + t1) / 2))[1]]
+            note = "timed region shorter than the 100 ms sampling period; nearest sample"
+        mhz = [float(s[0]) for s in inside if s[0].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for s in inside for n, v in zip(names, s[3:7]) if v == "Active"})
+        out = {"sm_mhz": statistics.median(mhz) if mhz else None,
+               "sm_max_mhz": float(inside[0][1]) if inside[0][1].replace(".", "").isdigit() else None,
+               "reasons": reasons, "samples": len(inside)}
+        if note:
+            out["note"] = note
+        return out
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline(H, seconds: float):
+    """The oracle port (restated reference mul!) on this host: single thread,
+    kets applied one at a time until `seconds` pass; then all threads."""
+    import numpy as np
+
+    import oracle as OR
+    import qobgpu as Q
+
+    node = OR.build_node(H)
+    dim = len(H.basis_l)
+    rng = Q.Rng(99)
+    X = rng.kets_data(dim, 1)
+    Y = rng.kets_data(dim, 1)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        OR.mul_kets_threaded(node, ALPHA, X, BETA, Y, 1)
+        n += 1
+        if time.perf_counter() - t0 >= seconds and n >= 4:
+            break
+    single = n / (time.perf_counter() - t0)
+    threads = os.cpu_count() or 1
+    Xa = np.asfortranarray(np.repeat(X, threads * 2, axis=1))
+    Ya = np.asfortranarray(np.repeat(Y, threads * 2, axis=1))
+    t0 = time.perf_counter()
+    OR.mul_kets_threaded(node, ALPHA, Xa, BETA, Ya, threads)
+    allc = Xa.shape[1] / (time.perf_counter() - t0)
+    return {"value": single, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n} kets of the 14-spin Heisenberg LazySum, mul!(y, H, x, α, β) one ket at a time on one "
+                      f"thread (restated reference CPU path; Julia absent), {seconds:.0f} s bound",
+            "all_cores": {"value": allc, "cores": threads, "sample": f"{Xa.shape[1]} kets over {threads} threads"}}
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import numpy as np
+
+    import oracle as OR
+    import qobgpu as Q
+    from qobgpu.hamiltonians import heisenberg_chain
+
+    H = heisenberg_chain(NSPINS, seed=SEED_H)
+    node = OR.build_node(H)
+    threads = os.cpu_count() or 1
+    dim = len(H.basis_l)
+    rng = Q.Rng(98)
+    X = rng.kets_data(dim, threads)
+    Y = rng.kets_data(dim, threads)
+    for _ in range(args.warmup):
+        OR.mul_kets_threaded(node, ALPHA, X, BETA, Y, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        OR.mul_kets_threaded(node, ALPHA, X, BETA, Y, threads)
+    dt = time.perf_counter() - t0
+    value = threads * args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic (seeded complex-Gaussian kets)", "config": config(),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"each step applies H to {threads} kets, one per host thread "
+                                   "(restated reference CPU path; Julia absent)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def run_own(args, rank, world, local_rank):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import qobgpu as Q
+    from qobgpu import _lib as L
+    from qobgpu.device import dtype_code, get_context, handle, prepare, raise_for
+    from qobgpu.hamiltonians import heisenberg_chain
+
+    dev = local_rank
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+    lib = L.lib()
+    H = heisenberg_chain(NSPINS, seed=SEED_H)
+    ctx = get_context(dev)
+    hd = handle(ctx, H)
+    dim = len(H.basis_l)
+    stream = torch.cuda.Stream(dev)
+    sp = C.c_void_p(stream.cuda_stream)
+    plan = prepare(H, L.QOB_LEFT, np.complex128, dev)
+    sampler = ClockSampler(dev) if rank == 0 else None
+
+    gen = torch.Generator(device=f"cuda:{dev}")
+    gen.manual_seed(1234 + rank)
+
+    def batches(tdt):
+        xs, ys = [], []
+        for _ in range(ROTATE):
+            for lst in (xs, ys):
+                t = torch.randn(BATCH, dim, dtype=tdt, device=f"cuda:{dev}", generator=gen)
+                t /= torch.linalg.vector_norm(t, dim=1, keepdim=True)
+                lst.append(t.t())  # column-major dim x 64, ld = dim
+        return xs, ys
+
+    def mul_args(x, y, code):
+        return (ctx.ptr, L.QOB_LEFT, 0, hd.ptr, code, ALPHA.real, ALPHA.imag, C.c_void_p(x.data_ptr()), dim, BATCH,
+                dim, BETA, 0.0, C.c_void_p(y.data_ptr()), dim, BATCH, dim, sp)
+
+    def timed(tdt, code, steps, warmup):
+        xs, ys = batches(tdt)
+        argl = [mul_args(xs[b], ys[b], code) for b in range(ROTATE)]
+        with torch.cuda.stream(stream):
+            for i in range(warmup):
+                raise_for(lib.qob_mul(*argl[i % ROTATE]), ctx)
+        stream.synchronize()
+        n0 = lib.qob_kernel_launches()
+        graph = None
+        if not args.no_graph:
+            g = C.c_void_p()
+            reps, per = (steps // ROTATE, ROTATE) if steps % ROTATE == 0 and steps >= ROTATE else (1, steps)
+            raise_for(lib.qob_graph_begin(ctx.ptr, sp), ctx)
+            for i in range(per):
+                raise_for(lib.qob_mul(*argl[i % ROTATE]), ctx)
+            raise_for(lib.qob_graph_end(ctx.ptr, sp, C.byref(g)), ctx)
+            graph = g
+            launches = (lib.qob_kernel_launches() - n0) * reps
+            raise_for(lib.qob_graph_launch(ctx.ptr, graph, sp), ctx)  # one untimed replay
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t_host0 = time.time()
+        e0.record(stream)
+        if graph is not None:
+            for _ in range(reps):
+                raise_for(lib.qob_graph_launch(ctx.ptr, graph, sp), ctx)
+        else:
+            n1 = lib.qob_kernel_launches()
+            for i in range(steps):
+                raise_for(lib.qob_mul(*argl[i % ROTATE]), ctx)
+            launches = lib.qob_kernel_launches() - n1
+        e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize(dev)
+        t_host1 = time.time()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            import torch.distributed as dist
+
+            t = torch.tensor([ms], device=f"cuda:{dev}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        if graph is not None:
+            lib.qob_graph_free(ctx.ptr, graph)
+        return ms, launches, (t_host0, t_host1), (xs, ys)
+
+    K, W = args.steps, max(3, args.warmup)
+    ms64, launches64, win64, _ = timed(torch.complex128, dtype_code(np.complex128), K, W)
+    value = BATCH * K * world / (ms64 / 1e3)
+
+    # ComplexF32 mode on the same workload, error against the oracle on one ket
+    prepare(H, L.QOB_LEFT, np.complex64, dev)
+    ms32, _, _, _ = timed(torch.complex64, dtype_code(np.complex64), K, W)
+    value32 = BATCH * K * world / (ms32 / 1e3)
+    err32 = fp32_error(H, dev) if rank == 0 else None
+
+    # end to end through the host-buffer C call with pinned host memory
+    e2e = None
+    if rank == 0 or world > 1:
+        e2e = end_to_end(lib, ctx, hd, dim, K, dev, world)
+
+    if sampler:
+        sampler.stop()
+    if rank != 0:
+        return
+    bytes_per_ket = (2 + (1 if BETA != 0 else 0)) * dim * 16
+    t_launch = ms64 / 1e3 / K
+    achieved = bytes_per_ket * BATCH / t_launch / 1e9
+    peaks = read_json(os.path.join(ROOT, "MEASURED_PEAKS.json"))
+    peak, peak_src = (peaks["hbm_gbs"], "measured") if peaks and "hbm_gbs" in peaks else (6800.0, "fallback")
+    prof = read_json(os.path.join(ROOT, "profiles", "gather_heisenberg14_batch64.json")) or {}
+    fp64 = None
+    if prof.get("dfma_per_launch"):
+        fp64_rate = 2.0 * prof["dfma_per_launch"] / t_launch / 1e12
+        fp64 = {"bound": "fp64 FMA pipe", "achieved": fp64_rate, "peak": prof.get("fp64_peak_tflops"),
+                "unit": "TFLOP/s (executed DFMA x2)",
+                "frac": fp64_rate / prof["fp64_peak_tflops"] if prof.get("fp64_peak_tflops") else None}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms64 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128", "data": "synthetic (seeded complex-Gaussian kets, normalised)", "config": config(),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_src, "traffic": prof.get("dram_bytes_per_launch"),
+                     "algorithmic_bytes_per_launch": bytes_per_ket * BATCH,
+                     "kernel": "k_gather_j<double, real, square, TC=8, beta general>",
+                     "binding": "fp64 FMA throughput (GB300 FP64 ~1.25 TFLOP/s), see fp64_compute"},
+        "fp64_compute": fp64,
+        "plan": plan,
+        "gpu_launches": launches64,
+        "fp32_mode": {"value": value32, "unit": UNIT, "ms_per_step": ms32 / K, "vs_fp64": value32 / value,
+                      "rel_l2_err_vs_oracle": err32},
+        "e2e": e2e,
+        "clocks": sampler.summary(*win64) if sampler else None,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(H, args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+
+
+def fp32_error(H, dev):
+    import numpy as np
+
+    import oracle as OR
+    import qobgpu as Q
+    from qobgpu.mul import mul_, to_device
+
+    rng = Q.Rng(97)
+    psi = Q.Ket(H.basis_r, rng.ket_data(len(H.basis_r)))
+    out = Q.Ket(H.basis_l, rng.ket_data(len(H.basis_l)))
+    ref = OR.mul(out, H, psi, ALPHA, BETA)
+    d_out = to_device(out, dev, np.complex64)
+    mul_(d_out, H, to_device(psi, dev, np.complex64), ALPHA, BETA)
+    got = d_out.data.cpu().numpy().astype(np.complex128)
+    return float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+
+
+def end_to_end(lib, ctx, hd, dim, K, dev, world):
+    import ctypes as C
+
+    import torch
+
+    from qobgpu import _lib as L
+    from qobgpu.device import raise_for
+
+    xh = torch.randn(BATCH, dim, dtype=torch.complex128).pin_memory()
+    yh = torch.randn(BATCH, dim, dtype=torch.complex128).pin_memory()
+    args = (ctx.ptr, L.QOB_LEFT, 0, hd.ptr, L.QOB_C128, ALPHA.real, ALPHA.imag, C.c_void_p(xh.data_ptr()), dim,
+            BATCH, BETA, 0.0, C.c_void_p(yh.data_ptr()), dim, BATCH)
+    for _ in range(3):
+        raise_for(lib.qob_mul_host(*args), ctx)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    n0 = lib.qob_kernel_launches()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        raise_for(lib.qob_mul_host(*args), ctx)
+    torch.cuda.synchronize(dev)
+    dt = time.perf_counter() - t0
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([dt], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dt = float(t.item())
+    nbytes = BATCH * dim * 16
+    return {"value": BATCH * K * world / dt, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
+            "d2h_bytes_per_step": nbytes, "gpu_launches": lib.qob_kernel_launches() - n0,
+            "api": "qob_mul_host (pinned host buffers; x and beta-scaled y copied in, y copied out each step)"}
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    import __graft_entry__ as g
+
+    g.build()
+    run_own(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -57,6 +57,10 @@ typedef struct qob_op qob_op;
 
 int qob_version(void);
 
+/* Number of CUDA kernels this library has launched in the process so far
+ * (diagnostics: lets a caller count the device work behind a call). */
+int64_t qob_kernel_launches(void);
+
 /* Context on one CUDA device.  flags: reserved, pass 0. */
 int qob_create(qob_ctx** ctx, int device, unsigned flags);
 int qob_destroy(qob_ctx* ctx);
@@ -160,6 +164,19 @@ int qob_dot(qob_ctx* ctx, int dtype, const void* x, const void* y, int64_t n, do
 /* expect(op, psi) = <psi|op|psi> (src/operators.jl:119) */
 int qob_expect(qob_ctx* ctx, qob_op* op, int dtype, const void* psi, int64_t n, double* result,
                void* stream);
+
+/* ---------------------------------------------------------------------------
+ * CUDA graphs of library calls.  Between qob_graph_begin and qob_graph_end the
+ * qob_* calls issued on `stream` (a non-default stream) are recorded instead of
+ * run; qob_graph_launch replays them.  Operators used inside must have been
+ * applied (or qob_op_prepare'd) once with the same shapes before capture, so
+ * that no allocation or upload happens while recording.
+ * ------------------------------------------------------------------------- */
+typedef struct qob_graph qob_graph;
+int qob_graph_begin(qob_ctx* ctx, void* stream);
+int qob_graph_end(qob_ctx* ctx, void* stream, qob_graph** out);
+int qob_graph_launch(qob_ctx* ctx, qob_graph* graph, void* stream);
+int qob_graph_free(qob_ctx* ctx, qob_graph* graph);
 
 #ifdef __cplusplus
 }

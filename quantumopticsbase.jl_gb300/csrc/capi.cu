@@ -1,6 +1,7 @@
 // capi.cu -- the C ABI (include/qobgpu.h): operator handles, plan cache,
 // execution of compiled plans, and the FP64 reductions.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <new>
 
@@ -9,6 +10,9 @@
 namespace qob {
 
 void fail(int code, const std::string& msg) { throw Error{code, msg}; }
+
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void cuda_check(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return;
@@ -224,6 +228,8 @@ bool overlaps(const void* a, size_t abytes, const void* b, size_t bbytes) {
 extern "C" {
 
 int qob_version(void) { return 10000; }
+
+int64_t qob_kernel_launches(void) { return (int64_t)g_launches.load(std::memory_order_relaxed); }
 
 int qob_create(qob_ctx** ctx, int device, unsigned flags) {
   (void)flags;
@@ -510,6 +516,53 @@ int qob_dot(qob_ctx* ctx, int dtype, const void* x, const void* y, int64_t n, do
     if (!ctx || !x || !y || !result || n < 0) fail(QOB_ERR_ARG, "qob_dot: bad arguments");
     check_dtype(dtype);
     reduce_dot(ctx->c, dtype, x, y, n, false, result, (cudaStream_t)stream);
+  });
+}
+
+struct qob_graph {
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t e = nullptr;
+};
+
+int qob_graph_begin(qob_ctx* ctx, void* stream) {
+  return guard(ctx, [&] {
+    if (!ctx || !stream) fail(QOB_ERR_ARG, "capture needs a context and a non-default stream");
+    QOB_CUDA(cudaStreamBeginCapture((cudaStream_t)stream, cudaStreamCaptureModeThreadLocal));
+  });
+}
+
+int qob_graph_end(qob_ctx* ctx, void* stream, qob_graph** out) {
+  return guard(ctx, [&] {
+    if (!ctx || !stream || !out) fail(QOB_ERR_ARG, "qob_graph_end: bad arguments");
+    auto* gr = new qob_graph;
+    cudaError_t e = cudaStreamEndCapture((cudaStream_t)stream, &gr->g);
+    if (e != cudaSuccess) {
+      delete gr;
+      cuda_check(e, "cudaStreamEndCapture");
+    }
+    e = cudaGraphInstantiate(&gr->e, gr->g, 0);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(gr->g);
+      delete gr;
+      cuda_check(e, "cudaGraphInstantiate");
+    }
+    *out = gr;
+  });
+}
+
+int qob_graph_launch(qob_ctx* ctx, qob_graph* graph, void* stream) {
+  return guard(ctx, [&] {
+    if (!graph) fail(QOB_ERR_ARG, "null graph");
+    QOB_CUDA(cudaGraphLaunch(graph->e, (cudaStream_t)stream));
+  });
+}
+
+int qob_graph_free(qob_ctx* ctx, qob_graph* graph) {
+  return guard(ctx, [&] {
+    if (!graph) return;
+    if (graph->e) cudaGraphExecDestroy(graph->e);
+    if (graph->g) cudaGraphDestroy(graph->g);
+    delete graph;
   });
 }
 

@@ -382,7 +382,7 @@ void launch_gather(const GatherPlan& g, int precision, const void* x, int64_t xe
       dispatch_kind<double>(c, g.sites, x, xes, xcs, y, yes, ycs, ncols, alpha, b, s);
     else
       dispatch_kind<float>(c, g.sites, x, xes, xcs, y, yes, ycs, ncols, alpha, b, s);
-    QOB_CUDA(cudaGetLastError());
+    QOB_LAUNCHED();
     g0 += c.ngroups;
     first = false;
   } while (g0 < v.ngroups);
@@ -404,7 +404,7 @@ void launch_build_diag(const GatherPlan& g, cudaStream_t s) {
     else
       k_build_diag<float, false><<<blocks, threads, 0, s>>>(g.m, g.ndgroups, dg, dt, g.diag.p);
   }
-  QOB_CUDA(cudaGetLastError());
+  QOB_LAUNCHED();
 }
 
 }  // namespace qob

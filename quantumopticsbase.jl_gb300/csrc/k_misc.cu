@@ -211,7 +211,7 @@ void launch_scale(int precision, void* y, int64_t rows, int64_t cols, int64_t lr
     k_scale<double2><<<blocks_for(n, 256), 256, 0, s>>>((double2*)y, rows, cols, lr, lc, beta.re, beta.im);
   else
     k_scale<float2><<<blocks_for(n, 256), 256, 0, s>>>((float2*)y, rows, cols, lr, lc, beta.re, beta.im);
-  QOB_CUDA(cudaGetLastError());
+  QOB_LAUNCHED();
 }
 
 void launch_axpby(int precision, const void* x, int64_t xes, int64_t xcs, c128 alpha, void* y,
@@ -224,7 +224,7 @@ void launch_axpby(int precision, const void* x, int64_t xes, int64_t xcs, c128 a
   else
     k_axpby<float2, float><<<blocks_for(n, 256), 256, 0, s>>>(
         (const float2*)x, xes, xcs, (float2*)y, yes, ycs, len, ncols, alpha.re, alpha.im, beta.re, beta.im);
-  QOB_CUDA(cudaGetLastError());
+  QOB_LAUNCHED();
 }
 
 void launch_dense(int precision, const void* a, int64_t m, int64_t n, c128 alpha, const void* x,
@@ -247,7 +247,7 @@ void launch_dense(int precision, const void* a, int64_t m, int64_t n, c128 alpha
     k_dense<float2, float><<<grid, 128, 0, s>>>((const float2*)a, m, n, (const float2*)x, xes, xcs,
                                                 (float2*)y, yes, ycs, ncols, alpha.re, alpha.im,
                                                 beta.re, beta.im);
-  QOB_CUDA(cudaGetLastError());
+  QOB_LAUNCHED();
 }
 
 void launch_modek(int precision, const void* a, bool eye, int64_t s1, int64_t dout, int64_t din,
@@ -282,7 +282,7 @@ void launch_modek(int precision, const void* a, bool eye, int64_t s1, int64_t do
                                                          (const float2*)x, xes, xcs, (float2*)y, yes, ycs,
                                                          ncols, alpha.re, alpha.im, beta.re, beta.im);
   }
-  QOB_CUDA(cudaGetLastError());
+  QOB_LAUNCHED();
 }
 
 // result: interleaved complex dot (norm: sqrt of the real part in out[0]).
@@ -297,9 +297,9 @@ void reduce_dot(Context& ctx, int precision, const void* x, const void* y, int64
     k_dot_partial<double2><<<kRedBlocks, kRedThreads, 0, s>>>((const double2*)x, (const double2*)y, n, part);
   else
     k_dot_partial<float2><<<kRedBlocks, kRedThreads, 0, s>>>((const float2*)x, (const float2*)y, n, part);
-  QOB_CUDA(cudaGetLastError());
+  QOB_LAUNCHED();
   k_dot_final<<<1, kRedThreads, 0, s>>>(part, kRedBlocks, res);
-  QOB_CUDA(cudaGetLastError());
+  QOB_LAUNCHED();
   QOB_CUDA(cudaMemcpyAsync(ctx.reduce_host, res, sizeof(double2), cudaMemcpyDeviceToHost, s));
   QOB_CUDA(cudaStreamSynchronize(s));
   const double2 r = *(const double2*)ctx.reduce_host;

@@ -42,6 +42,13 @@ struct Error {
 [[noreturn]] void fail(int code, const std::string& msg);
 void cuda_check(cudaError_t e, const char* what);
 #define QOB_CUDA(call) ::qob::cuda_check((call), #call)
+// Every kernel launch of the library is checked and counted (qob_kernel_launches).
+void count_launch();
+#define QOB_LAUNCHED()                  \
+  do {                                  \
+    QOB_CUDA(cudaGetLastError());       \
+    ::qob::count_launch();              \
+  } while (0)
 
 // ---------------------------------------------------------------------------
 // operator tree (host)

@@ -35,6 +35,7 @@ I = C.c_int
 # name -> (restype, argtypes)
 SIGNATURES = {
     "qob_version": (I, []),
+    "qob_kernel_launches": (I64, []),
     "qob_create": (I, [C.POINTER(VP), I, C.c_uint]),
     "qob_destroy": (I, [VP]),
     "qob_last_error": (C.c_char_p, [VP]),
@@ -53,6 +54,10 @@ SIGNATURES = {
     "qob_norm": (I, [VP, I, VP, I64, DP, VP]),
     "qob_dot": (I, [VP, I, VP, VP, I64, DP, VP]),
     "qob_expect": (I, [VP, VP, I, VP, I64, DP, VP]),
+    "qob_graph_begin": (I, [VP, VP]),
+    "qob_graph_end": (I, [VP, VP, C.POINTER(VP)]),
+    "qob_graph_launch": (I, [VP, VP, VP]),
+    "qob_graph_free": (I, [VP, VP]),
 }
 
 _lib = None

@@ -14,7 +14,7 @@ def declared_symbols():
     for f in os.listdir(os.path.join(ROOT, "include")):
         if f.endswith(".h"):
             txt = open(os.path.join(ROOT, "include", f)).read()
-            names |= set(re.findall(r"^\s*(?:int|const char\*|void)\s+(qob_\w+)\s*\(", txt, re.M))
+            names |= set(re.findall(r"^\s*(?:int|int64_t|const char\*|void)\s+(qob_\w+)\s*\(", txt, re.M))
     return names
 
 
