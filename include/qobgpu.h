@@ -165,6 +165,22 @@ int qob_dot(qob_ctx* ctx, int dtype, const void* x, const void* y, int64_t n, do
 int qob_expect(qob_ctx* ctx, qob_op* op, int dtype, const void* psi, int64_t n, double* result,
                void* stream);
 
+/* qob_dot_noalloc: the inner product of qob_dot for callers that cannot
+ * allocate device memory while they run (their memory pool owns the device, or
+ * they issue work during a stream capture).  No counterpart in the reference:
+ * it is an addition of this library.
+ *   - allocates nothing: partial sums live in a 128 KiB static device array held
+ *     by every GPU that loads the library until exit; the result (two doubles,
+ *     re and im) is written to DEVICE memory `result` owned by the caller,
+ *     stream-ordered on `stream`, without synchronising;
+ *   - n is limited to 16,777,216 elements; larger n returns QOB_ERR_ARG;
+ *   - all calls share the one array: calls that overlap on the GPU race; order
+ *     them (one stream);
+ *   - the first call on a device looks up the array's address; make it before
+ *     any stream capture. */
+int qob_dot_noalloc(qob_ctx* ctx, int dtype, const void* x, const void* y, int64_t n,
+                    double* result, void* stream);
+
 /* ---------------------------------------------------------------------------
  * CUDA graphs of library calls.  Between qob_graph_begin and qob_graph_end the
  * qob_* calls issued on `stream` (a non-default stream) are recorded instead of

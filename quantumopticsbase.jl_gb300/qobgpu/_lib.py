@@ -54,6 +54,7 @@ SIGNATURES = {
     "qob_norm": (I, [VP, I, VP, I64, DP, VP]),
     "qob_dot": (I, [VP, I, VP, VP, I64, DP, VP]),
     "qob_expect": (I, [VP, VP, I, VP, I64, DP, VP]),
+    "qob_dot_noalloc": (I, [VP, I, VP, VP, I64, VP, VP]),
     "qob_graph_begin": (I, [VP, VP]),
     "qob_graph_end": (I, [VP, VP, C.POINTER(VP)]),
     "qob_graph_launch": (I, [VP, VP, VP]),
