@@ -289,12 +289,19 @@ def run_own(args, rank, world, local_rank):
             lib.qob_graph_free(ctx.ptr, graph)
         return ms, launches, (t_host0, t_host1), (xs, ys)
 
+    def tune(dt):
+        times = (C.c_double * 4)()
+        chosen = C.c_int()
+        raise_for(lib.qob_op_tune(ctx.ptr, hd.ptr, L.QOB_LEFT, dtype_code(dt), BATCH, times, C.byref(chosen)), ctx)
+        return {"kets_per_thread": chosen.value, "ms_by_kets_per_thread": {str(1 << k): times[k] for k in range(4)}}
+
+    prepare(H, L.QOB_LEFT, np.complex64, dev)
+    tuning = {"c128": tune(np.complex128), "c64": tune(np.complex64)}
     K, W = args.steps, max(3, args.warmup)
     ms64, launches64, win64, _ = timed(torch.complex128, dtype_code(np.complex128), K, W)
     value = BATCH * K * world / (ms64 / 1e3)
 
     # ComplexF32 mode on the same workload, error against the oracle on one ket
-    prepare(H, L.QOB_LEFT, np.complex64, dev)
     ms32, _, _, _ = timed(torch.complex64, dtype_code(np.complex64), K, W)
     value32 = BATCH * K * world / (ms32 / 1e3)
     err32 = fp32_error(H, dev) if rank == 0 else None
@@ -331,6 +338,7 @@ def run_own(args, rank, world, local_rank):
                      "binding": "fp64 FMA throughput (GB300 FP64 ~1.25 TFLOP/s), see fp64_compute"},
         "fp64_compute": fp64,
         "plan": plan,
+        "tuning": tuning,
         "gpu_launches": launches64,
         "fp32_mode": {"value": value32, "unit": UNIT, "ms_per_step": ms32 / K, "vs_fp64": value32 / value,
                       "rel_l2_err_vs_oracle": err32},

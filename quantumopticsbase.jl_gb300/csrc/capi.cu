@@ -432,6 +432,58 @@ int qob_op_prepare(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t* info)
   });
 }
 
+int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, double* times_ms, int* chosen) {
+  return guard(ctx, [&] {
+    if (!ctx || !op || ncols < 1 || (side != QOB_LEFT && side != QOB_RIGHT))
+      fail(QOB_ERR_ARG, "qob_op_tune: bad arguments");
+    check_dtype(dtype);
+    Plan& P = get_plan(ctx->c, op, side, dtype);
+    const int tiles[4] = {1, 2, 4, 8};
+    double t[4] = {-1.0, -1.0, -1.0, -1.0};
+    int best = 0;
+    if (P.gather && P.kind == Plan::Kind::Sum) {
+      GatherPlan& g = *P.gather;
+      const size_t esz = dtype == QOB_C128 ? 16 : 8;
+      DeviceBuf x, y;
+      x.alloc((size_t)P.n * ncols * esz);
+      y.alloc((size_t)P.m * ncols * esz);
+      QOB_CUDA(cudaMemset(x.p, 0, x.bytes));
+      QOB_CUDA(cudaMemset(y.p, 0, y.bytes));
+      // vectors as the reference lays them out: columns for LEFT, rows for RIGHT
+      const int64_t xes = side == QOB_LEFT ? 1 : ncols, xcs = side == QOB_LEFT ? P.n : 1;
+      const int64_t yes = side == QOB_LEFT ? 1 : ncols, ycs = side == QOB_LEFT ? P.m : 1;
+      cudaEvent_t e0, e1;
+      QOB_CUDA(cudaEventCreate(&e0));
+      QOB_CUDA(cudaEventCreate(&e1));
+      double best_t = 1e300;
+      for (int k = 0; k < 4; ++k) {
+        if (tiles[k] > ncols || (k > 0 && side == QOB_RIGHT && ncols > 1)) continue;
+        g.tc = tiles[k];
+        for (int i = 0; i < 2; ++i)
+          apply_plan(ctx->c, P, {1.0, 0.0}, x.p, xes, xcs, {0.3, 0.0}, y.p, yes, ycs, ncols, 0, 0);
+        QOB_CUDA(cudaEventRecord(e0, 0));
+        for (int i = 0; i < 5; ++i)
+          apply_plan(ctx->c, P, {1.0, 0.0}, x.p, xes, xcs, {0.3, 0.0}, y.p, yes, ycs, ncols, 0, 0);
+        QOB_CUDA(cudaEventRecord(e1, 0));
+        QOB_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        QOB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        t[k] = ms / 5.0;
+        if (t[k] < best_t) {
+          best_t = t[k];
+          best = tiles[k];
+        }
+      }
+      g.tc = best;
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+    }
+    if (times_ms)
+      for (int k = 0; k < 4; ++k) times_ms[k] = t[k];
+    if (chosen) *chosen = best;
+  });
+}
+
 int qob_mul(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, double alpha_re, double alpha_im,
             const void* x, int64_t x_rows, int64_t x_cols, int64_t x_ld, double beta_re, double beta_im, void* y,
             int64_t y_rows, int64_t y_cols, int64_t y_ld, void* stream) {

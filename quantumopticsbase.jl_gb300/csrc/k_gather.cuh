@@ -1,0 +1,550 @@
+// k_gather.cuh -- the fused LazySum application kernel (templates; instantiated
+// per precision in k_gather_f64.cu and k_gather_f32.cu).
+//
+// One thread owns one output index J and a tile of TC vectors (kets, columns).
+// It accumulates, in registers, the merged diagonal times x[J] plus every
+// group's stored entries of its local row times the gathered x[base + coloff],
+// then writes y[J] = alpha * acc + beta * y[J] once.  This replaces the
+// reference's one pass per term over `result` (src/operators_lazysum.jl:189-200)
+// and the recursive per-nonzero gather (src/operators_lazytensor.jl:652-685):
+// the state is read once per entry from L1/L2 instead of once per term from
+// memory, and y is read and written once.
+//
+// Groups whose rows hold at most kMaxEllWidth entries (every ladder / Pauli /
+// number product) are read as fixed-width slots staged in shared memory with
+// the group descriptors: one shared-memory load per entry instead of the
+// dependent rowptr -> coloff -> value chain of the CSR form, which remains for
+// wide groups (a full-space SparseOperator with long rows).  When every group
+// has one slot per row (W1), the group loop is unrolled so the gathers of
+// several groups are in flight together, and when every group is also one run
+// of power-of-two subsystems (spin chains) a 16-byte compact record per group
+// replaces the descriptor reads.
+//
+// Subsystems of power-of-two length (spin-1/2 chains) use shifts and masks for
+// the index arithmetic, others Lemire's multiply-high division.
+//
+// FP64 keeps the reference's arithmetic type; with real merged values (all
+// the Hamiltonians built from number/ladder/Pauli factors with real
+// coefficients) each stored entry costs two DFMA per vector.  FP32 mode adds
+// Kahan compensation across the accumulated contributions.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "qob_internal.h"
+
+namespace qob {
+namespace gather {
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, uint32_t d, uint64_t M) {
+  return d == 1u ? n : (uint32_t)__umul64hi(M, (uint64_t)n);
+}
+__device__ __forceinline__ uint32_t fmodu(uint32_t n, uint32_t d, uint64_t M) {
+  uint64_t low = M * (uint64_t)n;
+  return (uint32_t)__umul64hi(low, (uint64_t)d);
+}
+
+template <typename R>
+struct Cx;
+template <>
+struct Cx<double> {
+  using T = double2;
+};
+template <>
+struct Cx<float> {
+  using T = float2;
+};
+
+template <typename R, bool REALV>
+struct Val {
+  using T = typename Cx<R>::T;
+};
+template <>
+struct Val<double, true> {
+  using T = double;
+};
+template <>
+struct Val<float, true> {
+  using T = float;
+};
+
+// fixed-width slot type per precision / realness, and its value
+template <typename R, bool REALV>
+struct Ell;
+template <>
+struct Ell<double, true> {
+  using T = EllD;
+  static __device__ __forceinline__ double v(const EllD& e) { return e.v; }
+};
+template <>
+struct Ell<double, false> {
+  using T = EllZ;
+  static __device__ __forceinline__ double2 v(const EllZ& e) { return make_double2(e.v[0], e.v[1]); }
+};
+template <>
+struct Ell<float, true> {
+  using T = EllF;
+  static __device__ __forceinline__ float v(const EllF& e) { return e.v; }
+};
+template <>
+struct Ell<float, false> {
+  using T = EllC;
+  static __device__ __forceinline__ float2 v(const EllC& e) { return make_float2(e.v[0], e.v[1]); }
+};
+
+__device__ __forceinline__ bool nz(double v) { return v != 0.0; }
+__device__ __forceinline__ bool nz(float v) { return v != 0.f; }
+__device__ __forceinline__ bool nz(double2 v) { return v.x != 0.0 || v.y != 0.0; }
+__device__ __forceinline__ bool nz(float2 v) { return v.x != 0.f || v.y != 0.f; }
+
+// FP64 accumulator: plain fused multiply-adds.
+struct AccD {
+  double re, im;
+  __device__ void zero() { re = im = 0.0; }
+  __device__ void mac(double v, double2 x) {
+    re = fma(v, x.x, re);
+    im = fma(v, x.y, im);
+  }
+  __device__ void mac(double2 v, double2 x) {
+    re = fma(v.x, x.x, re);
+    re = fma(-v.y, x.y, re);
+    im = fma(v.x, x.y, im);
+    im = fma(v.y, x.x, im);
+  }
+  __device__ void set(double v, double2 x) {
+    re = v * x.x;
+    im = v * x.y;
+  }
+  __device__ void set(double2 v, double2 x) {
+    re = fma(-v.y, x.y, v.x * x.x);
+    im = fma(v.y, x.x, v.x * x.y);
+  }
+  __device__ double2 total() const { return make_double2(re, im); }
+};
+
+// FP32 accumulator with Kahan compensation (Kahan 1965): c carries the
+// low-order part lost by each addition.
+struct AccF {
+  float re, im, cre, cim;
+  __device__ void zero() { re = im = cre = cim = 0.f; }
+  __device__ void add(float tr, float ti) {
+    float yr = tr - cre;
+    float sr = re + yr;
+    cre = (sr - re) - yr;
+    re = sr;
+    float yi = ti - cim;
+    float si = im + yi;
+    cim = (si - im) - yi;
+    im = si;
+  }
+  __device__ void mac(float v, float2 x) { add(v * x.x, v * x.y); }
+  __device__ void mac(float2 v, float2 x) {
+    add(__fmaf_rn(v.x, x.x, -v.y * x.y), __fmaf_rn(v.x, x.y, v.y * x.x));
+  }
+  __device__ void set(float v, float2 x) {
+    re = v * x.x;
+    im = v * x.y;
+    cre = cim = 0.f;
+  }
+  __device__ void set(float2 v, float2 x) {
+    re = __fmaf_rn(v.x, x.x, -v.y * x.y);
+    im = __fmaf_rn(v.x, x.y, v.y * x.x);
+    cre = cim = 0.f;
+  }
+  __device__ float2 total() const { return make_float2(re - cre, im - cim); }
+};
+
+template <typename R>
+struct AccOf;
+template <>
+struct AccOf<double> {
+  using T = AccD;
+};
+template <>
+struct AccOf<float> {
+  using T = AccF;
+};
+
+__device__ __forceinline__ double2 ld(const double2* p) { return __ldg(p); }
+__device__ __forceinline__ float2 ld(const float2* p) { return __ldg(p); }
+
+// y = alpha * acc + beta * y with the reference's beta semantics:
+// BMODE 0: beta == 0 (y is not read), 2: general complex beta, 3: real beta.
+template <int BMODE>
+__device__ __forceinline__ void combine(double2* yp, double2 a, double2 alpha, double2 beta) {
+  double re = alpha.x * a.x - alpha.y * a.y;
+  double im = alpha.x * a.y + alpha.y * a.x;
+  if (BMODE == 2) {
+    double2 o = *yp;
+    re = fma(beta.x, o.x, fma(-beta.y, o.y, re));
+    im = fma(beta.x, o.y, fma(beta.y, o.x, im));
+  } else if (BMODE == 3) {
+    double2 o = *yp;
+    re = fma(beta.x, o.x, re);
+    im = fma(beta.x, o.y, im);
+  }
+  *yp = make_double2(re, im);
+}
+template <int BMODE>
+__device__ __forceinline__ void combine(float2* yp, float2 a, float2 alpha, float2 beta) {
+  float re = alpha.x * a.x - alpha.y * a.y;
+  float im = alpha.x * a.y + alpha.y * a.x;
+  if (BMODE == 2) {
+    float2 o = *yp;
+    re = __fmaf_rn(beta.x, o.x, __fmaf_rn(-beta.y, o.y, re));
+    im = __fmaf_rn(beta.x, o.y, __fmaf_rn(beta.y, o.x, im));
+  } else if (BMODE == 3) {
+    float2 o = *yp;
+    re = __fmaf_rn(beta.x, o.x, re);
+    im = __fmaf_rn(beta.x, o.y, im);
+  }
+  *yp = make_float2(re, im);
+}
+
+// Copy the group descriptors (then, for plans with the compact form, one int4
+// per group; then, if requested, the fixed-width slots) to shared memory;
+// returns the slot pointer to use.
+template <typename ET>
+__device__ __forceinline__ const ET* stage(unsigned char* smem, const GatherView& g) {
+  GGroup* sg = reinterpret_cast<GGroup*>(smem);
+  {
+    const uint64_t* src = reinterpret_cast<const uint64_t*>(g.groups);
+    uint64_t* dst = reinterpret_cast<uint64_t*>(sg);
+    const int words = g.ngroups * (int)(sizeof(GGroup) / 8);
+    for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+  }
+  size_t off = (size_t)g.ngroups * sizeof(GGroup);
+  if (g.fast) {
+    int4* df = reinterpret_cast<int4*>(smem + off);
+    for (int i = threadIdx.x; i < g.ngroups; i += blockDim.x) df[i] = g.fastg[i];
+    off += (size_t)g.ngroups * sizeof(int4);
+  }
+  const ET* ell = static_cast<const ET*>(g.ell);
+  if (g.ell_smem) {
+    ET* se = reinterpret_cast<ET*>(smem + off);
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(g.ell);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(se);
+    const int words = g.ell_slots * (int)(sizeof(ET) / 4);
+    for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+    ell = se;
+  }
+  __syncthreads();
+  return ell;
+}
+
+// Local row r of output index J in group G, and sub = the part of J carried by
+// the group's subsystems (so J - sub is the row's base index on a square basis).
+__device__ __forceinline__ void local_row(const GGroup& G, uint32_t J, uint32_t& r, uint32_t& sub) {
+  if (G.nblk == 1) {  // one run of consecutive subsystems (the common case)
+    uint32_t d;
+    if (G.pow2) {
+      const uint32_t sh = G.shifts[0];
+      d = (J >> (sh & 0xffu)) & (G.mod[0] - 1u);
+      sub = d << (sh & 0xffu);
+    } else {
+      d = fmodu(fdiv(J, G.div[0], G.mdiv[0]), G.mod[0], G.mmod[0]);
+      sub = d * G.div[0];
+    }
+    r = d;
+    return;
+  }
+  r = 0;
+  sub = 0;
+  if (G.pow2) {  // shifts and masks (power-of-two subsystem lengths)
+#pragma unroll
+    for (int b = 0; b < kMaxBlocks; ++b) {
+      if (b < G.nblk) {
+        const uint32_t sh = G.shifts[b];
+        const uint32_t sd = sh & 0xffu, sm = (sh >> 8) & 0xffu, sl = sh >> 16;
+        const uint32_t d = (J >> sd) & ((1u << sm) - 1u);
+        r += d << sl;
+        sub += d << sd;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int b = 0; b < kMaxBlocks; ++b) {
+      if (b < G.nblk) {
+        const uint32_t q = fdiv(J, G.div[b], G.mdiv[b]);
+        const uint32_t d = fmodu(q, G.mod[b], G.mmod[b]);
+        r += d * G.lstride[b];
+        sub += d * G.div[b];
+      }
+    }
+  }
+}
+
+// Local row and input base offset of output index J in group G; false when a
+// subsystem outside the support has no counterpart on the input side.
+template <bool SQUARE>
+__device__ __forceinline__ bool group_row(const GGroup& G, const SiteTable& st, uint32_t J,
+                                          uint32_t& r, int64_t& base) {
+  uint32_t sub;
+  local_row(G, J, r, sub);
+  if (SQUARE) {
+    base = (int64_t)(J - sub);
+    return true;
+  }
+  // non-square basis: identity (truncated) on the subsystems outside the support
+  int64_t bs = 0;
+  for (int s = 0; s < st.nsites; ++s) {
+    const bool in_sup = s < 32 ? ((uint32_t)G.support_lo >> s) & 1u : (G.support_hi >> (s - 32)) & 1u;
+    if (in_sup) continue;
+    uint32_t js = fmodu(fdiv(J, st.sout[s], st.msout[s]), st.dout[s], st.mdout[s]);
+    if (js >= st.din[s]) return false;
+    bs += (int64_t)js * st.sin[s];
+  }
+  base = bs;
+  return true;
+}
+
+// acc[t] = (H x)[J] for the nt vectors starting at xb (element stride es,
+// vector stride xcs).
+template <typename R, bool REALV, bool SQUARE, bool W1, int TC>
+__device__ __forceinline__ void accumulate(const GatherView& g, const SiteTable& st, const GGroup* sg,
+                                           const typename Ell<R, REALV>::T* ell, uint32_t J,
+                                           const typename Cx<R>::T* xb, int64_t es, int64_t xcs, int nt,
+                                           typename AccOf<R>::T (&acc)[TC]) {
+  using VT = typename Val<R, REALV>::T;
+  using ET = typename Ell<R, REALV>::T;
+  using CT = typename Cx<R>::T;
+  if (g.has_diag) {
+    const VT d = static_cast<const VT*>(g.diag)[J];
+    const CT* xp = xb + (int64_t)J * es;
+#pragma unroll
+    for (int t = 0; t < TC; ++t)
+      if (t < nt) acc[t].set(d, ld(xp + t * xcs));
+  } else {
+#pragma unroll
+    for (int t = 0; t < TC; ++t) acc[t].zero();
+  }
+  if (W1 && g.fast) {
+    // every group: one run of power-of-two subsystems, one slot per row; its
+    // shift, mask and first slot sit in one 16-byte word after the descriptors
+    const int4* fg = reinterpret_cast<const int4*>(sg + g.ngroups);
+#pragma unroll 4
+    for (int gi = 0; gi < g.ngroups; ++gi) {
+      const int4 f = fg[gi];
+      const uint32_t r = (J >> f.x) & (uint32_t)f.y;
+      const ET s = ell[f.z + r];
+      const VT v = Ell<R, REALV>::v(s);
+      const CT* xp = xb + ((int64_t)(J - (r << f.x)) + s.col) * es;
+      if (nz(v)) {
+#pragma unroll
+        for (int t = 0; t < TC; ++t)
+          if (t < nt) acc[t].mac(v, ld(xp + t * xcs));
+      }
+    }
+    return;
+  }
+  if (W1) {
+    // one slot per row in every group: unrolled, loads of several groups in flight
+#pragma unroll 4
+    for (int gi = 0; gi < g.ngroups; ++gi) {
+      const GGroup& G = sg[gi];
+      uint32_t r, sub;
+      local_row(G, J, r, sub);
+      const ET s = ell[G.ell_off + r];
+      const VT v = Ell<R, REALV>::v(s);
+      const CT* xp = xb + ((int64_t)(J - sub) + s.col) * es;
+      if (nz(v)) {
+#pragma unroll
+        for (int t = 0; t < TC; ++t)
+          if (t < nt) acc[t].mac(v, ld(xp + t * xcs));
+      }
+    }
+    return;
+  }
+  const VT* vals = static_cast<const VT*>(g.vals);
+  for (int gi = 0; gi < g.ngroups; ++gi) {
+    const GGroup& G = sg[gi];
+    uint32_t r;
+    int64_t base;
+    if (!group_row<SQUARE>(G, st, J, r, base)) continue;
+    if (G.width > 0) {
+      const ET* e = ell + G.ell_off + (int64_t)r * G.width;
+      for (int k = 0; k < G.width; ++k) {
+        const ET s = e[k];
+        const VT v = Ell<R, REALV>::v(s);
+        if (nz(v)) {
+          const CT* xp = xb + (base + s.col) * es;
+#pragma unroll
+          for (int t = 0; t < TC; ++t)
+            if (t < nt) acc[t].mac(v, ld(xp + t * xcs));
+        }
+      }
+    } else {
+      const int p0 = __ldg(g.rowptr + G.rowptr_off + r);
+      const int p1 = __ldg(g.rowptr + G.rowptr_off + r + 1);
+      for (int p = p0; p < p1; ++p) {
+        const CT* xp = xb + (base + __ldg(g.coloff + p)) * es;
+        const VT v = vals[p];
+#pragma unroll
+        for (int t = 0; t < TC; ++t)
+          if (t < nt) acc[t].mac(v, ld(xp + t * xcs));
+      }
+    }
+  }
+}
+
+// Output index J fastest across threads: one thread per (J, tile of TC vectors);
+// the vectors are contiguous (element stride 1).
+template <typename R, bool REALV, bool SQUARE, bool W1, int TC, int BMODE>
+__global__ void __launch_bounds__(256) k_gather_j(GatherView g, SiteTable st,
+                                                  const typename Cx<R>::T* __restrict__ x, int64_t xcs,
+                                                  typename Cx<R>::T* __restrict__ y, int64_t ycs, int ncols,
+                                                  typename Cx<R>::T alpha, typename Cx<R>::T beta) {
+  using CT = typename Cx<R>::T;
+  using AT = typename AccOf<R>::T;
+  using ET = typename Ell<R, REALV>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const ET* ell = stage<ET>(smem_raw, g);
+  const GGroup* sg = reinterpret_cast<const GGroup*>(smem_raw);
+  const int64_t J = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (J >= g.m) return;
+  const int c0 = blockIdx.y * TC;
+  const int nt = min(TC, ncols - c0);
+  const CT* xb = x + (int64_t)c0 * xcs;
+  AT acc[TC];
+  accumulate<R, REALV, SQUARE, W1, TC>(g, st, sg, ell, (uint32_t)J, xb, 1, xcs, nt, acc);
+  CT* yb = y + J + (int64_t)c0 * ycs;
+#pragma unroll
+  for (int t = 0; t < TC; ++t)
+    if (t < nt) combine<BMODE>(yb + t * ycs, acc[t].total(), alpha, beta);
+}
+
+// Vectors with a stride between their elements (the rows of an operator
+// multiplied from the right, a strided bra): the vectors run across threads,
+// all threads of a block share one output index J.
+template <typename R, bool REALV, bool SQUARE, int BMODE>
+__global__ void __launch_bounds__(256) k_gather_c(GatherView g, SiteTable st,
+                                                  const typename Cx<R>::T* __restrict__ x, int64_t xes,
+                                                  int64_t xcs, typename Cx<R>::T* __restrict__ y,
+                                                  int64_t yes, int64_t ycs, int ncols, typename Cx<R>::T alpha,
+                                                  typename Cx<R>::T beta) {
+  using AT = typename AccOf<R>::T;
+  using ET = typename Ell<R, REALV>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const ET* ell = stage<ET>(smem_raw, g);
+  const GGroup* sg = reinterpret_cast<const GGroup*>(smem_raw);
+  const int64_t J = blockIdx.x;
+  const int64_t c = blockIdx.y * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ncols) return;
+  AT acc[1];
+  accumulate<R, REALV, SQUARE, false, 1>(g, st, sg, ell, (uint32_t)J, x + c * xcs, xes, xcs, 1, acc);
+  combine<BMODE>(y + J * yes + c * ycs, acc[0].total(), alpha, beta);
+}
+
+// ---------------------------------------------------------------------------
+// host-side dispatch (instantiated per precision)
+
+constexpr size_t kSmemBudget = 96 * 1024;  // descriptors + staged slots per block
+constexpr int kThreads = 256;
+
+template <typename K>
+void allow_smem(K kernel, size_t smem) {
+  if (smem > 48 * 1024)
+    QOB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+}
+
+template <typename R, bool REALV, bool SQUARE, bool W1, int TC, int BMODE>
+void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t xcs, void* y, int64_t ycs,
+              int64_t ncols, typename Cx<R>::T a, typename Cx<R>::T b, size_t smem, cudaStream_t s) {
+  using CT = typename Cx<R>::T;
+  auto kern = k_gather_j<R, REALV, SQUARE, W1, TC, BMODE>;
+  allow_smem(kern, smem);
+  const unsigned gx = (unsigned)((v.m + kThreads - 1) / kThreads);
+  for (int64_t c0 = 0; c0 < ncols; c0 += (int64_t)65535 * TC) {  // grid.y limit
+    const int64_t nc = std::min<int64_t>(ncols - c0, (int64_t)65535 * TC);
+    kern<<<dim3(gx, (unsigned)((nc + TC - 1) / TC)), kThreads, smem, s>>>(
+        v, st, (const CT*)x + c0 * xcs, xcs, (CT*)y + c0 * ycs, ycs, (int)nc, a, b);
+    QOB_LAUNCHED();
+  }
+}
+
+template <typename R, bool REALV, bool SQUARE, bool W1, int BMODE>
+void launch_tc(const GatherView& v, const SiteTable& st, int tc, const void* x, int64_t xcs, void* y,
+               int64_t ycs, int64_t ncols, typename Cx<R>::T a, typename Cx<R>::T b, size_t smem, cudaStream_t s) {
+  switch (tc) {
+    case 8:
+      launch_j<R, REALV, SQUARE, W1, 8, BMODE>(v, st, x, xcs, y, ycs, ncols, a, b, smem, s);
+      break;
+    case 4:
+      launch_j<R, REALV, SQUARE, W1, 4, BMODE>(v, st, x, xcs, y, ycs, ncols, a, b, smem, s);
+      break;
+    case 2:
+      launch_j<R, REALV, SQUARE, W1, 2, BMODE>(v, st, x, xcs, y, ycs, ncols, a, b, smem, s);
+      break;
+    default:
+      launch_j<R, REALV, SQUARE, W1, 1, BMODE>(v, st, x, xcs, y, ycs, ncols, a, b, smem, s);
+  }
+}
+
+template <typename R, bool REALV, bool SQUARE, int BMODE>
+void dispatch_layout(const GatherView& v, const SiteTable& st, int tc, const void* x, int64_t xes,
+                     int64_t xcs, void* y, int64_t yes, int64_t ycs, int64_t ncols, typename Cx<R>::T a, typename Cx<R>::T b,
+                     cudaStream_t s) {
+  using CT = typename Cx<R>::T;
+  using ET = typename Ell<R, REALV>::T;
+  GatherView w = v;
+  size_t smem = (size_t)v.ngroups * (sizeof(GGroup) + (v.fast ? sizeof(int4) : 0));
+  const size_t ell_bytes = (size_t)v.ell_slots * sizeof(ET);
+  w.ell_smem = (v.ell_slots > 0 && smem + ell_bytes <= kSmemBudget) ? 1 : 0;
+  if (w.ell_smem) smem += ell_bytes;
+  if (xes == 1 && yes == 1) {
+    if (SQUARE && v.all_w1)
+      launch_tc<R, REALV, SQUARE, true, BMODE>(w, st, tc, x, xcs, y, ycs, ncols, a, b, smem, s);
+    else
+      launch_tc<R, REALV, SQUARE, false, BMODE>(w, st, tc, x, xcs, y, ycs, ncols, a, b, smem, s);
+  } else {
+    auto kern = k_gather_c<R, REALV, SQUARE, BMODE>;
+    allow_smem(kern, smem);
+    const int threads = ncols >= 256 ? 256 : (int)((ncols + 31) / 32 * 32);
+    for (int64_t c0 = 0; c0 < ncols; c0 += (int64_t)65535 * threads) {  // grid.y limit
+      const int64_t nc = std::min<int64_t>(ncols - c0, (int64_t)65535 * threads);
+      dim3 grid((unsigned)v.m, (unsigned)((nc + threads - 1) / threads));
+      kern<<<grid, threads, smem, s>>>(w, st, (const CT*)x + c0 * xcs, xes, xcs, (CT*)y + c0 * ycs, yes, ycs,
+                                       (int)nc, a, b);
+      QOB_LAUNCHED();
+    }
+  }
+}
+
+template <typename R, bool REALV, bool SQUARE>
+void dispatch_beta(const GatherView& v, const SiteTable& st, int tc, const void* x, int64_t xes, int64_t xcs,
+                   void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta, cudaStream_t s) {
+  typename Cx<R>::T a, b;
+  a.x = (R)alpha.re;
+  a.y = (R)alpha.im;
+  b.x = (R)beta.re;
+  b.y = (R)beta.im;
+  if (beta.re == 0.0 && beta.im == 0.0)
+    dispatch_layout<R, REALV, SQUARE, 0>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, a, b, s);
+  else if (beta.im == 0.0)
+    dispatch_layout<R, REALV, SQUARE, 3>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, a, b, s);
+  else
+    dispatch_layout<R, REALV, SQUARE, 2>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, a, b, s);
+}
+
+// One launch (or one column chunk per grid limit) of the fused gather in
+// precision R.
+template <typename R>
+void dispatch(const GatherView& v, const SiteTable& st, int tc, const void* x, int64_t xes, int64_t xcs,
+              void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta, cudaStream_t s) {
+  if (v.real_vals) {
+    if (v.square)
+      dispatch_beta<R, true, true>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+    else
+      dispatch_beta<R, true, false>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+  } else {
+    if (v.square)
+      dispatch_beta<R, false, true>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+    else
+      dispatch_beta<R, false, false>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+  }
+}
+
+}  // namespace gather
+}  // namespace qob

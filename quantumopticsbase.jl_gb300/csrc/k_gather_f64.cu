@@ -1,0 +1,10 @@
+// k_gather_f64.cu -- the fused gather kernels instantiated for double (one
+// translation unit per precision so the two compile in parallel).
+#include "k_gather.cuh"
+
+namespace qob {
+namespace gather {
+template void dispatch<double>(const GatherView&, const SiteTable&, int, const void*, int64_t, int64_t, void*,
+                           int64_t, int64_t, int64_t, c128, c128, cudaStream_t);
+}  // namespace gather
+}  // namespace qob

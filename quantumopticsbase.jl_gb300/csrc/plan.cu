@@ -284,6 +284,22 @@ GGroup make_desc(const GroupBuild& g, const Shapes& S, int32_t rowptr_off) {
     d.mmod[b] = lemire_magic(d.mod[b]);
     ls *= mod;
   }
+  // power-of-two strides (spin-1/2 chains, qubit registers): shifts and masks
+  auto log2_exact = [](uint64_t v) -> int {
+    if (v == 0 || (v & (v - 1))) return -1;
+    int k = 0;
+    while ((uint64_t(1) << k) < v) ++k;
+    return k;
+  };
+  d.pow2 = 1;
+  for (int b = 0; b < d.nblk; ++b) {
+    const int a = log2_exact(d.div[b]), m = log2_exact(d.mod[b]), l = log2_exact(d.lstride[b]);
+    if (a < 0 || m < 0 || l < 0) {
+      d.pow2 = 0;
+      break;
+    }
+    d.shifts[b] = (uint32_t)a | ((uint32_t)m << 8) | ((uint32_t)l << 16);
+  }
   for (int s : g.ext) {
     if (s < 32)
       d.support_lo |= (1u << s);
@@ -377,7 +393,11 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
   std::vector<GGroup> descs;
   std::vector<int32_t> rowptr, coloff;
   std::vector<c128> vals;
-  std::vector<int> group_of_desc;
+  struct EllHost {
+    int32_t col;
+    c128 v;
+  };
+  std::vector<EllHost> ell;
   size_t s0 = 0;
   for (size_t gi = 0; gi < H.groups.size(); ++gi) {
     size_t s1 = s0;
@@ -398,12 +418,39 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
           coloff.push_back((int32_t)H.slots[s].coloff);
           vals.push_back(val[s]);
         }
+      // rows with at most kMaxEllWidth entries also get fixed-width slots
+      int32_t width = 0;
+      for (int64_t r = 0; r < g.nrows; ++r) width = std::max<int32_t>(width, cnt[r + 1] - cnt[r]);
+      if (width <= kMaxEllWidth && (int64_t)ell.size() + g.nrows * width < (int64_t(1) << 30)) {
+        d.width = width;
+        d.ell_off = (int32_t)ell.size();
+        for (int64_t r = 0; r < g.nrows; ++r) {
+          int32_t k = 0;
+          for (int32_t p = cnt[r]; p < cnt[r + 1]; ++p, ++k)
+            ell.push_back({coloff[base + p], vals[base + p]});
+          for (; k < width; ++k) ell.push_back({0, c128{0.0, 0.0}});
+        }
+      }
       descs.push_back(d);
     }
     s0 = s1;
   }
   gp.ngroups = (int)descs.size();
   gp.nentries = (int64_t)coloff.size();
+  gp.all_ell = true;
+  gp.all_w1 = true;
+  for (auto& d : descs) {
+    gp.all_ell &= (d.width > 0);
+    gp.all_w1 &= (d.width == 1);
+  }
+  // compact form: every group one run of power-of-two subsystems with one slot per row
+  gp.fast = square && !descs.empty();
+  std::vector<int4> fastg;
+  for (auto& d : descs) {
+    if (!(d.pow2 && d.nblk == 1 && d.width == 1)) gp.fast = false;
+    fastg.push_back(make_int4((int)(d.shifts[0] & 0xffu), (int)(d.mod[0] - 1u), d.ell_off, 0));
+  }
+  if (gp.fast) upload_vec(gp.fastg, fastg);
   gp.square = square;
   upload_vec(gp.groups, descs);
   upload_vec(gp.rowptr, rowptr);
@@ -426,6 +473,29 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
       std::vector<c64> v(vals.size());
       for (size_t i = 0; i < vals.size(); ++i) v[i] = {(float)vals[i].re, (float)vals[i].im};
       upload_vec(gp.vals, v);
+    }
+  }
+  // fixed-width slots in the plan precision
+  gp.ell_slots = (int32_t)ell.size();
+  if (precision == QOB_C128) {
+    if (real) {
+      std::vector<EllD> e(ell.size());
+      for (size_t i = 0; i < ell.size(); ++i) e[i] = {ell[i].col, 0, ell[i].v.re};
+      upload_vec(gp.ell, e);
+    } else {
+      std::vector<EllZ> e(ell.size());
+      for (size_t i = 0; i < ell.size(); ++i) e[i] = {ell[i].col, {0, 0, 0}, {ell[i].v.re, ell[i].v.im}};
+      upload_vec(gp.ell, e);
+    }
+  } else {
+    if (real) {
+      std::vector<EllF> e(ell.size());
+      for (size_t i = 0; i < ell.size(); ++i) e[i] = {ell[i].col, (float)ell[i].v.re};
+      upload_vec(gp.ell, e);
+    } else {
+      std::vector<EllC> e(ell.size());
+      for (size_t i = 0; i < ell.size(); ++i) e[i] = {ell[i].col, 0, {(float)ell[i].v.re, (float)ell[i].v.im}};
+      upload_vec(gp.ell, e);
     }
   }
   // diagonal sources: one descriptor + local table per group that has diagonal slots
@@ -785,6 +855,13 @@ GatherView GatherPlan::view() const {
   v.coloff = (const int32_t*)coloff.p;
   v.vals = vals.p;
   v.diag = diag.p;
+  v.ell = ell.p;
+  v.ell_slots = ell_slots;
+  v.ell_smem = 0;  // decided per launch from the shared-memory budget
+  v.all_ell = all_ell ? 1 : 0;
+  v.all_w1 = all_w1 ? 1 : 0;
+  v.fast = fast ? 1 : 0;
+  v.fastg = (const int4*)fastg.p;
   return v;
 }
 

@@ -92,9 +92,35 @@ struct GGroup {
   uint32_t mod[kMaxBlocks];
   uint32_t lstride[kMaxBlocks];
   uint32_t support_hi;
-  uint32_t pad_;
+  int32_t width;    // > 0: rows stored as fixed-width (ELL) slots in ell[]; 0: CSR
+  int32_t ell_off;  // first ELL slot of this group (slot = one (coloff, value) pair)
+  int32_t pow2;     // 1: every div and mod is a power of two (shifts[] are valid)
   uint64_t mdiv[kMaxBlocks];  // Lemire magic numbers of div / mod
   uint64_t mmod[kMaxBlocks];
+  uint32_t shifts[kMaxBlocks];  // log2 div | log2 mod << 8 | log2 lstride << 16
+};
+
+// Fixed-width row slots: a row's entries padded with value 0 to the group's
+// width (at most kMaxEllWidth).  One 8/16/32-byte load per slot.
+constexpr int kMaxEllWidth = 8;
+struct EllD {  // FP64, real value
+  int32_t col;
+  int32_t pad;
+  double v;
+};
+struct EllZ {  // FP64, complex value
+  int32_t col;
+  int32_t pad[3];
+  double v[2];
+};
+struct EllF {  // FP32, real value
+  int32_t col;
+  float v;
+};
+struct EllC {  // FP32, complex value
+  int32_t col;
+  int32_t pad;
+  float v[2];
 };
 
 static_assert(sizeof(GGroup) % 8 == 0, "GGroup is copied to shared memory in 8-byte words");
@@ -123,6 +149,13 @@ struct GatherView {
   const int32_t* coloff;
   const void* vals;  // double / double2 / float / float2 by precision and real_vals
   const void* diag;  // same element type as vals, length m
+  const void* ell;   // EllD / EllZ / EllF / EllC slots of the fixed-width groups
+  int32_t ell_slots; // number of ELL slots (all groups)
+  int32_t ell_smem;  // 1: stage the ELL slots in shared memory with the descriptors
+  int32_t all_ell;   // 1: every group has fixed-width slots
+  int32_t all_w1;    // 1: every group has exactly one slot per row
+  int32_t fast;      // 1: fastg holds {log2 div, mod - 1, first slot, 0} per group
+  const int4* fastg; // compact form: one run of power-of-two subsystems, width 1
 };
 
 // A host-side record of how each stored entry is made from the terms, so a
@@ -167,7 +200,13 @@ struct GatherPlan {
   int ngroups = 0;
   int64_t nentries = 0;
   // device arrays
-  DeviceBuf groups, rowptr, coloff, vals, diag;
+  DeviceBuf groups, rowptr, coloff, vals, diag, ell;
+  int32_t ell_slots = 0;
+  bool all_ell = true;
+  bool all_w1 = true;
+  bool fast = false;
+  DeviceBuf fastg;
+  int tc = 0;  // vectors per thread chosen by qob_op_tune (0: automatic)
   DeviceBuf dgroups, dvals;  // diagonal sources: groups + local diagonal tables
   int ndgroups = 0;
   SiteTable sites{};
@@ -253,6 +292,7 @@ void launch_gather(const GatherPlan& g, int precision, const void* x, int64_t xe
                    void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta,
                    cudaStream_t s);
 void launch_build_diag(const GatherPlan& g, cudaStream_t s);
+int gather_tile(const GatherPlan& g, int64_t ncols);
 void launch_scale(int precision, void* y, int64_t rows, int64_t cols, int64_t ld_row,
                   int64_t ld_col, c128 beta, cudaStream_t s);
 void launch_dense(int precision, const void* a, int64_t m, int64_t n, c128 alpha, const void* x,
