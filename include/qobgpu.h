@@ -192,6 +192,70 @@ int qob_dot_noalloc(qob_ctx* ctx, int dtype, const void* x, const void* y, int64
                     double* result, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Batches of uneven applications in one launch (no counterpart in the
+ * reference, which would issue one mul! per operator).  Each item is
+ * y = alpha * op * x + beta * y for one ket (x: op cols, y: op rows, DEVICE
+ * pointers in the batch's dtype); the items may have different operators and
+ * dimensions.  qob_batch_run applies all items: the fused parts of every item
+ * in one persistent launch over equal tiles of their output indices, the rest
+ * per item.  Pointers are captured at qob_batch_add; a run reads the current
+ * contents, so a run recorded in a CUDA graph can be replayed after refilling
+ * the same buffers.
+ * ------------------------------------------------------------------------- */
+typedef struct qob_batch qob_batch;
+int qob_batch_create(qob_ctx* ctx, int dtype, qob_batch** out);
+int qob_batch_add(qob_ctx* ctx, qob_batch* batch, qob_op* op, double alpha_re, double alpha_im,
+                  const void* x, void* y, double beta_re, double beta_im);
+int qob_batch_run(qob_ctx* ctx, qob_batch* batch, void* stream);
+/* Time tile lengths 128 / 256 / 512 / 1024 (times_ms[0..3]) and keep the
+ * fastest; runs the batch 28 times, so the outputs are overwritten. */
+int qob_batch_tune(qob_ctx* ctx, qob_batch* batch, double* times_ms, int* chosen);
+/* info[0] items, [1] items in the fused launch, [2] tiles, [3] tile length,
+ * [4] blocks of the persistent grid. */
+int qob_batch_info(qob_ctx* ctx, qob_batch* batch, int64_t* info);
+int qob_batch_free(qob_ctx* ctx, qob_batch* batch);
+
+/* ---------------------------------------------------------------------------
+ * Time evolution.  qob_rk4 advances a device state by nsteps fixed RK4 steps
+ * of dpsi/dt = -i H psi (the right-hand side QuantumOptics.jl's Schroedinger
+ * solver evaluates with mul!(dpsi, H, psi, -im, 0) on top of this package).
+ * renormalise != 0 rescales psi to unit FP64 norm after every step.
+ * Synchronous on `stream`.
+ * ------------------------------------------------------------------------- */
+int qob_rk4(qob_ctx* ctx, qob_op* H, int dtype, void* psi, int64_t n, double dt, int nsteps,
+            int renormalise, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Request server with continuous batching (no counterpart in the reference).
+ * A request = (H, psi0 on the HOST, nsteps, dt): nsteps RK4 steps of
+ * dpsi/dt = -i H psi.  States and operators stay resident on the device; a
+ * queued request is admitted when fewer than max_active run and its device
+ * memory (4 state vectors) fits both mem_budget and the free device memory;
+ * requests larger than mem_budget are rejected (status -QOB_ERR_OOM).  Each
+ * engine iteration advances every active request by one step in eight batched
+ * launches, so requests that arrive while others run join at the next
+ * iteration.  A request's result does not depend on the others in flight.
+ * Either run the engine on its own thread (qob_server_start / _stop) or drive
+ * it with qob_server_step.
+ * status: 0 queued, 1 running, 2 done, < 0 failed (-error code).
+ * times[0..2]: submit, admit and completion time (seconds, steady clock).
+ * stats[0..7]: queued, active, completed, rejected, request-steps, engine
+ * iterations, device bytes held, last engine error code.
+ * ------------------------------------------------------------------------- */
+typedef struct qob_server qob_server;
+int qob_server_create(qob_ctx* ctx, int dtype, size_t mem_budget, int max_active, int renormalise,
+                      qob_server** out);
+int qob_server_submit(qob_server* server, qob_op* H, const void* psi0, int64_t n, int nsteps,
+                      double dt, int64_t* id);
+int qob_server_step(qob_server* server, int* nactive);
+int qob_server_start(qob_server* server);
+int qob_server_stop(qob_server* server);
+int qob_server_poll(qob_server* server, int64_t id, void* psi_out, double* times, int* status);
+int qob_server_wait(qob_server* server, int64_t id, double timeout_s, int* status);
+int qob_server_stats(qob_server* server, int64_t* stats);
+int qob_server_destroy(qob_server* server);
+
+/* ---------------------------------------------------------------------------
  * CUDA graphs of library calls.  Between qob_graph_begin and qob_graph_end the
  * qob_* calls issued on `stream` (a non-default stream) are recorded instead of
  * run; qob_graph_launch replays them.  Operators used inside must have been

@@ -217,6 +217,15 @@ Plan& get_plan(Context& ctx, qob_op* op, int side, int prec) {
   return *slot;
 }
 
+}  // namespace
+
+namespace qob {
+// The LEFT-side plan of an operator, compiled or refreshed on demand (batch.cu).
+Plan& batch_plan(Context& ctx, qob_op* op, int prec) { return get_plan(ctx, op, QOB_LEFT, prec); }
+}  // namespace qob
+
+namespace {
+
 bool overlaps(const void* a, size_t abytes, const void* b, size_t bbytes) {
   const char* pa = static_cast<const char*>(a);
   const char* pb = static_cast<const char*>(b);

@@ -1,0 +1,578 @@
+// evolve.cu -- fixed-step RK4 time evolution on the device and the
+// continuous-batching request server built on it.
+//
+// Time evolution is the reference's main consumer of mul!: an ODE solver
+// calls mul!(dpsi, H, psi, -im, 0) on every right-hand-side evaluation
+// (QuantumOptics.jl's timeevolution on top of src/operators_lazysum.jl:189).
+// One RK4 step of dpsi/dt = -i H psi is four applications of H plus the
+// stage combinations:
+//   k1 = -iH psi,           acc = k1,        tmp = psi + dt/2 k1
+//   k2 = -iH tmp,           acc += 2 k2,     tmp = psi + dt/2 k2
+//   k3 = -iH tmp,           acc += 2 k3,     tmp = psi + dt k3
+//   k4 = -iH tmp,           psi += dt/6 (acc + k4)
+// Every application and every stage combination of all states in flight runs
+// as one launch (the batch tables of batch.cu), so a step of many requests of
+// different dimensions costs eight launches.  The optional renormalisation
+// computes |psi| in FP64 with a per-request reduction of fixed order, so a
+// request's result does not depend on which other requests share its launches.
+//
+// The server (qob_server_*) keeps states and operators resident on the
+// device, admits queued requests when a slot and device memory (its own
+// budget and cudaMemGetInfo) allow, advances every active request by one RK4
+// step per engine iteration, and retires finished ones with their latency
+// record.  Requests that arrive while others run join at the next iteration.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+
+#include "batch.h"
+
+namespace qob {
+
+struct StageItemDev {
+  void* psi;
+  void* k;
+  void* acc;
+  void* tmp;
+  int64_t n;
+  double dt;
+  int32_t part0;  // first FP64 partial of this item (renormalisation)
+  int32_t nparts;
+};
+
+namespace {
+
+constexpr int kStageTile = 1024;
+
+// Stage combination over all items, tile by tile (element-wise, so the
+// result of an element does not depend on the tiling).
+template <typename CT, typename R>
+__global__ void __launch_bounds__(256) k_rk4_stage(const StageItemDev* __restrict__ items,
+                                                   const int2* __restrict__ tiles, int ntiles, int mode) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int2 td = tiles[t];
+    const StageItemDev& it = items[td.x];
+    const int64_t end = min((int64_t)td.y + kStageTile, it.n);
+    CT* psi = (CT*)it.psi;
+    const CT* k = (const CT*)it.k;
+    CT* acc = (CT*)it.acc;
+    CT* tmp = (CT*)it.tmp;
+    const R dt = (R)it.dt;
+    for (int64_t j = td.y + threadIdx.x; j < end; j += blockDim.x) {
+      const CT kv = k[j];
+      if (mode == 1) {
+        const CT p = psi[j];
+        const R c = dt * (R)0.5;
+        acc[j] = kv;
+        CT o;
+        o.x = p.x + c * kv.x;
+        o.y = p.y + c * kv.y;
+        tmp[j] = o;
+      } else if (mode == 2 || mode == 3) {
+        const CT p = psi[j];
+        const R c = mode == 2 ? dt * (R)0.5 : dt;
+        CT a = acc[j];
+        a.x += (R)2 * kv.x;
+        a.y += (R)2 * kv.y;
+        acc[j] = a;
+        CT o;
+        o.x = p.x + c * kv.x;
+        o.y = p.y + c * kv.y;
+        tmp[j] = o;
+      } else {
+        const CT a = acc[j];
+        CT p = psi[j];
+        const R c = dt / (R)6;
+        p.x += c * (a.x + kv.x);
+        p.y += c * (a.y + kv.y);
+        psi[j] = p;
+      }
+    }
+  }
+}
+
+// |psi|^2 partials in FP64: one partial per (item, tile), tree order fixed.
+template <typename CT>
+__global__ void __launch_bounds__(256) k_norm_partial(const StageItemDev* __restrict__ items,
+                                                      const int2* __restrict__ tiles, int ntiles,
+                                                      double* __restrict__ part) {
+  __shared__ double s[256];
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int2 td = tiles[t];
+    const StageItemDev& it = items[td.x];
+    const int64_t end = min((int64_t)td.y + kStageTile, it.n);
+    const CT* psi = (const CT*)it.psi;
+    double a = 0.0;
+    for (int64_t j = td.y + threadIdx.x; j < end; j += blockDim.x) {
+      const CT p = psi[j];
+      a = fma((double)p.x, (double)p.x, a);
+      a = fma((double)p.y, (double)p.y, a);
+    }
+    __syncthreads();
+    s[threadIdx.x] = a;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+      if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) part[it.part0 + (td.y / kStageTile)] = s[0];
+  }
+}
+
+// psi /= |psi| per item; the item's partials are added in index order.
+template <typename CT, typename R>
+__global__ void __launch_bounds__(256) k_renormalise(const StageItemDev* __restrict__ items,
+                                                     const int2* __restrict__ tiles, int ntiles,
+                                                     const double* __restrict__ part) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int2 td = tiles[t];
+    const StageItemDev& it = items[td.x];
+    double nn = 0.0;
+    for (int q = 0; q < it.nparts; ++q) nn += part[it.part0 + q];
+    const R inv = nn > 0.0 ? (R)(1.0 / sqrt(nn)) : (R)1;
+    const int64_t end = min((int64_t)td.y + kStageTile, it.n);
+    CT* psi = (CT*)it.psi;
+    for (int64_t j = td.y + threadIdx.x; j < end; j += blockDim.x) {
+      CT p = psi[j];
+      p.x *= inv;
+      p.y *= inv;
+      psi[j] = p;
+    }
+  }
+}
+
+}  // namespace
+
+// Device tables of an ensemble of states being evolved together.
+struct Ensemble {
+  int prec = QOB_C128;
+  std::vector<BatchSpec> from_psi, from_tmp;  // k = -i H psi  /  k = -i H tmp
+  BatchTables g_psi, g_tmp;
+  DeviceBuf stage_items, stage_tiles, partials;
+  int stage_ntiles = 0;
+  int grid = 1;
+  bool renormalise = false;
+};
+
+struct EvolveState {
+  Plan* plan;
+  void* psi;
+  void* k;
+  void* acc;
+  void* tmp;
+  int64_t n;
+  double dt;
+};
+
+void ensemble_build(Context& ctx, Ensemble& E, const std::vector<EvolveState>& states, int prec) {
+  E.prec = prec;
+  E.from_psi.clear();
+  E.from_tmp.clear();
+  std::vector<StageItemDev> items;
+  std::vector<int2> tiles;
+  int32_t nparts = 0;
+  for (size_t i = 0; i < states.size(); ++i) {
+    const EvolveState& s = states[i];
+    E.from_psi.push_back({s.plan, s.psi, s.k, {0.0, -1.0}, {0.0, 0.0}});
+    E.from_tmp.push_back({s.plan, s.tmp, s.k, {0.0, -1.0}, {0.0, 0.0}});
+    StageItemDev d;
+    d.psi = s.psi;
+    d.k = s.k;
+    d.acc = s.acc;
+    d.tmp = s.tmp;
+    d.n = s.n;
+    d.dt = s.dt;
+    d.part0 = nparts;
+    d.nparts = (int32_t)((s.n + kStageTile - 1) / kStageTile);
+    nparts += d.nparts;
+    for (int64_t j = 0; j < s.n; j += kStageTile) tiles.push_back(make_int2((int)i, (int)j));
+    items.push_back(d);
+  }
+  build_tables(ctx, E.g_psi, E.from_psi, prec, 256);
+  build_tables(ctx, E.g_tmp, E.from_tmp, prec, 256);
+  E.stage_ntiles = (int)tiles.size();
+  if (!items.empty()) {
+    E.stage_items.upload(items.data(), items.size() * sizeof(StageItemDev));
+    E.stage_tiles.upload(tiles.data(), tiles.size() * sizeof(int2));
+    if (E.partials.bytes < (size_t)nparts * sizeof(double)) E.partials.alloc((size_t)std::max(nparts, 1) * sizeof(double));
+  }
+  E.grid = std::max(1, std::min(E.stage_ntiles, ctx.num_sms * 8));
+}
+
+void ensemble_step(Context& ctx, Ensemble& E, cudaStream_t s) {
+  if (E.stage_ntiles == 0) return;
+  const StageItemDev* it = (const StageItemDev*)E.stage_items.p;
+  const int2* tl = (const int2*)E.stage_tiles.p;
+  for (int mode = 1; mode <= 4; ++mode) {
+    launch_tables(ctx, mode == 1 ? E.g_psi : E.g_tmp, mode == 1 ? E.from_psi : E.from_tmp, s);
+    if (E.prec == QOB_C128)
+      k_rk4_stage<double2, double><<<E.grid, 256, 0, s>>>(it, tl, E.stage_ntiles, mode);
+    else
+      k_rk4_stage<float2, float><<<E.grid, 256, 0, s>>>(it, tl, E.stage_ntiles, mode);
+    QOB_LAUNCHED();
+  }
+  if (E.renormalise) {
+    double* part = (double*)E.partials.p;
+    if (E.prec == QOB_C128) {
+      k_norm_partial<double2><<<E.grid, 256, 0, s>>>(it, tl, E.stage_ntiles, part);
+      QOB_LAUNCHED();
+      k_renormalise<double2, double><<<E.grid, 256, 0, s>>>(it, tl, E.stage_ntiles, part);
+    } else {
+      k_norm_partial<float2><<<E.grid, 256, 0, s>>>(it, tl, E.stage_ntiles, part);
+      QOB_LAUNCHED();
+      k_renormalise<float2, float><<<E.grid, 256, 0, s>>>(it, tl, E.stage_ntiles, part);
+    }
+    QOB_LAUNCHED();
+  }
+}
+
+}  // namespace qob
+
+// ---------------------------------------------------------------------------
+// server
+// ---------------------------------------------------------------------------
+namespace {
+
+using Clock = std::chrono::steady_clock;
+double now_s() { return std::chrono::duration<double>(Clock::now().time_since_epoch()).count(); }
+
+struct Request {
+  int64_t id = 0;
+  qob_op* op = nullptr;
+  int64_t n = 0;
+  int nsteps = 0;
+  int step = 0;
+  double dt = 0.0;
+  int status = 0;  // 0 queued, 1 active, 2 done, negative: error code
+  std::vector<char> psi0, result;
+  double t_submit = 0, t_admit = 0, t_done = 0;
+  void* dev = nullptr;
+  size_t bytes = 0;
+  qob::Plan* plan = nullptr;
+};
+
+}  // namespace
+
+struct qob_server {
+  qob_ctx* ctx = nullptr;
+  int dtype = QOB_C128;
+  size_t budget = 0;
+  int max_active = 64;
+  bool renormalise = false;
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<Request*> queue;
+  std::vector<Request*> active;
+  std::unordered_map<int64_t, std::unique_ptr<Request>> all;
+  int64_t next_id = 1;
+  size_t mem_used = 0;
+  cudaStream_t stream = nullptr;
+  qob::Ensemble ens;
+  bool dirty = true;
+  std::thread worker;
+  bool stop = false;
+  bool running = false;
+  int64_t steps_run = 0, iterations = 0, rejected = 0, completed = 0;
+  int last_error = 0;
+  std::string last_msg;
+};
+
+namespace {
+
+size_t elem_bytes(int dtype) { return dtype == QOB_C128 ? 16 : 8; }
+
+// Admit queued requests while a slot and memory are free (lock held).
+void admit(qob_server* S) {
+  while (!S->queue.empty() && (int)S->active.size() < S->max_active) {
+    Request* r = S->queue.front();
+    const size_t need = 4 * (size_t)r->n * elem_bytes(S->dtype);
+    size_t free_b = 0, total_b = 0;
+    QOB_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    if (S->mem_used + need > S->budget || need + (size_t(256) << 20) > free_b) break;  // wait for memory
+    QOB_CUDA(cudaMallocAsync(&r->dev, need, S->stream));
+    r->bytes = need;
+    S->mem_used += need;
+    QOB_CUDA(cudaMemcpyAsync(r->dev, r->psi0.data(), r->psi0.size(), cudaMemcpyHostToDevice, S->stream));
+    r->plan = &qob::batch_plan(S->ctx->c, r->op, S->dtype);
+    r->status = 1;
+    r->t_admit = now_s();
+    S->queue.pop_front();
+    S->active.push_back(r);
+    S->dirty = true;
+  }
+}
+
+// One engine iteration: admit, one RK4 step of every active request, retire.
+// Returns the number of active requests after the step.
+int iterate(qob_server* S) {
+  std::vector<Request*> act;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    admit(S);
+    act = S->active;
+  }
+  if (act.empty()) return 0;
+  qob::Context& ctx = S->ctx->c;
+  if (S->dirty) {
+    std::vector<qob::EvolveState> states;
+    for (Request* r : act) {
+      const size_t sz = (size_t)r->n * elem_bytes(S->dtype);
+      char* base = static_cast<char*>(r->dev);
+      states.push_back({r->plan, base, base + sz, base + 2 * sz, base + 3 * sz, r->n, r->dt});
+    }
+    S->ens.renormalise = S->renormalise;
+    qob::ensemble_build(ctx, S->ens, states, S->dtype);
+    S->dirty = false;
+  }
+  qob::ensemble_step(ctx, S->ens, S->stream);
+  QOB_CUDA(cudaStreamSynchronize(S->stream));
+  S->iterations++;
+  std::vector<Request*> finished;
+  for (Request* r : act) {
+    r->step++;
+    S->steps_run++;
+    if (r->step >= r->nsteps) finished.push_back(r);
+  }
+  for (Request* r : finished) {
+    r->result.resize(r->psi0.size());
+    QOB_CUDA(cudaMemcpyAsync(r->result.data(), r->dev, r->result.size(), cudaMemcpyDeviceToHost, S->stream));
+  }
+  if (!finished.empty()) {
+    QOB_CUDA(cudaStreamSynchronize(S->stream));
+    std::lock_guard<std::mutex> lk(S->mu);
+    const double t = now_s();
+    for (Request* r : finished) {
+      QOB_CUDA(cudaFreeAsync(r->dev, S->stream));
+      S->mem_used -= r->bytes;
+      r->dev = nullptr;
+      r->status = 2;
+      r->t_done = t;
+      S->completed++;
+      S->active.erase(std::find(S->active.begin(), S->active.end(), r));
+    }
+    S->dirty = true;
+    S->cv.notify_all();
+  }
+  std::lock_guard<std::mutex> lk(S->mu);
+  return (int)S->active.size();
+}
+
+void worker_loop(qob_server* S) {
+  cudaSetDevice(S->ctx->c.device);
+  while (true) {
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv.wait_for(lk, std::chrono::milliseconds(2),
+                     [&] { return S->stop || !S->queue.empty() || !S->active.empty(); });
+      if (S->stop) break;
+      if (S->queue.empty() && S->active.empty()) continue;
+    }
+    int code = 0;
+    std::string msg;
+    try {
+      iterate(S);
+    } catch (const qob::Error& e) {
+      code = e.code;
+      msg = e.msg;
+    } catch (const std::exception& e) {
+      code = QOB_ERR_ARG;
+      msg = e.what();
+    }
+    if (code) {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->last_error = code;
+      S->last_msg = msg;
+      // fail the requests in flight; the server keeps serving new ones
+      for (Request* r : S->active) {
+        r->status = -code;
+        r->t_done = now_s();
+      }
+      S->active.clear();
+      S->dirty = true;
+      S->cv.notify_all();
+    }
+  }
+}
+
+template <class F>
+int sguard(qob_server* S, F&& f) {
+  if (!S || !S->ctx) return QOB_ERR_ARG;
+  try {
+    QOB_CUDA(cudaSetDevice(S->ctx->c.device));
+    f();
+    return QOB_OK;
+  } catch (const qob::Error& e) {
+    S->ctx->c.err = e.msg;
+    return e.code;
+  } catch (const std::exception& e) {
+    S->ctx->c.err = e.what();
+    return QOB_ERR_ARG;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int qob_server_create(qob_ctx* ctx, int dtype, size_t mem_budget, int max_active, int renormalise,
+                      qob_server** out) {
+  if (!ctx || !out || (dtype != QOB_C128 && dtype != QOB_C64) || max_active < 1) return QOB_ERR_ARG;
+  auto* S = new qob_server;
+  S->ctx = ctx;
+  S->dtype = dtype;
+  S->budget = mem_budget;
+  S->max_active = max_active;
+  S->renormalise = renormalise != 0;
+  int rc = sguard(S, [&] { QOB_CUDA(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking)); });
+  if (rc) {
+    delete S;
+    return rc;
+  }
+  *out = S;
+  return QOB_OK;
+}
+
+int qob_server_submit(qob_server* S, qob_op* H, const void* psi0, int64_t n, int nsteps, double dt,
+                      int64_t* id) {
+  return sguard(S, [&] {
+    if (!H || !psi0 || n < 1 || nsteps < 0 || !id) qob::fail(QOB_ERR_ARG, "qob_server_submit: bad arguments");
+    if (H->node->m != n || H->node->n != n) qob::fail(QOB_ERR_DIM, "Hamiltonian and state dimensions differ");
+    auto r = std::make_unique<Request>();
+    r->op = H;
+    r->n = n;
+    r->nsteps = nsteps;
+    r->dt = dt;
+    const size_t bytes = (size_t)n * elem_bytes(S->dtype);
+    r->psi0.assign(static_cast<const char*>(psi0), static_cast<const char*>(psi0) + bytes);
+    r->t_submit = now_s();
+    std::lock_guard<std::mutex> lk(S->mu);
+    r->id = S->next_id++;
+    *id = r->id;
+    if (4 * bytes > S->budget) {  // can never be admitted
+      r->status = -QOB_ERR_OOM;
+      r->t_done = r->t_submit;
+      S->rejected++;
+    } else {
+      S->queue.push_back(r.get());
+    }
+    S->all[r->id] = std::move(r);
+    S->cv.notify_all();
+  });
+}
+
+int qob_server_step(qob_server* S, int* nactive) {
+  return sguard(S, [&] {
+    if (S->running) qob::fail(QOB_ERR_STATE, "the server's worker thread is running");
+    const int a = iterate(S);
+    if (nactive) *nactive = a;
+  });
+}
+
+int qob_server_start(qob_server* S) {
+  return sguard(S, [&] {
+    if (S->running) return;
+    S->stop = false;
+    S->running = true;
+    S->worker = std::thread(worker_loop, S);
+  });
+}
+
+int qob_server_stop(qob_server* S) {
+  return sguard(S, [&] {
+    if (!S->running) return;
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->stop = true;
+      S->cv.notify_all();
+    }
+    S->worker.join();
+    S->running = false;
+  });
+}
+
+int qob_server_poll(qob_server* S, int64_t id, void* psi_out, double* times, int* status) {
+  return sguard(S, [&] {
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->all.find(id);
+    if (it == S->all.end()) qob::fail(QOB_ERR_ARG, "unknown request id");
+    Request* r = it->second.get();
+    if (status) *status = r->status;
+    if (times) {
+      times[0] = r->t_submit;
+      times[1] = r->t_admit;
+      times[2] = r->t_done;
+    }
+    if (r->status == 2 && psi_out) std::memcpy(psi_out, r->result.data(), r->result.size());
+  });
+}
+
+int qob_server_wait(qob_server* S, int64_t id, double timeout_s, int* status) {
+  return sguard(S, [&] {
+    std::unique_lock<std::mutex> lk(S->mu);
+    auto it = S->all.find(id);
+    if (it == S->all.end()) qob::fail(QOB_ERR_ARG, "unknown request id");
+    Request* r = it->second.get();
+    const bool ok = S->cv.wait_for(lk, std::chrono::duration<double>(timeout_s), [&] { return r->status >= 2 || r->status < 0; });
+    if (status) *status = r->status;
+    if (!ok) qob::fail(QOB_ERR_TIMEOUT, "request did not finish in time");
+  });
+}
+
+int qob_server_stats(qob_server* S, int64_t* out) {
+  return sguard(S, [&] {
+    std::lock_guard<std::mutex> lk(S->mu);
+    out[0] = (int64_t)S->queue.size();
+    out[1] = (int64_t)S->active.size();
+    out[2] = S->completed;
+    out[3] = S->rejected;
+    out[4] = S->steps_run;
+    out[5] = S->iterations;
+    out[6] = (int64_t)S->mem_used;
+    out[7] = S->last_error;
+  });
+}
+
+int qob_server_destroy(qob_server* S) {
+  if (!S) return QOB_ERR_ARG;
+  qob_server_stop(S);
+  cudaSetDevice(S->ctx->c.device);
+  for (Request* r : S->active)
+    if (r->dev) cudaFreeAsync(r->dev, S->stream);
+  if (S->stream) {
+    cudaStreamSynchronize(S->stream);
+    cudaStreamDestroy(S->stream);
+  }
+  delete S;
+  return QOB_OK;
+}
+
+// Single-state RK4: nsteps steps of dpsi/dt = -i H psi on device state psi.
+int qob_rk4(qob_ctx* ctx, qob_op* H, int dtype, void* psi, int64_t n, double dt, int nsteps, int renormalise,
+            void* stream) {
+  if (!ctx) return QOB_ERR_ARG;
+  try {
+    QOB_CUDA(cudaSetDevice(ctx->c.device));
+    if (!H || !psi || n < 1 || (dtype != QOB_C128 && dtype != QOB_C64)) qob::fail(QOB_ERR_ARG, "qob_rk4: bad arguments");
+    if (H->node->m != n || H->node->n != n) qob::fail(QOB_ERR_DIM, "Hamiltonian and state dimensions differ");
+    const size_t sz = (size_t)n * (dtype == QOB_C128 ? 16 : 8);
+    char* w = static_cast<char*>(ctx->c.ws.get(20, 3 * sz));
+    qob::Plan& P = qob::batch_plan(ctx->c, H, dtype);
+    qob::Ensemble E;
+    E.renormalise = renormalise != 0;
+    qob::ensemble_build(ctx->c, E, {qob::EvolveState{&P, psi, w, w + sz, w + 2 * sz, n, dt}}, dtype);
+    for (int s = 0; s < nsteps; ++s) qob::ensemble_step(ctx->c, E, (cudaStream_t)stream);
+    QOB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    return QOB_OK;
+  } catch (const qob::Error& e) {
+    ctx->c.err = e.msg;
+    return e.code;
+  }
+}
+
+}  // extern "C"

@@ -56,6 +56,22 @@ SIGNATURES = {
     "qob_dot": (I, [VP, I, VP, VP, I64, DP, VP]),
     "qob_expect": (I, [VP, VP, I, VP, I64, DP, VP]),
     "qob_dot_noalloc": (I, [VP, I, VP, VP, I64, VP, VP]),
+    "qob_batch_create": (I, [VP, I, C.POINTER(VP)]),
+    "qob_batch_add": (I, [VP, VP, VP, D, D, VP, VP, D, D]),
+    "qob_batch_run": (I, [VP, VP, VP]),
+    "qob_batch_tune": (I, [VP, VP, DP, C.POINTER(C.c_int)]),
+    "qob_batch_info": (I, [VP, VP, I64P]),
+    "qob_batch_free": (I, [VP, VP]),
+    "qob_rk4": (I, [VP, VP, I, VP, I64, D, I, I, VP]),
+    "qob_server_create": (I, [VP, I, C.c_size_t, I, I, C.POINTER(VP)]),
+    "qob_server_submit": (I, [VP, VP, VP, I64, I, D, I64P]),
+    "qob_server_step": (I, [VP, C.POINTER(C.c_int)]),
+    "qob_server_start": (I, [VP]),
+    "qob_server_stop": (I, [VP]),
+    "qob_server_poll": (I, [VP, I64, VP, DP, C.POINTER(C.c_int)]),
+    "qob_server_wait": (I, [VP, I64, D, C.POINTER(C.c_int)]),
+    "qob_server_stats": (I, [VP, I64P]),
+    "qob_server_destroy": (I, [VP]),
     "qob_graph_begin": (I, [VP, VP]),
     "qob_graph_end": (I, [VP, VP, C.POINTER(VP)]),
     "qob_graph_launch": (I, [VP, VP, VP]),

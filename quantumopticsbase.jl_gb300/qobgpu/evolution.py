@@ -1,0 +1,144 @@
+"""Batched application, RK4 time evolution and the request server (device side).
+
+* ``Batch`` -- many (operator, x, y, alpha, beta) applications of uneven size
+  run as one persistent launch (``qob_batch_*``).
+* ``rk4(H, psi, dt, nsteps)`` -- fixed-step RK4 of dpsi/dt = -i H psi on a
+  device state (``qob_rk4``).
+* ``Server`` -- continuous-batching request loop for short time evolutions
+  (``qob_server_*``): states and operators stay on the device, requests are
+  admitted by free device memory, finished ones report their latency.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .device import Context, dtype_code, get_context, handle, raise_for
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+class Batch:
+    """y_i = alpha_i * op_i * x_i + beta_i * y_i for many kets in one launch."""
+
+    def __init__(self, dtype=np.complex128, device: int = 0):
+        self.ctx = get_context(device)
+        self.dtype = np.dtype(dtype)
+        p = C.c_void_p()
+        raise_for(L.lib().qob_batch_create(self.ctx.ptr, dtype_code(self.dtype), C.byref(p)), self.ctx)
+        self.ptr = p
+        self._keep = []
+
+    def add(self, op, x, y, alpha=1.0, beta=0.0):
+        """x, y: contiguous CUDA tensors of the batch's dtype (kept alive by the batch)."""
+        h = handle(self.ctx, op)
+        a, b = complex(alpha), complex(beta)
+        raise_for(L.lib().qob_batch_add(self.ctx.ptr, self.ptr, h.ptr, a.real, a.imag, _ptr(x), _ptr(y), b.real,
+                                        b.imag), self.ctx)
+        self._keep.append((h, x, y))
+
+    def run(self, stream=None):
+        raise_for(L.lib().qob_batch_run(self.ctx.ptr, self.ptr, stream), self.ctx)
+
+    def tune(self):
+        t = (C.c_double * 4)()
+        ch = C.c_int()
+        raise_for(L.lib().qob_batch_tune(self.ctx.ptr, self.ptr, t, C.byref(ch)), self.ctx)
+        return ch.value, list(t)
+
+    def info(self):
+        v = (C.c_int64 * 5)()
+        raise_for(L.lib().qob_batch_info(self.ctx.ptr, self.ptr, v), self.ctx)
+        return {"items": v[0], "fused": v[1], "tiles": v[2], "tile": v[3], "grid": v[4]}
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                L.lib().qob_batch_free(self.ctx.ptr, self.ptr)
+        except Exception:
+            pass
+
+
+def rk4(H, psi, dt: float, nsteps: int, renormalise: bool = False):
+    """In-place RK4 on a device Ket (or a contiguous CUDA tensor)."""
+    data = psi.data if hasattr(psi, "data") and not hasattr(psi, "data_ptr") else psi
+    ctx = get_context(data.device.index)
+    h = handle(ctx, H)
+    import torch
+
+    dt_code = L.QOB_C64 if data.dtype == torch.complex64 else L.QOB_C128
+    s = C.c_void_p(torch.cuda.current_stream(data.device.index).cuda_stream)
+    raise_for(L.lib().qob_rk4(ctx.ptr, h.ptr, dt_code, _ptr(data), data.shape[0], float(dt), int(nsteps),
+                              int(renormalise), s), ctx)
+    return psi
+
+
+class Server:
+    """Continuous-batching server of RK4 time-evolution requests."""
+
+    def __init__(self, dtype=np.complex128, mem_budget: int = 8 << 30, max_active: int = 256,
+                 renormalise: bool = False, device: int = 0):
+        self.ctx: Context = get_context(device)
+        self.dtype = np.dtype(dtype)
+        p = C.c_void_p()
+        raise_for(L.lib().qob_server_create(self.ctx.ptr, dtype_code(self.dtype), int(mem_budget), int(max_active),
+                                            int(renormalise), C.byref(p)), self.ctx)
+        self.ptr = p
+        self._ops = {}
+        self._sizes = {}
+
+    def submit(self, H, psi0: np.ndarray, nsteps: int, dt: float) -> int:
+        h = handle(self.ctx, H)
+        self._ops[id(H)] = (H, h)
+        a = np.ascontiguousarray(psi0, dtype=self.dtype)
+        rid = C.c_int64()
+        raise_for(L.lib().qob_server_submit(self.ptr, h.ptr, a.ctypes.data_as(C.c_void_p), a.shape[0], int(nsteps),
+                                            float(dt), C.byref(rid)), self.ctx)
+        self._sizes[rid.value] = a.shape[0]
+        return rid.value
+
+    def step(self) -> int:
+        n = C.c_int()
+        raise_for(L.lib().qob_server_step(self.ptr, C.byref(n)), self.ctx)
+        return n.value
+
+    def start(self):
+        raise_for(L.lib().qob_server_start(self.ptr), self.ctx)
+
+    def stop(self):
+        raise_for(L.lib().qob_server_stop(self.ptr), self.ctx)
+
+    def poll(self, rid: int):
+        """(status, times[submit, admit, done], result or None)."""
+        out = np.empty(self._sizes[rid], dtype=self.dtype)
+        t = (C.c_double * 3)()
+        st = C.c_int()
+        raise_for(L.lib().qob_server_poll(self.ptr, rid, out.ctypes.data_as(C.c_void_p), t, C.byref(st)), self.ctx)
+        return st.value, list(t), (out if st.value == 2 else None)
+
+    def wait(self, rid: int, timeout: float = 60.0) -> int:
+        st = C.c_int()
+        raise_for(L.lib().qob_server_wait(self.ptr, rid, float(timeout), C.byref(st)), self.ctx)
+        return st.value
+
+    def stats(self):
+        v = (C.c_int64 * 8)()
+        raise_for(L.lib().qob_server_stats(self.ptr, v), self.ctx)
+        keys = ["queued", "active", "completed", "rejected", "request_steps", "iterations", "device_bytes",
+                "last_error"]
+        return dict(zip(keys, list(v)))
+
+    def close(self):
+        if self.ptr:
+            L.lib().qob_server_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
