@@ -63,6 +63,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-graph", action="store_true", help="direct launches (used for ncu captures)")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--suite", action="store_true", help="secondary workloads, one JSON line each")
     return p.parse_args()
 
 
@@ -414,6 +415,10 @@ def main():
     import __graft_entry__ as g
 
     g.build()
+    if args.suite:
+        from qobgpu.suite import run_suite
+
+        return run_suite(local_rank)
     run_own(args, rank, world, local_rank)
 
 

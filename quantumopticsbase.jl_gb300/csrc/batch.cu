@@ -108,7 +108,7 @@ void build_tables(Context& ctx, BatchTables& T, const std::vector<BatchSpec>& sp
     d.v = g.view();
     size_t smem = (size_t)d.v.ngroups * (sizeof(GGroup) + (d.v.fast ? sizeof(int4) : 0));
     const size_t eb = (size_t)d.v.ell_slots * ell_size(prec, T.real);
-    d.v.ell_smem = (d.v.ell_slots > 0 && smem + eb <= kBatchSmemBudget) ? 1 : 0;
+    d.v.ell_smem = (d.v.ell_slots > 0 && eb <= gather::kStageSlotsMax && smem + eb <= kBatchSmemBudget) ? 1 : 0;
     if (d.v.ell_smem) smem += eb;
     T.smem = std::max(T.smem, smem);
     d.x = specs[i].x;

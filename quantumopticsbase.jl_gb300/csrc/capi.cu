@@ -51,6 +51,8 @@ void* Workspace::get(size_t slot, size_t bytes) {
 
 Context::~Context() {
   if (reduce_host) cudaFreeHost(reduce_host);
+  for (auto s : copy_stream)
+    if (s) cudaStreamDestroy(s);
 }
 
 namespace {
@@ -541,6 +543,42 @@ int qob_mul(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, double
 int qob_mul_host(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, double alpha_re, double alpha_im,
                  const void* x, int64_t x_rows, int64_t x_cols, double beta_re, double beta_im, void* y,
                  int64_t y_rows, int64_t y_cols) {
+  const bool has_beta = beta_re != 0.0 || beta_im != 0.0;
+  // Several kets from the left: pipeline chunks of columns over two streams so
+  // the copies of one chunk overlap the kernels of the other.
+  if (side == QOB_LEFT && x_cols >= 8 && x_cols == y_cols) {
+    return guard(ctx, [&] {
+      if (!ctx || !op || !x || !y) fail(QOB_ERR_ARG, "null argument");
+      check_dtype(dtype);
+      if (x_rows != op->node->n || y_rows != op->node->m)
+        fail(QOB_ERR_DIM, "A and B dimensions do not match. Can't do `A*B`");
+      const size_t esz = dtype == QOB_C128 ? 16 : 8;
+      const size_t xb = (size_t)x_rows * x_cols * esz, yb = (size_t)y_rows * y_cols * esz;
+      if (ctx->c.host_x.bytes < xb) ctx->c.host_x.alloc(xb);
+      if (ctx->c.host_y.bytes < yb) ctx->c.host_y.alloc(yb);
+      for (int k = 0; k < 2; ++k)
+        if (!ctx->c.copy_stream[k]) QOB_CUDA(cudaStreamCreateWithFlags(&ctx->c.copy_stream[k], cudaStreamNonBlocking));
+      Plan& P = get_plan(ctx->c, op, QOB_LEFT, dtype);
+      const int64_t nchunk = std::min<int64_t>(4, x_cols / 4);
+      const int64_t per = (x_cols + nchunk - 1) / nchunk;
+      for (int64_t c0 = 0, k = 0; c0 < x_cols; c0 += per, ++k) {
+        const int64_t nc = std::min(per, x_cols - c0);
+        cudaStream_t s = ctx->c.copy_stream[k % 2];
+        char* dx = static_cast<char*>(ctx->c.host_x.p) + (size_t)c0 * x_rows * esz;
+        char* dy = static_cast<char*>(ctx->c.host_y.p) + (size_t)c0 * y_rows * esz;
+        const char* hx = static_cast<const char*>(x) + (size_t)c0 * x_rows * esz;
+        char* hy = static_cast<char*>(y) + (size_t)c0 * y_rows * esz;
+        QOB_CUDA(cudaMemcpyAsync(dx, hx, (size_t)nc * x_rows * esz, cudaMemcpyHostToDevice, s));
+        if (has_beta) QOB_CUDA(cudaMemcpyAsync(dy, hy, (size_t)nc * y_rows * esz, cudaMemcpyHostToDevice, s));
+        // the two streams use workspace slots of their own
+        apply_plan(ctx->c, P, {alpha_re, alpha_im}, dx, 1, x_rows, {beta_re, beta_im}, dy, 1, y_rows, nc, s,
+                   24 + 8 * (int)(k % 2));
+        QOB_CUDA(cudaMemcpyAsync(hy, dy, (size_t)nc * y_rows * esz, cudaMemcpyDeviceToHost, s));
+      }
+      QOB_CUDA(cudaStreamSynchronize(ctx->c.copy_stream[0]));
+      QOB_CUDA(cudaStreamSynchronize(ctx->c.copy_stream[1]));
+    });
+  }
   int rc = guard(ctx, [&] {
     if (!ctx || !op || !x || !y) fail(QOB_ERR_ARG, "null argument");
     check_dtype(dtype);
@@ -549,8 +587,7 @@ int qob_mul_host(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, d
     if (ctx->c.host_x.bytes < xb) ctx->c.host_x.alloc(xb);
     if (ctx->c.host_y.bytes < yb) ctx->c.host_y.alloc(yb);
     QOB_CUDA(cudaMemcpyAsync(ctx->c.host_x.p, x, xb, cudaMemcpyHostToDevice, 0));
-    if (beta_re != 0.0 || beta_im != 0.0)
-      QOB_CUDA(cudaMemcpyAsync(ctx->c.host_y.p, y, yb, cudaMemcpyHostToDevice, 0));
+    if (has_beta) QOB_CUDA(cudaMemcpyAsync(ctx->c.host_y.p, y, yb, cudaMemcpyHostToDevice, 0));
   });
   if (rc) return rc;
   rc = qob_mul(ctx, side, is_vector, op, dtype, alpha_re, alpha_im, ctx->c.host_x.p, x_rows, x_cols,

@@ -441,6 +441,10 @@ __global__ void __launch_bounds__(256) k_gather_c(GatherView g, SiteTable st,
 // host-side dispatch (instantiated per precision)
 
 constexpr size_t kSmemBudget = 96 * 1024;  // descriptors + staged slots per block
+// Slots are staged per block only when the table is small: local operators
+// (bonds, couplings) are read by every row, while a full-space sparse operator's
+// table is read one block-sized slice per block and stays in L1/L2.
+constexpr size_t kStageSlotsMax = 16 * 1024;
 constexpr int kThreads = 256;
 
 template <typename K>
@@ -491,7 +495,7 @@ void dispatch_layout(const GatherView& v, const SiteTable& st, int tc, const voi
   GatherView w = v;
   size_t smem = (size_t)v.ngroups * (sizeof(GGroup) + (v.fast ? sizeof(int4) : 0));
   const size_t ell_bytes = (size_t)v.ell_slots * sizeof(ET);
-  w.ell_smem = (v.ell_slots > 0 && smem + ell_bytes <= kSmemBudget) ? 1 : 0;
+  w.ell_smem = (v.ell_slots > 0 && ell_bytes <= kStageSlotsMax && smem + ell_bytes <= kSmemBudget) ? 1 : 0;
   if (w.ell_smem) smem += ell_bytes;
   if (xes == 1 && yes == 1) {
     if (SQUARE && v.all_w1)

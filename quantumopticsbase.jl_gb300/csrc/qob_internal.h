@@ -279,6 +279,7 @@ struct Context {
   DeviceBuf reduce_buf;
   void* reduce_host = nullptr;  // pinned
   DeviceBuf host_x, host_y;     // staging for qob_mul_host
+  cudaStream_t copy_stream[2] = {nullptr, nullptr};  // qob_mul_host's copy/compute pipeline
   ~Context();
 };
 

@@ -1,0 +1,231 @@
+"""Secondary workloads of the benchmark (``python bench.py --suite``).
+
+One JSON line per workload, each timed with CUDA events on the launching
+stream (device-resident data, CUDA-graph replay where the workload is a fixed
+launch sequence) or, for the served stream, with the host clock around request
+submission and completion:
+
+* ``jc512``       Jaynes-Cummings LazySum, FockBasis(15) x Spin(1/2) x FockBasis(15),
+                  mul!(out, H, psi, 0.7-0.2i, 0.3) on one ket and on 64 kets;
+* ``sparse4096``  sparse(H) of the 32 x 2 x 64 Jaynes-Cummings model: SpMV on a ket
+                  and SpMM on 256 columns of a density matrix, FP64 and FP32;
+* ``rho_h8``      mul!(rho', rho, H) and mul!(rho', H, rho) with the 8-spin
+                  Heisenberg chain on a 256 x 256 operator;
+* ``cavities256`` 256 two-mode cavity models (dims 81 ... 4225) in one launch;
+* ``served``      Poisson arrivals of 100-step RK4 requests (Heisenberg chains of
+                  8 ... 16 spins, Jaynes-Cummings models of dim 512 ... 8192).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import time
+
+import numpy as np
+
+from . import _lib as L
+from .device import dtype_code, get_context, handle, raise_for
+from .hamiltonians import (heisenberg_chain, jaynes_cummings, jaynes_cummings_sparse, random_density_columns,
+                           two_mode_cavity)
+from .rng import Rng
+
+
+def _timed_graph(ctx, stream, record, reps=20):
+    """ms per replay of a graph that `record()` issues on `stream`."""
+    import torch
+
+    lib = L.lib()
+    sp = C.c_void_p(stream.cuda_stream)
+    record(sp)  # warm-up: compiles plans, sizes workspaces
+    stream.synchronize()
+    g = C.c_void_p()
+    raise_for(lib.qob_graph_begin(ctx.ptr, sp), ctx)
+    record(sp)
+    raise_for(lib.qob_graph_end(ctx.ptr, sp, C.byref(g)), ctx)
+    for _ in range(3):
+        lib.qob_graph_launch(ctx.ptr, g, sp)
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        lib.qob_graph_launch(ctx.ptr, g, sp)
+    e1.record(stream)
+    e1.synchronize()
+    lib.qob_graph_free(ctx.ptr, g)
+    return e0.elapsed_time(e1) / reps
+
+
+def _cols(n, k, dt, seed):
+    import torch
+
+    g = torch.Generator(device="cuda:0")
+    g.manual_seed(seed)
+    t = torch.randn(k, n, dtype=dt, device="cuda:0", generator=g)
+    return t.t()  # column-major n x k
+
+
+def _mul_recorder(ctx, h, side, n_out, n_in, ncols, x, y, code, alpha=0.7 - 0.2j, beta=0.3, reps=1):
+    lib = L.lib()
+
+    def rec(sp):
+        for _ in range(reps):
+            if side == L.QOB_LEFT:
+                rc = lib.qob_mul(ctx.ptr, L.QOB_LEFT, int(ncols == 1), h.ptr, code, alpha.real, alpha.imag,
+                                 C.c_void_p(x.data_ptr()), n_in, ncols, n_in, beta, 0.0, C.c_void_p(y.data_ptr()),
+                                 n_out, ncols, n_out, sp)
+            else:
+                rows = x.shape[0]
+                rc = lib.qob_mul(ctx.ptr, L.QOB_RIGHT, 0, h.ptr, code, alpha.real, alpha.imag,
+                                 C.c_void_p(x.data_ptr()), rows, n_in, rows, beta, 0.0, C.c_void_p(y.data_ptr()),
+                                 rows, n_out, rows, sp)
+            raise_for(rc, ctx)
+
+    return rec
+
+
+def jc512(ctx, stream):
+    import torch
+
+    H = jaynes_cummings(15, 15, seed=1)
+    h = handle(ctx, H)
+    out = []
+    for tdt, npdt in ((torch.complex128, np.complex128), (torch.complex64, np.complex64)):
+        for ncols in (1, 64):
+            x = _cols(512, ncols, tdt, 1)
+            y = _cols(512, ncols, tdt, 2)
+            reps = 50
+            ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, L.QOB_LEFT, 512, 512, ncols, x, y, dtype_code(npdt),
+                                                         reps=reps))
+            out.append({"dtype": np.dtype(npdt).name, "kets": ncols, "us_per_apply_call": ms * 1e3 / reps,
+                        "applies_per_s": ncols * reps / (ms * 1e-3)})
+    return {"workload": "jc512", "results": out}
+
+
+def sparse4096(ctx, stream):
+    import torch
+
+    out = []
+    for tdt, npdt in ((torch.complex128, np.complex128), (torch.complex64, np.complex64)):
+        S = jaynes_cummings_sparse(31, 63, seed=1, dtype=npdt)
+        h = handle(ctx, S)
+        n = len(S.basis_l)
+        nnz = S.data.nnz
+        s = 16 if npdt == np.complex128 else 8
+        for ncols in (1, 256):
+            if ncols == 1:
+                x = _cols(n, 1, tdt, 3).contiguous()
+                y = _cols(n, 1, tdt, 4).contiguous()
+            else:
+                rho = random_density_columns(n, 256, seed=5, dtype=npdt)
+                x = torch.as_tensor(np.ascontiguousarray(rho.T), device="cuda:0").t()
+                y = _cols(n, 256, tdt, 6)
+            reps = 20
+            ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, L.QOB_LEFT, n, n, ncols, x, y, dtype_code(npdt), reps=reps))
+            t = ms * 1e-3 / reps
+            bytes_ = nnz * (s + 4) + (n + 1) * 4 + 3 * n * ncols * s
+            out.append({"dtype": np.dtype(npdt).name, "columns": ncols, "nnz": int(nnz), "us_per_call": t * 1e6,
+                        "algorithmic_GBps": bytes_ / t / 1e9})
+    return {"workload": "sparse4096", "results": out}
+
+
+def rho_h8(ctx, stream):
+    import torch
+
+    H = heisenberg_chain(8, seed=4)
+    h = handle(ctx, H)
+    out = []
+    for tdt, npdt in ((torch.complex128, np.complex128), (torch.complex64, np.complex64)):
+        x = _cols(256, 256, tdt, 7)
+        y = _cols(256, 256, tdt, 8)
+        for side in (L.QOB_LEFT, L.QOB_RIGHT):
+            reps = 20
+            ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, side, 256, 256, 256, x, y, dtype_code(npdt), reps=reps))
+            out.append({"dtype": np.dtype(npdt).name, "form": "H*rho" if side == L.QOB_LEFT else "rho*H",
+                        "us_per_call": ms * 1e3 / reps})
+    return {"workload": "rho_h8", "results": out}
+
+
+def cavities256(ctx, stream):
+    import torch
+
+    from .evolution import Batch
+
+    rng = Rng(40)
+    models = []
+    for k in range(256):
+        n1, n2 = rng.integers(2, 8, 64)
+        models.append(two_mode_cavity(int(n1), int(n2), seed=1000 + k))
+    dims = [len(m.basis_l) for m in models]
+    out = []
+    for tdt, npdt in ((torch.complex128, np.complex128), (torch.complex64, np.complex64)):
+        b = Batch(npdt)
+        for k, H in enumerate(models):
+            x = _cols(dims[k], 1, tdt, 10 + k).contiguous()
+            y = _cols(dims[k], 1, tdt, 20 + k).contiguous()
+            b.add(H, x, y, 0.7 - 0.2j, 0.3)
+        chosen, times = b.tune()
+        ms = _timed_graph(ctx, stream, lambda sp: raise_for(L.lib().qob_batch_run(ctx.ptr, b.ptr, sp), ctx), reps=50)
+        s = 16 if npdt == np.complex128 else 8
+        bytes_ = 3 * sum(dims) * s
+        out.append({"dtype": np.dtype(npdt).name, "models": 256, "total_dim": int(sum(dims)), "tile": chosen,
+                    "us_per_launch": ms * 1e3, "applies_per_s": 256 / (ms * 1e-3),
+                    "algorithmic_GBps": bytes_ / (ms * 1e-3) / 1e9, "info": b.info()})
+    return {"workload": "cavities256", "results": out}
+
+
+def served(ctx, stream, nreq=192, rate=2000.0, seed=50):
+    from .evolution import Server
+
+    rng = Rng(seed)
+    pool = [heisenberg_chain(n, seed=60 + n) for n in (8, 10, 12, 14, 16)]
+    pool += [jaynes_cummings(15, 15, seed=70), jaynes_cummings(31, 63, seed=71), jaynes_cummings(63, 63, seed=72)]
+    picks = rng.integers(nreq, 0, len(pool) - 1)
+    gaps = -np.log(1.0 - rng.uniform(nreq)) / rate
+    psis = [rng.ket_data(len(pool[p].basis_l)) for p in picks]
+    results = {}
+    for npdt in (np.complex64, np.complex128):
+        S = Server(npdt, mem_budget=16 << 30, max_active=256)
+        for H in pool:  # compile plans before the clock starts
+            S.submit(H, np.zeros(len(H.basis_l)), 1, 1e-3)
+        while S.step():
+            pass
+        S.start()
+        ids = []
+        t0 = time.perf_counter()
+        for k in range(nreq):
+            ids.append(S.submit(pool[picks[k]], psis[k], 100, 1e-3))
+            time.sleep(gaps[k])
+        for i in ids:
+            S.wait(i, 600.0)
+        wall = time.perf_counter() - t0
+        lat, res = [], []
+        for i in ids:
+            st, tm, r = S.poll(i)
+            lat.append(tm[2] - tm[0])
+            res.append(r)
+        stats = S.stats()
+        S.stop()
+        S.close()
+        results[np.dtype(npdt).name] = {"p50_ms": float(np.percentile(lat, 50) * 1e3),
+                                        "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                                        "requests_per_s": nreq / wall, "applies_per_s": nreq * 400 / wall,
+                                        "wall_s": wall, "engine_iterations": stats["iterations"], "res": res}
+    errs = [float(np.linalg.norm(a.astype(np.complex128) - b) / np.linalg.norm(b))
+            for a, b in zip(results["complex64"]["res"], results["complex128"]["res"])]
+    for v in results.values():
+        v.pop("res")
+    return {"workload": "served", "requests": nreq, "poisson_rate_per_s": rate, "steps_per_request": 100,
+            "dt": 1e-3, "results": results, "fp32_rel_err_vs_fp64_max": max(errs),
+            "fp32_rel_err_vs_fp64_median": float(np.median(errs))}
+
+
+def run_suite(device: int = 0):
+    import torch
+
+    ctx = get_context(device)
+    stream = torch.cuda.Stream(device)
+    for fn in (jc512, sparse4096, rho_h8, cavities256, served):
+        t0 = time.perf_counter()
+        line = fn(ctx, stream)
+        line["seconds"] = time.perf_counter() - t0
+        print(json.dumps(line), flush=True)

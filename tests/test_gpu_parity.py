@@ -204,6 +204,23 @@ def test_large_dense_factor_mode_products():
     check(out, op, psi, 1.5, 2.1, TOL64)
 
 
+@pytest.mark.parametrize("ncols", [1, 3, 16, 37])
+def test_host_buffers_through_qob_mul_host(ncols):
+    """numpy (host) data goes through qob_mul_host: copies in, kernels, copy out
+    (pipelined over two streams for 8 or more columns)."""
+    from qobgpu.mul import mul_
+
+    H = heisenberg_chain(9, seed=5)
+    rng = Q.Rng(115)
+    n = len(H.basis_l)
+    X = O.Operator(H.basis_r, Q.GenericBasis(ncols), rng.kets_data(n, ncols))
+    Y = O.Operator(H.basis_l, Q.GenericBasis(ncols), rng.kets_data(n, ncols))
+    ref = OR.mul(Y, H, X, AL, BE)
+    got = O.Operator(Y.basis_l, Y.basis_r, np.array(Y.data, order="F", copy=True))
+    mul_(got, H, X, AL, BE)
+    assert rel_l2(got.data, ref) < TOL64
+
+
 # ---------------------------------------------------------------- errors and state
 def test_dimension_and_alias_errors():
     from qobgpu.mul import mul_, to_device
