@@ -291,10 +291,12 @@ def run_own(args, rank, world, local_rank):
         return ms, launches, (t_host0, t_host1), (xs, ys)
 
     def tune(dt):
-        times = (C.c_double * 4)()
+        times = (C.c_double * 8)()
         chosen = C.c_int()
         raise_for(lib.qob_op_tune(ctx.ptr, hd.ptr, L.QOB_LEFT, dtype_code(dt), BATCH, times, C.byref(chosen)), ctx)
-        return {"kets_per_thread": chosen.value, "ms_by_kets_per_thread": {str(1 << k): times[k] for k in range(4)}}
+        return {"kets_per_thread": chosen.value & 0xFFFF, "threads_per_block": chosen.value >> 16,
+                "ms_by_kets_per_thread_and_block": {f"{1 << (k // 2)}x{(128, 256)[k % 2]}": times[k]
+                                                    for k in range(8)}}
 
     prepare(H, L.QOB_LEFT, np.complex64, dev)
     tuning = {"c128": tune(np.complex128), "c64": tune(np.complex64)}

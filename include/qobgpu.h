@@ -123,13 +123,14 @@ int qob_op_shape(qob_ctx* ctx, const qob_op* op, int64_t* rows, int64_t* cols);
  * info[3] = number of extra (non-fused) passes.  info may be NULL. */
 int qob_op_prepare(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t* info);
 
-/* Autotuner: time the fused kernel with 1, 2, 4 and 8 vectors per thread for
- * applications of op to ncols vectors (side, dtype as in qob_mul) and keep the
- * fastest for later calls with this operator, side and dtype.  times_ms[k] =
- * milliseconds per application with 2^k vectors per thread (-1 when not
- * tried); *chosen = the vectors per thread kept (0: the operator has no fused
- * part).  Either pointer may be NULL.  Allocates and frees two scratch arrays;
- * synchronous. */
+/* Autotuner: time the fused kernel with 1, 2, 4 and 8 vectors per thread and
+ * blocks of 128 or 256 threads for applications of op to ncols vectors (side,
+ * dtype as in qob_mul) and keep the fastest for later calls with this
+ * operator, side and dtype.  times_ms[2k + b] = milliseconds per application
+ * with 2^k vectors per thread and blocks of 128 (b = 0) or 256 (b = 1)
+ * threads, -1 when not tried (8 entries); *chosen = vectors per thread |
+ * (threads per block << 16), 0 when the operator has no fused part.  Either
+ * pointer may be NULL.  Allocates and frees two scratch arrays; synchronous. */
 int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, double* times_ms,
                 int* chosen);
 

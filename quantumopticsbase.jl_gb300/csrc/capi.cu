@@ -450,8 +450,9 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
     check_dtype(dtype);
     Plan& P = get_plan(ctx->c, op, side, dtype);
     const int tiles[4] = {1, 2, 4, 8};
-    double t[4] = {-1.0, -1.0, -1.0, -1.0};
-    int best = 0;
+    const int blocks[2] = {128, 256};
+    double t[8] = {-1.0, -1.0, -1.0, -1.0, -1.0, -1.0, -1.0, -1.0};
+    int best = 0, best_block = 256;
     if (P.gather && P.kind == Plan::Kind::Sum) {
       GatherPlan& g = *P.gather;
       const size_t esz = dtype == QOB_C128 ? 16 : 8;
@@ -467,9 +468,11 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
       QOB_CUDA(cudaEventCreate(&e0));
       QOB_CUDA(cudaEventCreate(&e1));
       double best_t = 1e300;
-      for (int k = 0; k < 4; ++k) {
-        if (tiles[k] > ncols || (k > 0 && side == QOB_RIGHT && ncols > 1)) continue;
-        g.tc = tiles[k];
+      for (int k = 0; k < 8; ++k) {
+        const int tc = tiles[k / 2], blk = blocks[k % 2];
+        if (tc > ncols || (tc > 1 && side == QOB_RIGHT && ncols > 1)) continue;
+        g.tc = tc;
+        g.block = blk;
         for (int i = 0; i < 2; ++i)
           apply_plan(ctx->c, P, {1.0, 0.0}, x.p, xes, xcs, {0.3, 0.0}, y.p, yes, ycs, ncols, 0, 0);
         QOB_CUDA(cudaEventRecord(e0, 0));
@@ -482,16 +485,18 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
         t[k] = ms / 5.0;
         if (t[k] < best_t) {
           best_t = t[k];
-          best = tiles[k];
+          best = tc;
+          best_block = blk;
         }
       }
       g.tc = best;
+      g.block = best_block;
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
     }
     if (times_ms)
-      for (int k = 0; k < 4; ++k) times_ms[k] = t[k];
-    if (chosen) *chosen = best;
+      for (int k = 0; k < 8; ++k) times_ms[k] = t[k];
+    if (chosen) *chosen = best | (best_block << 16);
   });
 }
 

@@ -459,10 +459,11 @@ void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t x
   using CT = typename Cx<R>::T;
   auto kern = k_gather_j<R, REALV, SQUARE, W1, TC, BMODE>;
   allow_smem(kern, smem);
-  const unsigned gx = (unsigned)((v.m + kThreads - 1) / kThreads);
+  const int threads = v.block > 0 ? v.block : kThreads;
+  const unsigned gx = (unsigned)((v.m + threads - 1) / threads);
   for (int64_t c0 = 0; c0 < ncols; c0 += (int64_t)65535 * TC) {  // grid.y limit
     const int64_t nc = std::min<int64_t>(ncols - c0, (int64_t)65535 * TC);
-    kern<<<dim3(gx, (unsigned)((nc + TC - 1) / TC)), kThreads, smem, s>>>(
+    kern<<<dim3(gx, (unsigned)((nc + TC - 1) / TC)), threads, smem, s>>>(
         v, st, (const CT*)x + c0 * xcs, xcs, (CT*)y + c0 * ycs, ycs, (int)nc, a, b);
     QOB_LAUNCHED();
   }

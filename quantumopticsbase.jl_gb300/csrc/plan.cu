@@ -862,6 +862,7 @@ GatherView GatherPlan::view() const {
   v.all_w1 = all_w1 ? 1 : 0;
   v.fast = fast ? 1 : 0;
   v.fastg = (const int4*)fastg.p;
+  v.block = block;
   return v;
 }
 

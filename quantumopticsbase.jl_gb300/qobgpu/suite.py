@@ -219,12 +219,34 @@ def served(ctx, stream, nreq=192, rate=2000.0, seed=50):
             "fp32_rel_err_vs_fp64_median": float(np.median(errs))}
 
 
+def host_link(ctx, stream):
+    """Pinned host <-> device copy bandwidth (explains the end-to-end numbers)."""
+    import torch
+
+    n = 64 * 16384  # one 64-ket ComplexF64 batch: 16 MiB
+    h = torch.empty(n, dtype=torch.complex128).pin_memory()
+    d = torch.empty(n, dtype=torch.complex128, device="cuda:0")
+    out = {}
+    for name, fn in (("h2d", lambda: d.copy_(h, non_blocking=True)), ("d2h", lambda: h.copy_(d, non_blocking=True))):
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                fn()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(20):
+                fn()
+            e1.record(stream)
+        e1.synchronize()
+        out[name + "_GBps"] = 20 * n * 16 / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    return {"workload": "host_link", "bytes_per_copy": n * 16, "results": out}
+
+
 def run_suite(device: int = 0):
     import torch
 
     ctx = get_context(device)
     stream = torch.cuda.Stream(device)
-    for fn in (jc512, sparse4096, rho_h8, cavities256, served):
+    for fn in (jc512, sparse4096, rho_h8, cavities256, served, host_link):
         t0 = time.perf_counter()
         line = fn(ctx, stream)
         line["seconds"] = time.perf_counter() - t0

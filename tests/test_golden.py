@@ -1,0 +1,65 @@
+"""The oracle (CPU) and libqobgpu (GPU) against the committed golden fixtures
+(tests/golden/golden.npz, made by tests/golden/make_golden.py from numpy dense
+materialisation)."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as OR
+from golden.make_golden import CASES, make_inputs
+from helpers import rel_l2
+from qobgpu import operators as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = np.load(os.path.join(HERE, "golden", "golden.npz"))
+NAMES = sorted(CASES)
+
+
+def _operands(name):
+    build, form = CASES[name]
+    H = build()
+    x, y = GOLD[name + "__x"], GOLD[name + "__y"]
+    return H, form, x, y, GOLD[name + "__expected"]
+
+
+def test_fixture_inputs_regenerate_identically():
+    """The seeded generator reproduces the stored inputs (platform independence)."""
+    for i, name in enumerate(NAMES):
+        build, form = CASES[name]
+        x, y = make_inputs(build(), form, 900 + i)
+        assert np.array_equal(x, GOLD[name + "__x"]) and np.array_equal(y, GOLD[name + "__y"]), name
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_matches_golden(name):
+    H, form, x, y, exp = _operands(name)
+    node = OR.build_node(H)
+    side = 0 if form in ("ket", "opL") else 1
+    got = OR.mul_arrays(side, form in ("ket", "bra"), node, GOLD["alpha"], x, GOLD["beta"], y)
+    assert rel_l2(got, exp) < 1e-13
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", NAMES)
+def test_gpu_matches_golden(name):
+    import qobgpu as Q
+    from qobgpu.mul import mul_, to_device
+
+    H, form, x, y, exp = _operands(name)
+    a, b = complex(GOLD["alpha"]), complex(GOLD["beta"])
+    if form == "ket":
+        r = to_device(Q.Ket(H.basis_l, y.copy()))
+        mul_(r, H, to_device(Q.Ket(H.basis_r, x)), a, b)
+    elif form == "bra":
+        r = to_device(Q.Bra(H.basis_r, y.copy()))
+        mul_(r, to_device(Q.Bra(H.basis_l, x)), H, a, b)
+    elif form == "opL":
+        gb = Q.GenericBasis(x.shape[1])
+        r = to_device(O.Operator(H.basis_l, gb, np.asfortranarray(y)))
+        mul_(r, H, to_device(O.Operator(H.basis_r, gb, np.asfortranarray(x))), a, b)
+    else:
+        gb = Q.GenericBasis(x.shape[0])
+        r = to_device(O.Operator(gb, H.basis_r, np.asfortranarray(y)))
+        mul_(r, to_device(O.Operator(gb, H.basis_l, np.asfortranarray(x))), H, a, b)
+    assert rel_l2(r.data.cpu().numpy(), exp) < 1e-12
