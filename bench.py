@@ -337,7 +337,9 @@ def run_own(args, rank, world, local_rank):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src, "traffic": prof.get("dram_bytes_per_launch"),
                      "algorithmic_bytes_per_launch": bytes_per_ket * BATCH,
-                     "kernel": "k_gather_j<double, real, square, TC=8, beta general>",
+                     "kernel": "k_gather_j<double, real values, square, {} kets/thread, real beta> x {} threads".format(
+                         tuning["c128"]["kets_per_thread"], tuning["c128"]["threads_per_block"]),
+                     "ncu_kernel": prof.get("kernel"),
                      "binding": "fp64 FMA throughput (GB300 FP64 ~1.25 TFLOP/s), see fp64_compute"},
         "fp64_compute": fp64,
         "plan": plan,

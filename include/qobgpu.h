@@ -108,7 +108,11 @@ int qob_op_lazyproduct(qob_ctx* ctx, int nops, qob_op* const* ops, double factor
 
 /* Rewrite a LazySum's factors in place, as TimeDependentSum's
  * update_static_coefficients! does (src/time_dependent_operator.jl:279-290).
- * The compiled device form is updated without recompiling its structure. */
+ * The compiled device forms are updated at their next use without recompiling:
+ * while the stored pattern holds the new values, the factors are copied to the
+ * device and the values re-evaluated there in the order of the next call's
+ * stream (no synchronisation); a value that becomes nonzero outside the stored
+ * pattern, or complex in a real-valued form, rebuilds the structure. */
 int qob_op_set_factors(qob_ctx* ctx, qob_op* sum, const double* factors);
 
 int qob_op_free(qob_ctx* ctx, qob_op* op);
@@ -225,6 +229,19 @@ int qob_batch_free(qob_ctx* ctx, qob_batch* batch);
  * ------------------------------------------------------------------------- */
 int qob_rk4(qob_ctx* ctx, qob_op* H, int dtype, void* psi, int64_t n, double dt, int nsteps,
             int renormalise, void* stream);
+
+/* RK4 of dpsi/dt = -i H(t) psi for a TimeDependentSum: H is the LazySum of its
+ * operators and row r of `factors` (nrows = 2*nsteps + 1 rows of nterms
+ * interleaved complex doubles, host memory) holds the coefficients at
+ * t0 + r*dt/2, i.e. what set_time!(H, t) writes through
+ * update_static_coefficients! (src/time_dependent_operator.jl:162-171,279-290)
+ * before each right-hand-side evaluation.  The table is copied to the device
+ * once; before each stage the compiled values are re-evaluated on the device
+ * from its row, so no host round trip happens inside the steps.  Every term
+ * must compile into the fused gather (QOB_ERR_UNSUPPORTED otherwise).
+ * Synchronous on `stream`. */
+int qob_rk4_td(qob_ctx* ctx, qob_op* H, int dtype, void* psi, int64_t n, double dt, int nsteps,
+               const double* factors, int64_t nrows, int renormalise, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Request server with continuous batching (no counterpart in the reference).

@@ -26,6 +26,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <memory>
 #include <mutex>
 #include <thread>
@@ -205,11 +206,15 @@ void ensemble_build(Context& ctx, Ensemble& E, const std::vector<EvolveState>& s
   E.grid = std::max(1, std::min(E.stage_ntiles, ctx.num_sms * 8));
 }
 
-void ensemble_step(Context& ctx, Ensemble& E, cudaStream_t s) {
+// One RK4 step of every state; before_stage(mode), when given, runs before the
+// application of each stage (time-dependent operators refresh their values there).
+void ensemble_step(Context& ctx, Ensemble& E, cudaStream_t s,
+                   const std::function<void(int)>* before_stage = nullptr) {
   if (E.stage_ntiles == 0) return;
   const StageItemDev* it = (const StageItemDev*)E.stage_items.p;
   const int2* tl = (const int2*)E.stage_tiles.p;
   for (int mode = 1; mode <= 4; ++mode) {
+    if (before_stage) (*before_stage)(mode);
     launch_tables(ctx, mode == 1 ? E.g_psi : E.g_tmp, mode == 1 ? E.from_psi : E.from_tmp, s);
     if (E.prec == QOB_C128)
       k_rk4_stage<double2, double><<<E.grid, 256, 0, s>>>(it, tl, E.stage_ntiles, mode);
@@ -568,6 +573,58 @@ int qob_rk4(qob_ctx* ctx, qob_op* H, int dtype, void* psi, int64_t n, double dt,
     qob::ensemble_build(ctx->c, E, {qob::EvolveState{&P, psi, w, w + sz, w + 2 * sz, n, dt}}, dtype);
     for (int s = 0; s < nsteps; ++s) qob::ensemble_step(ctx->c, E, (cudaStream_t)stream);
     QOB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    return QOB_OK;
+  } catch (const qob::Error& e) {
+    ctx->c.err = e.msg;
+    return e.code;
+  }
+}
+
+// RK4 with time-dependent LazySum factors: row r of `factors` holds the factors
+// at t0 + r*dt/2.  Stage 1 of step s uses row 2s, stages 2 and 3 row 2s+1,
+// stage 4 row 2s+2; the values are re-evaluated on the device before each
+// stage whose row differs from the previous one.
+int qob_rk4_td(qob_ctx* ctx, qob_op* H, int dtype, void* psi, int64_t n, double dt, int nsteps,
+               const double* factors, int64_t nrows, int renormalise, void* stream) {
+  if (!ctx) return QOB_ERR_ARG;
+  try {
+    QOB_CUDA(cudaSetDevice(ctx->c.device));
+    if (!H || !psi || n < 1 || nsteps < 0 || (dtype != QOB_C128 && dtype != QOB_C64))
+      qob::fail(QOB_ERR_ARG, "qob_rk4_td: bad arguments");
+    if (H->node->kind != qob::Kind::LazySum) qob::fail(QOB_ERR_ARG, "qob_rk4_td needs a LazySum");
+    if (nrows != 2 * (int64_t)nsteps + 1) qob::fail(QOB_ERR_ARG, "qob_rk4_td: nrows must be 2*nsteps+1");
+    const size_t nf = H->node->factors.size();
+    if (nf > 0 && !factors) qob::fail(QOB_ERR_ARG, "qob_rk4_td: null factor table");
+    if (H->node->m != n || H->node->n != n) qob::fail(QOB_ERR_DIM, "Hamiltonian and state dimensions differ");
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t sz = (size_t)n * (dtype == QOB_C128 ? 16 : 8);
+    char* w = static_cast<char*>(ctx->c.ws.get(20, 3 * sz));
+    qob::Plan& P = qob::batch_plan(ctx->c, H, dtype);
+    if (P.kind != qob::Plan::Kind::Sum || !P.dense.empty() || !P.modek.empty() || !P.subs.empty())
+      qob::fail(QOB_ERR_UNSUPPORTED, "qob_rk4_td: every term must compile into the fused gather");
+    if (nsteps == 0) return QOB_OK;
+    qob::prepare_factor_rows(P, *H->node, factors, nrows);
+    qob::DeviceBuf table;
+    table.upload(factors, std::max<size_t>((size_t)nrows * nf, 1) * 16);
+    const double2* rows = (const double2*)table.p;
+    qob::Ensemble E;
+    E.renormalise = renormalise != 0;
+    qob::ensemble_build(ctx->c, E, {qob::EvolveState{&P, psi, w, w + sz, w + 2 * sz, n, dt}}, dtype);
+    int step = 0;
+    std::function<void(int)> hook = [&](int mode) {
+      if (!P.gather) return;
+      int64_t row = -1;
+      if (mode == 1 && step == 0) row = 0;
+      if (mode == 2) row = 2 * (int64_t)step + 1;
+      if (mode == 4) row = 2 * (int64_t)step + 2;
+      if (row >= 0) qob::device_refresh(*P.gather, rows + row * nf, st);
+    };
+    for (step = 0; step < nsteps; ++step) qob::ensemble_step(ctx->c, E, st, &hook);
+    QOB_CUDA(cudaStreamSynchronize(st));
+    // the values now belong to the last row: the next use re-evaluates them
+    // from the operator's own factors
+    for (auto& d : P.deps)
+      if (d.first == H->node.get()) d.second = ~uint64_t(0);
     return QOB_OK;
   } catch (const qob::Error& e) {
     ctx->c.err = e.msg;

@@ -45,7 +45,84 @@ __global__ void k_build_diag(int64_t m, int ndg, const GGroup* __restrict__ dg,
   }
 }
 
+// Stored values re-evaluated from the root LazySum's factors: one thread per
+// merged slot, value = sum over its contributions of (f[top] * inner) * pv,
+// summed in the order of the host record (the order of the LazySum's terms).
+template <typename R, bool REALV>
+__global__ void __launch_bounds__(256) k_td_values(int nslots, const TdSlot* __restrict__ slots,
+                                                   const TdContrib* __restrict__ contrib,
+                                                   const TdTerm* __restrict__ terms,
+                                                   const double2* __restrict__ f, void* vals, void* ell,
+                                                   double2* __restrict__ dtab) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nslots) return;
+  const TdSlot sl = slots[s];
+  double re = 0.0, im = 0.0;
+  for (int k = 0; k < sl.count; ++k) {
+    const TdContrib& c = contrib[sl.first + k];
+    const TdTerm& t = terms[c.term];
+    double cr = t.inner[0], ci = t.inner[1];
+    if (t.top >= 0) {
+      const double2 a = f[t.top];
+      const double r2 = __dsub_rn(__dmul_rn(a.x, t.inner[0]), __dmul_rn(a.y, t.inner[1]));
+      const double i2 = __dadd_rn(__dmul_rn(a.x, t.inner[1]), __dmul_rn(a.y, t.inner[0]));
+      cr = r2;
+      ci = i2;
+    }
+    re = __dadd_rn(re, __dsub_rn(__dmul_rn(cr, c.pv[0]), __dmul_rn(ci, c.pv[1])));
+    im = __dadd_rn(im, __dadd_rn(__dmul_rn(cr, c.pv[1]), __dmul_rn(ci, c.pv[0])));
+  }
+  if (sl.dst_diag >= 0) dtab[sl.dst_diag] = make_double2(re, im);
+  if (sl.dst_val >= 0) {
+    if constexpr (REALV) {
+      static_cast<R*>(vals)[sl.dst_val] = (R)re;
+    } else {
+      typename gather::Cx<R>::T o;
+      o.x = (R)re;
+      o.y = (R)im;
+      static_cast<typename gather::Cx<R>::T*>(vals)[sl.dst_val] = o;
+    }
+  }
+  if (sl.dst_ell >= 0) {
+    if constexpr (sizeof(R) == 8 && REALV) {
+      static_cast<EllD*>(ell)[sl.dst_ell].v = re;
+    } else if constexpr (sizeof(R) == 8) {
+      EllZ& e = static_cast<EllZ*>(ell)[sl.dst_ell];
+      e.v[0] = re;
+      e.v[1] = im;
+    } else if constexpr (REALV) {
+      static_cast<EllF*>(ell)[sl.dst_ell].v = (float)re;
+    } else {
+      EllC& e = static_cast<EllC*>(ell)[sl.dst_ell];
+      e.v[0] = (float)re;
+      e.v[1] = (float)im;
+    }
+  }
+}
+
 }  // namespace
+
+void launch_td_values(const GatherPlan& g, const double2* factors_dev, cudaStream_t s) {
+  if (g.td_nslots == 0) return;
+  const int threads = 256;
+  const unsigned blocks = (unsigned)((g.td_nslots + threads - 1) / threads);
+  const TdSlot* sl = (const TdSlot*)g.td_slots.p;
+  const TdContrib* co = (const TdContrib*)g.td_contrib.p;
+  const TdTerm* te = (const TdTerm*)g.td_terms.p;
+  double2* dt = (double2*)g.dvals.p;
+  if (g.precision == QOB_C128) {
+    if (g.real_vals)
+      k_td_values<double, true><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, g.vals.p, g.ell.p, dt);
+    else
+      k_td_values<double, false><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, g.vals.p, g.ell.p, dt);
+  } else {
+    if (g.real_vals)
+      k_td_values<float, true><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, g.vals.p, g.ell.p, dt);
+    else
+      k_td_values<float, false><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, g.vals.p, g.ell.p, dt);
+  }
+  QOB_LAUNCHED();
+}
 
 // Vectors per thread: the tuned choice, else the largest of 8 / 4 / 2 / 1 that
 // the number of vectors fills.

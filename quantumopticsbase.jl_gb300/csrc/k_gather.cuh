@@ -94,10 +94,15 @@ struct Ell<float, false> {
   static __device__ __forceinline__ float2 v(const EllC& e) { return make_float2(e.v[0], e.v[1]); }
 };
 
-__device__ __forceinline__ bool nz(double v) { return v != 0.0; }
-__device__ __forceinline__ bool nz(float v) { return v != 0.f; }
-__device__ __forceinline__ bool nz(double2 v) { return v.x != 0.0 || v.y != 0.0; }
-__device__ __forceinline__ bool nz(float2 v) { return v.x != 0.f || v.y != 0.f; }
+// Nonzero tests on the bit patterns (sign bit shifted out, so -0 counts as
+// zero, NaN as nonzero): integer instructions, where a floating-point compare
+// of a double would occupy the FP64 pipe that bounds the ComplexF64 kernels.
+__device__ __forceinline__ bool nz(double v) { return ((unsigned long long)__double_as_longlong(v) << 1) != 0ull; }
+__device__ __forceinline__ bool nz(float v) { return (__float_as_uint(v) << 1) != 0u; }
+__device__ __forceinline__ bool nz(double2 v) {
+  return ((unsigned long long)(__double_as_longlong(v.x) | __double_as_longlong(v.y)) << 1) != 0ull;
+}
+__device__ __forceinline__ bool nz(float2 v) { return ((__float_as_uint(v.x) | __float_as_uint(v.y)) << 1) != 0u; }
 
 // FP64 accumulator: plain fused multiply-adds.
 struct AccD {

@@ -356,6 +356,8 @@ struct GatherHost {
   std::vector<Contribution> contrib;  // sorted by slot
   Shapes S;
   std::vector<uint8_t> live;  // current nonzero pattern of off-diagonal slots
+  // where each slot's value is stored on the device (-1: not stored)
+  std::vector<int32_t> dst_val, dst_ell, dst_diag;
 };
 
 // ---------------------------------------------------------------------------
@@ -377,21 +379,28 @@ static std::vector<c128> eval_slots(const GatherHost& H, const std::vector<TermC
 }
 
 
+// keep: off-diagonal slots stored even where their value is zero (a factor
+// table's union pattern); complex: store complex values even if all are real.
 static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c128>& val,
-                             int precision) {
+                             int precision, const std::vector<uint8_t>* keep = nullptr,
+                             bool complex = false) {
   const bool square = H.S.square;
   // live pattern of off-diagonal slots
   H.live.assign(H.slots.size(), 0);
   for (size_t s = 0; s < H.slots.size(); ++s)
-    if (!H.slots[s].diag && (val[s].re != 0.0 || val[s].im != 0.0)) H.live[s] = 1;
+    if (!H.slots[s].diag && (val[s].re != 0.0 || val[s].im != 0.0 || (keep && (*keep)[s]))) H.live[s] = 1;
+  H.dst_val.assign(H.slots.size(), -1);
+  H.dst_ell.assign(H.slots.size(), -1);
+  H.dst_diag.assign(H.slots.size(), -1);
   // realness
-  bool real = true;
+  bool real = !complex;
   for (size_t s = 0; s < H.slots.size(); ++s)
     if (val[s].im != 0.0) real = false;
   gp.real_vals = real;
+  gp.td_ready = false;  // destinations change with the structure
   // per group: live entries ordered by (r, coloff)
   std::vector<GGroup> descs;
-  std::vector<int32_t> rowptr, coloff;
+  std::vector<int32_t> rowptr, coloff, pos_slot;
   std::vector<c128> vals;
   struct EllHost {
     int32_t col;
@@ -415,6 +424,8 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
       for (int64_t r = 0; r <= g.nrows; ++r) rowptr.push_back(base + cnt[r]);
       for (size_t s = s0; s < s1; ++s)
         if (H.live[s]) {
+          H.dst_val[s] = (int32_t)vals.size();
+          pos_slot.push_back((int32_t)s);
           coloff.push_back((int32_t)H.slots[s].coloff);
           vals.push_back(val[s]);
         }
@@ -426,8 +437,10 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
         d.ell_off = (int32_t)ell.size();
         for (int64_t r = 0; r < g.nrows; ++r) {
           int32_t k = 0;
-          for (int32_t p = cnt[r]; p < cnt[r + 1]; ++p, ++k)
+          for (int32_t p = cnt[r]; p < cnt[r + 1]; ++p, ++k) {
+            H.dst_ell[pos_slot[base + p]] = (int32_t)ell.size();
             ell.push_back({coloff[base + p], vals[base + p]});
+          }
           for (; k < width; ++k) ell.push_back({0, c128{0.0, 0.0}});
         }
       }
@@ -515,7 +528,10 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
         GGroup d = make_desc(g, H.S, (int32_t)dtab.size());  // rowptr_off = table offset
         std::vector<c128> tab(g.nrows, c128{0.0, 0.0});
         for (size_t s = t0; s < t1; ++s)
-          if (H.slots[s].diag) tab[H.slots[s].r] = val[s];
+          if (H.slots[s].diag) {
+            tab[H.slots[s].r] = val[s];
+            H.dst_diag[s] = (int32_t)(dtab.size() + H.slots[s].r);
+          }
         dtab.insert(dtab.end(), tab.begin(), tab.end());
         dd.push_back(d);
       }
@@ -830,16 +846,112 @@ bool plan_is_current(const Plan& plan) {
   return true;
 }
 
-// Only the root LazySum's factors changed: re-evaluate the gather values.
-void refresh_coefficients(Plan& plan, const OpNode& root) {
+// The contribution record on the device (once per structure).
+static void build_td_tables(GatherPlan& gp, const GatherHost& H, size_t nfactors) {
+  if (gp.td_ready && gp.td_nfactors == (int32_t)nfactors) return;
+  std::vector<TdSlot> sl;
+  std::vector<TdContrib> co;
+  for (size_t s = 0; s < H.slots.size(); ++s) {
+    if (H.dst_val[s] < 0 && H.dst_ell[s] < 0 && H.dst_diag[s] < 0) continue;
+    TdSlot d{};
+    d.first = (int32_t)co.size();
+    d.count = (int32_t)H.slots[s].count;
+    d.dst_val = H.dst_val[s];
+    d.dst_ell = H.dst_ell[s];
+    d.dst_diag = H.dst_diag[s];
+    for (int64_t k = 0; k < H.slots[s].count; ++k) {
+      const Contribution& c = H.contrib[H.slots[s].first + k];
+      TdContrib t{};
+      t.term = c.term;
+      t.pv[0] = c.pv.re;
+      t.pv[1] = c.pv.im;
+      co.push_back(t);
+    }
+    sl.push_back(d);
+  }
+  std::vector<TdTerm> te(gp.terms.size());
+  for (size_t t = 0; t < gp.terms.size(); ++t) {
+    te[t] = TdTerm{};
+    te[t].top = gp.terms[t].top;
+    te[t].inner[0] = gp.terms[t].inner.re;
+    te[t].inner[1] = gp.terms[t].inner.im;
+  }
+  upload_vec(gp.td_slots, sl);
+  upload_vec(gp.td_contrib, co);
+  upload_vec(gp.td_terms, te);
+  if (gp.td_factors.bytes < std::max<size_t>(nfactors, 1) * 16) gp.td_factors.alloc(std::max<size_t>(nfactors, 1) * 16);
+  gp.td_nslots = (int32_t)sl.size();
+  gp.td_nfactors = (int32_t)nfactors;
+  gp.td_ready = true;
+}
+
+void device_refresh(GatherPlan& g, const double2* factors_dev, cudaStream_t s) {
+  if (!g.td_ready) fail(QOB_ERR_STATE, "device refresh without its tables");
+  launch_td_values(g, factors_dev, s);
+  if (g.has_diag) launch_build_diag(g, s);
+}
+
+// Whether the current structure holds these values: every nonzero
+// off-diagonal slot is stored and complex values have complex storage.
+static bool structure_holds(const GatherPlan& gp, const GatherHost& H, const std::vector<c128>& val) {
+  for (size_t s = 0; s < H.slots.size(); ++s) {
+    if (gp.real_vals && val[s].im != 0.0) return false;
+    if (!H.slots[s].diag && !H.live[s] && (val[s].re != 0.0 || val[s].im != 0.0)) return false;
+  }
+  return true;
+}
+
+// Only the root LazySum's factors changed: re-evaluate the gather values.  When
+// the stored pattern still holds them, the factors go to the device and the
+// values are re-evaluated there, in stream order (no structure upload, no
+// synchronisation); otherwise the structure is rebuilt.
+void refresh_coefficients(Plan& plan, const OpNode& root, cudaStream_t s) {
   if (plan.gather) {
-    if (!plan.gather->host_rec) fail(QOB_ERR_STATE, "gather plan lost its host record");
-    GatherHost& H = *static_cast<GatherHost*>(plan.gather->host_rec.get());
-    std::vector<c128> val = eval_slots(H, plan.gather->terms, &root);
-    upload_structure(*plan.gather, H, val, plan.precision);
+    GatherPlan& gp = *plan.gather;
+    if (!gp.host_rec) fail(QOB_ERR_STATE, "gather plan lost its host record");
+    GatherHost& H = *static_cast<GatherHost*>(gp.host_rec.get());
+    std::vector<c128> val = eval_slots(H, gp.terms, &root);
+    if (structure_holds(gp, H, val)) {
+      build_td_tables(gp, H, root.factors.size());
+      if (!root.factors.empty())
+        QOB_CUDA(cudaMemcpyAsync(gp.td_factors.p, root.factors.data(), root.factors.size() * sizeof(c128),
+                                 cudaMemcpyHostToDevice, s));
+      device_refresh(gp, (const double2*)gp.td_factors.p, s);
+    } else {
+      upload_structure(gp, H, val, plan.precision);
+    }
   }
   for (auto& d : plan.deps)
     if (d.first == &root) d.second = root.factors_version;
+}
+
+void prepare_factor_rows(Plan& plan, const OpNode& root, const double* rows, int64_t nrows) {
+  if (!plan.gather) return;
+  GatherPlan& gp = *plan.gather;
+  if (!gp.host_rec) fail(QOB_ERR_STATE, "gather plan lost its host record");
+  GatherHost& H = *static_cast<GatherHost*>(gp.host_rec.get());
+  const size_t nf = root.factors.size();
+  // union of the nonzero patterns and realness over all rows
+  OpNode tmp;
+  tmp.factors.resize(nf);
+  std::vector<uint8_t> keep(H.slots.size(), 0);
+  bool complex = false;
+  for (int64_t r = 0; r < nrows; ++r) {
+    for (size_t k = 0; k < nf; ++k) tmp.factors[k] = {rows[2 * (r * nf + k)], rows[2 * (r * nf + k) + 1]};
+    std::vector<c128> v = eval_slots(H, gp.terms, &tmp);
+    for (size_t s = 0; s < v.size(); ++s) {
+      if (v[s].re != 0.0 || v[s].im != 0.0) keep[s] = 1;
+      if (v[s].im != 0.0) complex = true;
+    }
+  }
+  bool holds = !(gp.real_vals && complex);
+  for (size_t s = 0; s < H.slots.size() && holds; ++s)
+    if (!H.slots[s].diag && keep[s] && !H.live[s]) holds = false;
+  if (!holds) {
+    std::vector<c128> val = eval_slots(H, gp.terms, &root);
+    upload_structure(gp, H, val, plan.precision, &keep, complex);
+  }
+  build_td_tables(gp, H, nf);
 }
 
 GatherView GatherPlan::view() const {

@@ -172,6 +172,27 @@ struct TermCoef {
   c128 inner;     // product of inner factors (LazyTensor factor, nested sums)
 };
 
+// Device copy of the contribution record: every stored value re-evaluated on
+// the device from the root LazySum's factors (time-dependent sums), written
+// to its places in vals[], ell[] and the local diagonal tables.
+struct TdSlot {
+  int32_t first, count;  // range in the TdContrib array
+  int32_t dst_val;       // index into vals[] or -1
+  int32_t dst_ell;       // ELL slot or -1
+  int32_t dst_diag;      // index into the local diagonal tables or -1
+  int32_t pad;
+};
+struct TdContrib {
+  int32_t term;
+  int32_t pad[3];
+  double pv[2];
+};
+struct TdTerm {
+  int32_t top;  // factor index or -1
+  int32_t pad[3];
+  double inner[2];
+};
+
 struct DeviceBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -218,6 +239,11 @@ struct GatherPlan {
   std::vector<int64_t> dslot_count;
   int64_t ndslots = 0;
   std::shared_ptr<void> host_rec;  // merged-slot record used by set_factors
+  // device re-evaluation (built on first use; the structure stays as it is)
+  DeviceBuf td_slots, td_contrib, td_terms, td_factors;
+  int32_t td_nslots = 0;
+  int32_t td_nfactors = 0;
+  bool td_ready = false;
   GatherView view() const;
 };
 
@@ -287,14 +313,21 @@ struct Context {
 
 // plan.cu
 std::unique_ptr<Plan> compile_plan(Context& ctx, const NodeP& op, int side, int precision);
-void refresh_coefficients(Plan& plan, const OpNode& root);
+void refresh_coefficients(Plan& plan, const OpNode& root, cudaStream_t s = 0);
 bool plan_is_current(const Plan& plan);
+// Make the gather structure hold every row of a factor table (rows x nfactors,
+// interleaved complex) and build the device re-evaluation tables.
+void prepare_factor_rows(Plan& plan, const OpNode& root, const double* rows, int64_t nrows);
+// Re-evaluate the gather values on the device from factors in device memory
+// (nfactors complex values) and rebuild the merged diagonal, on stream s.
+void device_refresh(GatherPlan& g, const double2* factors_dev, cudaStream_t s);
 
 // kernels (launchers)
 void launch_gather(const GatherPlan& g, int precision, const void* x, int64_t xes, int64_t xcs,
                    void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta,
                    cudaStream_t s);
 void launch_build_diag(const GatherPlan& g, cudaStream_t s);
+void launch_td_values(const GatherPlan& g, const double2* factors_dev, cudaStream_t s);
 int gather_tile(const GatherPlan& g, int64_t ncols);
 void launch_scale(int precision, void* y, int64_t rows, int64_t cols, int64_t ld_row,
                   int64_t ld_col, c128 beta, cudaStream_t s);

@@ -15,6 +15,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib as L
+from . import operators as O
 from .device import Context, dtype_code, get_context, handle, raise_for
 
 
@@ -63,15 +64,37 @@ class Batch:
             pass
 
 
-def rk4(H, psi, dt: float, nsteps: int, renormalise: bool = False):
-    """In-place RK4 on a device Ket (or a contiguous CUDA tensor)."""
+def factor_rows(H: O.TimeDependentSum, t0: float, dt: float, nsteps: int) -> np.ndarray:
+    """The coefficients of ``H`` at t0 + r*dt/2, r = 0 .. 2*nsteps (the times at
+    which an RK4 step evaluates its right-hand side), as (rows, nterms) complex."""
+    times = t0 + 0.5 * dt * np.arange(2 * nsteps + 1)
+    rows = np.empty((len(times), len(H.coefficients)), np.complex128)
+    for k, c in enumerate(H.coefficients):
+        rows[:, k] = [c(t) for t in times] if callable(c) else c
+    return rows
+
+
+def rk4(H, psi, dt: float, nsteps: int, renormalise: bool = False, t0: float = 0.0):
+    """In-place RK4 on a device Ket (or a contiguous CUDA tensor).
+
+    A ``TimeDependentSum`` is evolved with its coefficients evaluated on the host
+    at every stage time (as ``set_time!`` would, src/time_dependent_operator.jl:162-171)
+    and applied on the device inside the steps; afterwards its current time is
+    t0 + nsteps*dt."""
     data = psi.data if hasattr(psi, "data") and not hasattr(psi, "data_ptr") else psi
     ctx = get_context(data.device.index)
-    h = handle(ctx, H)
     import torch
 
     dt_code = L.QOB_C64 if data.dtype == torch.complex64 else L.QOB_C128
     s = C.c_void_p(torch.cuda.current_stream(data.device.index).cuda_stream)
+    if isinstance(H, O.TimeDependentSum):
+        h = handle(ctx, H)
+        rows = np.ascontiguousarray(factor_rows(H, t0, dt, nsteps))
+        raise_for(L.lib().qob_rk4_td(ctx.ptr, h.ptr, dt_code, _ptr(data), data.shape[0], float(dt), int(nsteps),
+                                     rows.ctypes.data_as(C.c_void_p), rows.shape[0], int(renormalise), s), ctx)
+        H.set_time(t0 + nsteps * dt)
+        return psi
+    h = handle(ctx, H)
     raise_for(L.lib().qob_rk4(ctx.ptr, h.ptr, dt_code, _ptr(data), data.shape[0], float(dt), int(nsteps),
                               int(renormalise), s), ctx)
     return psi
