@@ -11,6 +11,8 @@ submission and completion:
                   and SpMM on 256 columns of a density matrix, FP64 and FP32;
 * ``rho_h8``      mul!(rho', rho, H) and mul!(rho', H, rho) with the 8-spin
                   Heisenberg chain on a 256 x 256 operator;
+* ``lindblad``    Lindblad right-hand side S rho, lazy Liouvillian of 8 / 10 / 12-spin
+                  chains with sigma_- decay (and the materialised one at 8 spins);
 * ``cavities256`` 256 two-mode cavity models (dims 81 ... 4225) in one launch;
 * ``served``      Poisson arrivals of 100-step RK4 requests (Heisenberg chains of
                   8 ... 16 spins, Jaynes-Cummings models of dim 512 ... 8192).
@@ -173,6 +175,51 @@ def cavities256(ctx, stream):
     return {"workload": "cavities256", "results": out}
 
 
+def lindblad(ctx, stream):
+    """Lindblad right-hand side S rho on an N x N density operator: the lazy
+    Liouvillian (one fused gather over vec(rho)) for Heisenberg chains of 8, 10
+    and 12 spins with sigma_- decay on every spin, and the materialised sparse
+    Liouvillian (the reference's form) at 8 spins."""
+    import torch
+
+    from . import operators as O
+    from . import superoperators as SO
+    from .bases import SpinBasis
+
+    out = []
+    for nspins in (8, 10, 12):
+        H = heisenberg_chain(nspins, seed=80 + nspins)
+        b = H.basis_l
+        J = [O.LazyTensor(b, b, (i,), (O.sigmam(SpinBasis("1/2")),)) for i in range(1, nspins + 1)]
+        rates = Rng(90 + nspins).uniform(nspins, 0.1, 1.0)
+        forms = [("lazy", SO.lazy_liouvillian(H, J, rates=rates))]
+        if nspins == 8:
+            forms.append(("materialised", SO.liouvillian(O.sparse(H), [O.sparse(j) for j in J], rates=rates)))
+        n2 = len(b) ** 2
+        for form, L_ in forms:
+            h = handle(ctx, L_.vectorised)
+            for tdt, npdt in ((torch.complex128, np.complex128), (torch.complex64, np.complex64)):
+                x = _cols(n2, 1, tdt, 30).contiguous()
+                y = _cols(n2, 1, tdt, 31).contiguous()
+                reps = 20
+                ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, L.QOB_LEFT, n2, n2, 1, x, y, dtype_code(npdt),
+                                                             alpha=1.0 + 0j, beta=0.0, reps=reps))
+                t = ms * 1e-3 / reps
+                s = 16 if npdt == np.complex128 else 8
+                row = {"spins": nspins, "rho_dim": len(b), "form": form, "dtype": np.dtype(npdt).name,
+                       "us_per_apply": t * 1e6, "algorithmic_GBps": 2 * n2 * s / t / 1e9}
+                if form == "materialised":
+                    row["nnz"] = int(L_.data.nnz)
+                else:
+                    info = (C.c_int64 * 4)()
+                    raise_for(L.lib().qob_op_prepare(ctx.ptr, h.ptr, L.QOB_LEFT, dtype_code(npdt), info), ctx)
+                    row["terms"] = len(L_.operator.operators)
+                    row["groups"] = int(info[0])
+                out.append(row)
+            del h
+    return {"workload": "lindblad", "results": out}
+
+
 def served(ctx, stream, nreq=192, rate=2000.0, seed=50):
     from .evolution import Server
 
@@ -246,7 +293,7 @@ def run_suite(device: int = 0):
 
     ctx = get_context(device)
     stream = torch.cuda.Stream(device)
-    for fn in (jc512, sparse4096, rho_h8, cavities256, served, host_link):
+    for fn in (jc512, sparse4096, rho_h8, lindblad, cavities256, served, host_link):
         t0 = time.perf_counter()
         line = fn(ctx, stream)
         line["seconds"] = time.perf_counter() - t0
