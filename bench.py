@@ -291,12 +291,13 @@ def run_own(args, rank, world, local_rank):
         return ms, launches, (t_host0, t_host1), (xs, ys)
 
     def tune(dt):
-        times = (C.c_double * 8)()
+        times = (C.c_double * 12)()
         chosen = C.c_int()
         raise_for(lib.qob_op_tune(ctx.ptr, hd.ptr, L.QOB_LEFT, dtype_code(dt), BATCH, times, C.byref(chosen)), ctx)
-        return {"kets_per_thread": chosen.value & 0xFFFF, "threads_per_block": chosen.value >> 16,
-                "ms_by_kets_per_thread_and_block": {f"{1 << (k // 2)}x{(128, 256)[k % 2]}": times[k]
-                                                    for k in range(8)}}
+        return {"kets_per_thread": chosen.value & 0xFFFF, "threads_per_block": (chosen.value >> 16) & 0x3FFF,
+                "persistent": bool(chosen.value >> 30),
+                "ms_by_kets_per_thread_and_block": {f"{1 << (k // 3)}x{('128', '256', 'P256')[k % 3]}": times[k]
+                                                    for k in range(12)}}
 
     prepare(H, L.QOB_LEFT, np.complex64, dev)
     tuning = {"c128": tune(np.complex128), "c64": tune(np.complex64)}
@@ -337,7 +338,8 @@ def run_own(args, rank, world, local_rank):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src, "traffic": prof.get("dram_bytes_per_launch"),
                      "algorithmic_bytes_per_launch": bytes_per_ket * BATCH,
-                     "kernel": "k_gather_j<double, real values, square, {} kets/thread, real beta> x {} threads".format(
+                     "kernel": "{}<double, real values, square, {} kets/thread, real beta> x {} threads".format(
+                         "k_gather_p" if tuning["c128"]["persistent"] else "k_gather_j",
                          tuning["c128"]["kets_per_thread"], tuning["c128"]["threads_per_block"]),
                      "ncu_kernel": prof.get("kernel"),
                      "binding": "fp64 FMA throughput (GB300 FP64 ~1.25 TFLOP/s), see fp64_compute"},

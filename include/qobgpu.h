@@ -128,15 +128,22 @@ int qob_op_shape(qob_ctx* ctx, const qob_op* op, int64_t* rows, int64_t* cols);
 int qob_op_prepare(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t* info);
 
 /* Autotuner: time the fused kernel with 1, 2, 4 and 8 vectors per thread and
- * blocks of 128 or 256 threads for applications of op to ncols vectors (side,
- * dtype as in qob_mul) and keep the fastest for later calls with this
- * operator, side and dtype.  times_ms[2k + b] = milliseconds per application
- * with 2^k vectors per thread and blocks of 128 (b = 0) or 256 (b = 1)
- * threads, -1 when not tried (8 entries); *chosen = vectors per thread |
- * (threads per block << 16), 0 when the operator has no fused part.  Either
+ * three launch shapes -- blocks of 128 or 256 threads over the output indices,
+ * or a persistent grid of (SMs x resident blocks) 256-thread blocks that split
+ * the work evenly -- for applications of op to ncols vectors (side, dtype as
+ * in qob_mul) and keep the fastest for later calls with this operator, side
+ * and dtype.  times_ms[3k + b] = milliseconds per application with 2^k vectors
+ * per thread and shape b (0: 128, 1: 256, 2: persistent), -1 when not tried
+ * (12 entries); *chosen = vectors per thread | (threads per block << 16) |
+ * (1 << 30 when persistent), 0 when the operator has no fused part.  Either
  * pointer may be NULL.  Allocates and frees two scratch arrays; synchronous. */
 int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, double* times_ms,
                 int* chosen);
+
+/* Fix the launch shape instead of tuning: vectors_per_thread 1, 2, 4 or 8;
+ * block 128 or 256 threads, or -256 for the persistent grid (as chosen by
+ * qob_op_tune).  Kept until the next tune or recompilation. */
+int qob_op_set_launch(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_per_thread, int block);
 
 /* ---------------------------------------------------------------------------
  * Application: the 5-argument mul!.

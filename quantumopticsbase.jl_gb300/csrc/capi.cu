@@ -450,8 +450,9 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
     check_dtype(dtype);
     Plan& P = get_plan(ctx->c, op, side, dtype);
     const int tiles[4] = {1, 2, 4, 8};
-    const int blocks[2] = {128, 256};
-    double t[8] = {-1.0, -1.0, -1.0, -1.0, -1.0, -1.0, -1.0, -1.0};
+    const int blocks[3] = {128, 256, -256};  // -256: persistent grid of 256-thread blocks
+    double t[12];
+    for (double& v : t) v = -1.0;
     int best = 0, best_block = 256;
     if (P.gather && P.kind == Plan::Kind::Sum) {
       GatherPlan& g = *P.gather;
@@ -468,8 +469,8 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
       QOB_CUDA(cudaEventCreate(&e0));
       QOB_CUDA(cudaEventCreate(&e1));
       double best_t = 1e300;
-      for (int k = 0; k < 8; ++k) {
-        const int tc = tiles[k / 2], blk = blocks[k % 2];
+      for (int k = 0; k < 12; ++k) {
+        const int tc = tiles[k / 3], blk = blocks[k % 3];
         if (tc > ncols || (tc > 1 && side == QOB_RIGHT && ncols > 1)) continue;
         g.tc = tc;
         g.block = blk;
@@ -495,8 +496,23 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
       cudaEventDestroy(e1);
     }
     if (times_ms)
-      for (int k = 0; k < 8; ++k) times_ms[k] = t[k];
-    if (chosen) *chosen = best | (best_block << 16);
+      for (int k = 0; k < 12; ++k) times_ms[k] = t[k];
+    if (chosen) *chosen = best | ((best_block < 0 ? -best_block : best_block) << 16) | (best_block < 0 ? (1 << 30) : 0);
+  });
+}
+
+int qob_op_set_launch(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_per_thread, int block) {
+  return guard(ctx, [&] {
+    if (!ctx || !op || (side != QOB_LEFT && side != QOB_RIGHT)) fail(QOB_ERR_ARG, "qob_op_set_launch: bad arguments");
+    check_dtype(dtype);
+    if (vectors_per_thread != 1 && vectors_per_thread != 2 && vectors_per_thread != 4 && vectors_per_thread != 8)
+      fail(QOB_ERR_ARG, "vectors per thread must be 1, 2, 4 or 8");
+    if (block != 128 && block != 256 && block != -256) fail(QOB_ERR_ARG, "block must be 128, 256 or -256");
+    Plan& P = get_plan(ctx->c, op, side, dtype);
+    if (P.gather) {
+      P.gather->tc = vectors_per_thread;
+      P.gather->block = block;
+    }
   });
 }
 

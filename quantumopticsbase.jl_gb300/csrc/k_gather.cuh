@@ -420,6 +420,45 @@ __global__ void __launch_bounds__(256) k_gather_j(GatherView g, SiteTable st,
     if (t < nt) combine<BMODE>(yb + t * ycs, acc[t].total(), alpha, beta);
 }
 
+// The same work as k_gather_j on a grid of exactly (SMs x resident blocks per
+// SM): every block is resident at once, so every SM holds the same number of
+// blocks, and block b takes the b-th equal share of the warp-sized chunks (32
+// consecutive output indices x TC vectors).  With k_gather_j's grid of one
+// wave or less the hardware may place up to the occupancy limit on some SMs
+// and fewer on others; here the work per SM differs by at most one chunk per
+// block.
+template <typename R, bool REALV, bool SQUARE, bool W1, int TC, int BMODE>
+__global__ void __launch_bounds__(256) k_gather_p(GatherView g, SiteTable st,
+                                                  const typename Cx<R>::T* __restrict__ x, int64_t xcs,
+                                                  typename Cx<R>::T* __restrict__ y, int64_t ycs, int ncols,
+                                                  typename Cx<R>::T alpha, typename Cx<R>::T beta) {
+  using CT = typename Cx<R>::T;
+  using AT = typename AccOf<R>::T;
+  using ET = typename Ell<R, REALV>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const ET* ell = stage<ET>(smem_raw, g);
+  const GGroup* sg = reinterpret_cast<const GGroup*>(smem_raw);
+  const int64_t nj = (g.m + 31) / 32;
+  const int64_t nchunks = nj * (int64_t)((ncols + TC - 1) / TC);
+  const int64_t lo = (int64_t)blockIdx.x * nchunks / gridDim.x;
+  const int64_t hi = ((int64_t)blockIdx.x + 1) * nchunks / gridDim.x;
+  const int lane = threadIdx.x & 31;
+  for (int64_t c = lo + (threadIdx.x >> 5); c < hi; c += blockDim.x >> 5) {
+    const int64_t tile = c / nj;
+    const int64_t J = (c - tile * nj) * 32 + lane;
+    if (J >= g.m) continue;
+    const int c0 = (int)tile * TC;
+    const int nt = min(TC, ncols - c0);
+    const CT* xb = x + (int64_t)c0 * xcs;
+    AT acc[TC];
+    accumulate<R, REALV, SQUARE, W1, TC>(g, st, sg, ell, (uint32_t)J, xb, 1, xcs, nt, acc);
+    CT* yb = y + J + (int64_t)c0 * ycs;
+#pragma unroll
+    for (int t = 0; t < TC; ++t)
+      if (t < nt) combine<BMODE>(yb + t * ycs, acc[t].total(), alpha, beta);
+  }
+}
+
 // Vectors with a stride between their elements (the rows of an operator
 // multiplied from the right, a strided bra): the vectors run across threads,
 // all threads of a block share one output index J.
@@ -462,6 +501,21 @@ template <typename R, bool REALV, bool SQUARE, bool W1, int TC, int BMODE>
 void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t xcs, void* y, int64_t ycs,
               int64_t ncols, typename Cx<R>::T a, typename Cx<R>::T b, size_t smem, cudaStream_t s) {
   using CT = typename Cx<R>::T;
+  if (v.block < 0 && ncols <= (int64_t)INT32_MAX) {
+    // persistent grid: SMs x resident blocks of -v.block threads
+    auto pk = k_gather_p<R, REALV, SQUARE, W1, TC, BMODE>;
+    allow_smem(pk, smem);
+    const int threads = -v.block;
+    int dev = 0, sms = 0, occ = 0;
+    QOB_CUDA(cudaGetDevice(&dev));
+    QOB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    QOB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk, threads, smem));
+    if (occ > 0) {
+      pk<<<(unsigned)(sms * occ), threads, smem, s>>>(v, st, (const CT*)x, xcs, (CT*)y, ycs, (int)ncols, a, b);
+      QOB_LAUNCHED();
+      return;
+    }
+  }
   auto kern = k_gather_j<R, REALV, SQUARE, W1, TC, BMODE>;
   allow_smem(kern, smem);
   const int threads = v.block > 0 ? v.block : kThreads;

@@ -156,7 +156,7 @@ struct GatherView {
   int32_t all_w1;    // 1: every group has exactly one slot per row
   int32_t fast;      // 1: fastg holds {log2 div, mod - 1, first slot, 0} per group
   const int4* fastg; // compact form: one run of power-of-two subsystems, width 1
-  int32_t block;     // threads per block of the index-lanes kernel (0: 256)
+  int32_t block;     // threads per block of the index-lanes kernel (0: 256; < 0: persistent grid of -block)
 };
 
 // A host-side record of how each stored entry is made from the terms, so a
@@ -229,7 +229,7 @@ struct GatherPlan {
   bool fast = false;
   DeviceBuf fastg;
   int tc = 0;     // vectors per thread chosen by qob_op_tune (0: automatic)
-  int block = 0;  // threads per block chosen by qob_op_tune (0: 256)
+  int block = 0;  // threads per block chosen by qob_op_tune (0: 256; < 0: persistent grid of -block)
   DeviceBuf dgroups, dvals;  // diagonal sources: groups + local diagonal tables
   int ndgroups = 0;
   SiteTable sites{};

@@ -69,6 +69,28 @@ def test_heisenberg_14_spins_batch():
     check(out, H, psi, AL, BE, TOL64)
 
 
+@pytest.mark.parametrize("block", [128, 256, -256])
+@pytest.mark.parametrize("tc", [1, 2, 4, 8])
+def test_every_launch_shape(tc, block):
+    """Each vectors-per-thread tile and launch shape (-256: the persistent grid of
+    SMs x resident blocks) on the 10-spin chain (a compact-form plan) and the
+    Jaynes-Cummings model (generic groups), 37 kets (ragged last tile)."""
+    from qobgpu import _lib as L
+    from qobgpu.device import dtype_code, get_context, handle, raise_for
+
+    ctx = get_context(0)
+    for H, seed in ((heisenberg_chain(10, seed=6), 120), (jaynes_cummings(7, 7, seed=2), 121)):
+        rng = Q.Rng(seed)
+        nb = 37
+        X = O.Operator(H.basis_r, Q.GenericBasis(nb), rng.kets_data(len(H.basis_r), nb))
+        Y = O.Operator(H.basis_l, Q.GenericBasis(nb), rng.kets_data(len(H.basis_l), nb))
+        for dtype, tol in ((np.complex128, TOL64), (np.complex64, TOL32)):
+            h = handle(ctx, H)
+            raise_for(L.lib().qob_op_set_launch(ctx.ptr, h.ptr, L.QOB_LEFT, dtype_code(dtype), tc, block), ctx)
+            check(Y, H, X, AL, BE, tol, dtype)
+            check(Y, H, X, AL, 0.0, tol, dtype)
+
+
 def test_heisenberg_operator_both_sides_8_spins():
     H = heisenberg_chain(8, seed=4)
     rng = Q.Rng(102)
