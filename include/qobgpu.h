@@ -102,6 +102,22 @@ int qob_op_lazytensor(qob_ctx* ctx, int nsub, const int64_t* shape_l, const int6
 int qob_op_lazysum(qob_ctx* ctx, int64_t m, int64_t n, int nterms, const double* factors,
                    qob_op* const* ops, qob_op** out);
 
+/* FFTOperator (src/particle.jl:196-535): the transform between position and
+ * momentum grids on a composite shape of nsub subsystems (lengths shape[]).
+ * The naxes subsystems axes[] (1-based, increasing) are transformed; axis a
+ * has the sign sign[a] of the transform a ket sees (-1: FFTW's fft!,
+ * e^{-2 pi i jk/N}; +1: bfft!) and per-axis phase vectors before[a] and
+ * after[a] (shape[axes[a]-1] complex values each, concatenated in axis order;
+ * the reference's mul_before / mul_after are their Kronecker products, with
+ * ones on untransformed subsystems, and after includes 1/sqrt(N)).  qob_mul
+ * applies it to kets and operator columns (LEFT: after .* DFT(before .* x)) and
+ * to bras and operator rows (RIGHT: the same transform of the row with the two
+ * phase vectors swapped, as the reference's conj / opposite-sign / conj
+ * sequence gives); it may be a term of a LazySum or a factor of a LazyProduct.
+ * Power-of-two axes use a radix-2 FFT, other lengths a direct DFT. */
+int qob_op_fft(qob_ctx* ctx, int nsub, const int64_t* shape, int naxes, const int64_t* axes, const int* sign,
+               const double* before, const double* after, qob_op** out);
+
 /* LazyProduct(operators, factor) (src/operators_lazyproduct.jl:33-52). */
 int qob_op_lazyproduct(qob_ctx* ctx, int nops, qob_op* const* ops, double factor_re,
                        double factor_im, qob_op** out);
@@ -226,6 +242,22 @@ int qob_batch_tune(qob_ctx* ctx, qob_batch* batch, double* times_ms, int* chosen
  * [4] blocks of the persistent grid. */
 int qob_batch_info(qob_ctx* ctx, qob_batch* batch, int64_t* info);
 int qob_batch_free(qob_ctx* ctx, qob_batch* batch);
+
+/* ---------------------------------------------------------------------------
+ * Expectation values on product states (LazyKet, src/states_lazyket.jl:64-125).
+ * op: a LazyTensor, a LazySum (nested sums allowed) of LazyTensors and
+ * LazyProducts of LazyTensors, on the square composite basis whose nsites
+ * subsystems have the lengths site_dims.  kets: nstates product states on the
+ * device in dtype, one after another, each the concatenation of its site kets
+ * (state s, site i at element s * sum(site_dims) + sum_{j<i} site_dims[j]).
+ * result: nstates complex doubles on the device,
+ *   result[s] = expect(op, LazyKet(basis, (psi_s1, ..., psi_sn))):
+ *   for a LazyTensor  factor * prod_{i in indices} <psi_i|A_i|psi_i> * prod_{i not in indices} <psi_i|psi_i>,
+ *   for a LazyProduct factor * (factors of its LazyTensors) * prod_i <psi_i|F_1i ... F_ni|psi_i>,
+ *   for a LazySum     sum_k f_k * (its terms).
+ * Computed in FP64 for both dtypes.  Synchronous on `stream`. */
+int qob_expect_lazyket(qob_ctx* ctx, qob_op* op, int dtype, int nsites, const int64_t* site_dims,
+                       const void* kets, int64_t nstates, double* result, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Time evolution.  qob_rk4 advances a device state by nsteps fixed RK4 steps

@@ -54,6 +54,10 @@ def lib():
         L.oref_mul_kets_threaded.argtypes = [VP, C.c_double, C.c_double, D, C.c_double, C.c_double, D,
                                              C.c_int64, C.c_int]
         L.oref_mul_kets_threaded.restype = C.c_int
+        L.oref_fft.argtypes = [C.c_int, I64, C.c_int, I64, C.c_int, D, D]
+        L.oref_fft.restype = VP
+        L.oref_expect_lazyket.argtypes = [VP, C.c_int, I64, D, D]
+        L.oref_expect_lazyket.restype = C.c_int
         L.oref_last_error.restype = C.c_char_p
         _lib = L
     return _lib
@@ -128,6 +132,14 @@ def build_node(op) -> Node:
         arr = (VP * len(kids))(*[k.ptr for k in kids])
         p = L.oref_lazyproduct(len(kids), arr, op.factor.real, op.factor.imag)
         return Node(p, kids)
+    from qobgpu.particle import FFTOperator
+
+    if isinstance(op, FFTOperator):
+        shape = np.asarray(op.basis_l.shape, np.int64)
+        axes = np.asarray(op.axes, np.int64)
+        mb = _c128(op.mul_before)
+        ma = _c128(op.mul_after)
+        return Node(L.oref_fft(len(shape), _ip(shape), len(axes), _ip(axes), op.sign, _dp(mb), _dp(ma)))
     raise TypeError(f"oracle: unsupported operator {type(op)}")
 
 
@@ -191,3 +203,18 @@ def mul_kets_threaded(node: Node, alpha, X: np.ndarray, beta, Y: np.ndarray, nth
     if rc:
         raise OracleError(rc, L.oref_last_error().decode())
     return rc
+
+
+def expect_lazyket(op, kets) -> complex:
+    """Oracle ``expect(op, LazyKet(basis, kets))`` (src/states_lazyket.jl:64-125);
+    kets: the site kets (qobgpu Ket objects or arrays) in subsystem order."""
+    L = lib()
+    node = build_node(op)
+    arrs = [np.asarray(k.to_host() if hasattr(k, "to_host") else k, np.complex128) for k in kets]
+    dims = np.asarray([a.shape[0] for a in arrs], np.int64)
+    flat = np.ascontiguousarray(np.concatenate(arrs)).view(np.float64)
+    out = np.zeros(2)
+    rc = L.oref_expect_lazyket(node.ptr, len(arrs), _ip(dims), _dp(flat), _dp(out))
+    if rc:
+        raise OracleError(rc, L.oref_last_error().decode())
+    return complex(out[0], out[1])

@@ -18,6 +18,7 @@
 #include "qob_oracle.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -36,7 +37,7 @@ inline bool isone(cd a) { return a.re == 1.0 && a.im == 0.0; }
 const cd kOne{1.0, 0.0};
 const cd kZero{0.0, 0.0};
 
-enum Kind { K_SPARSE, K_DENSE, K_EYE, K_LT, K_LS, K_LP };
+enum Kind { K_SPARSE, K_DENSE, K_EYE, K_LT, K_LS, K_LP, K_FFT };
 
 thread_local std::string g_err;
 
@@ -66,6 +67,11 @@ struct oref_node {
   std::vector<oref_node*> ops;
   cd factor{1.0, 0.0};
   std::vector<cd> factors;
+  // FFTOperator: transformed subsystems (0-based), the sign of the transform a
+  // ket sees (fft_r!), and the full phase arrays mul_before / mul_after
+  std::vector<int> fft_axes;
+  int fft_sign = -1;
+  std::vector<cd> mul_before, mul_after;
 };
 
 namespace {
@@ -604,6 +610,116 @@ void eye_right(const Node* f, cd alpha, const cd* x, int64_t nr, cd beta, cd* y)
     }
 }
 
+// ---------------------------------------------------------------------------
+// FFTOperator (src/particle.jl:438-535).  FFTW's fft!/bfft! over a set of
+// dimensions compute the unnormalised multi-dimensional DFT
+// X_k = sum_j x_j exp(sign 2 pi i j.k / N) (sign -1: fft, +1: bfft); restated
+// here as direct sums, one dimension after the other (the DFT is separable).
+// ---------------------------------------------------------------------------
+
+// In-place DFT along dimension `dim` of an array of shape `shape` (column-major).
+void dft_dim(cd* a, const std::vector<int64_t>& shape, size_t dim, int sign) {
+  const int64_t n = shape[dim];
+  int64_t inner = 1, outer = 1;
+  for (size_t q = 0; q < dim; ++q) inner *= shape[q];
+  for (size_t q = dim + 1; q < shape.size(); ++q) outer *= shape[q];
+  std::vector<cd> w(n), line(n);
+  for (int64_t m = 0; m < n; ++m) {
+    const double th = 6.283185307179586476925286766559 * (double)m / (double)n;
+    w[m] = {std::cos(th), sign * std::sin(th)};
+  }
+  for (int64_t o = 0; o < outer; ++o)
+    for (int64_t i = 0; i < inner; ++i) {
+      cd* base = a + i + o * inner * n;
+      for (int64_t j = 0; j < n; ++j) line[j] = base[j * inner];
+      for (int64_t k = 0; k < n; ++k) {
+        cd acc = kZero;
+        int64_t idx = 0;
+        for (int64_t j = 0; j < n; ++j) {
+          acc = cadd(acc, cmul(line[j], w[idx]));
+          idx += k;
+          if (idx >= n) idx -= n;
+        }
+        base[k * inner] = acc;
+      }
+    }
+}
+
+// fft over the transformed dimensions of an array whose leading (or trailing)
+// dimensions are the operator's composite shape.
+void fft_dims(const Node* f, cd* a, const std::vector<int64_t>& shape, size_t offset, int sign) {
+  for (int ax : f->fft_axes) dft_dim(a, shape, offset + ax, sign);
+}
+
+// Ket (vec) and Operator (columns) from the left: :438-457, :504-535
+void fft_left(bool vec, const Node* f, cd alpha, const cd* x, int64_t xc, cd beta, cd* y) {
+  const int64_t N = f->m;
+  const std::vector<int64_t>& sh = f->shape_l;
+  if (vec) {
+    if (iszero(beta)) {
+      for (int64_t i = 0; i < N; ++i) y[i] = cmul(f->mul_before[i], x[i]);
+      fft_dims(f, y, sh, 0, f->fft_sign);
+      for (int64_t i = 0; i < N; ++i) y[i] = cmul(y[i], cmul(f->mul_after[i], alpha));
+    } else {
+      std::vector<cd> p(x, x + N);
+      for (int64_t i = 0; i < N; ++i) p[i] = cmul(p[i], f->mul_before[i]);
+      fft_dims(f, p.data(), sh, 0, f->fft_sign);
+      for (int64_t i = 0; i < N; ++i) y[i] = cadd(cmul(beta, y[i]), cmul(cmul(alpha, p[i]), f->mul_after[i]));
+    }
+    return;
+  }
+  std::vector<cd> d(x, x + N * xc);
+  for (int64_t j = 0; j < xc; ++j)
+    for (int64_t i = 0; i < N; ++i) d[i + j * N] = cmul(d[i + j * N], f->mul_before[i]);
+  std::vector<int64_t> sh2 = sh;
+  sh2.push_back(xc);
+  fft_dims(f, d.data(), sh2, 0, f->fft_sign);
+  for (int64_t j = 0; j < xc; ++j)
+    for (int64_t i = 0; i < N; ++i) d[i + j * N] = cmul(d[i + j * N], f->mul_after[i]);
+  if (!isone(alpha))
+    for (cd& v : d) v = cmul(alpha, v);
+  if (iszero(beta)) {
+    std::copy(d.begin(), d.end(), y);
+  } else {
+    for (int64_t k = 0; k < N * xc; ++k) y[k] = cadd(cmul(y[k], beta), d[k]);
+  }
+}
+
+// Bra (vec) and Operator (rows) from the right: :459-478, :481-502
+void fft_right(bool vec, const Node* f, cd alpha, const cd* x, int64_t xr, cd beta, cd* y) {
+  const int64_t N = f->m;
+  const std::vector<int64_t>& sh = f->shape_l;
+  if (vec) {
+    if (iszero(beta)) {
+      for (int64_t i = 0; i < N; ++i) y[i] = cmul(cconj(f->mul_after[i]), cconj(x[i]));
+      fft_dims(f, y, sh, 0, -f->fft_sign);
+      for (int64_t i = 0; i < N; ++i) y[i] = cmul(cmul(cconj(y[i]), f->mul_before[i]), alpha);
+    } else {
+      std::vector<cd> p(N);
+      for (int64_t i = 0; i < N; ++i) p[i] = cmul(cconj(x[i]), cconj(f->mul_after[i]));
+      fft_dims(f, p.data(), sh, 0, -f->fft_sign);
+      for (int64_t i = 0; i < N; ++i)
+        y[i] = cadd(cmul(beta, y[i]), cmul(cmul(alpha, cconj(p[i])), f->mul_before[i]));
+    }
+    return;
+  }
+  std::vector<cd> d(x, x + xr * N);
+  for (int64_t j = 0; j < N; ++j)
+    for (int64_t i = 0; i < xr; ++i) d[i + j * xr] = cconj(cmul(d[i + j * xr], f->mul_after[j]));
+  std::vector<int64_t> sh2{xr};
+  sh2.insert(sh2.end(), sh.begin(), sh.end());
+  fft_dims(f, d.data(), sh2, 1, -f->fft_sign);
+  for (int64_t j = 0; j < N; ++j)
+    for (int64_t i = 0; i < xr; ++i) d[i + j * xr] = cmul(cconj(d[i + j * xr]), f->mul_before[j]);
+  if (!isone(alpha))
+    for (cd& v : d) v = cmul(alpha, v);
+  if (iszero(beta)) {
+    std::copy(d.begin(), d.end(), y);
+  } else {
+    for (int64_t k = 0; k < xr * N; ++k) y[k] = cadd(cmul(y[k], beta), d[k]);
+  }
+}
+
 void mul_left(bool vec, const Node* op, cd alpha, const cd* x, int64_t xr, int64_t xc, cd beta,
               cd* y, int64_t yr, int64_t yc) {
   // _check_mul!_dim_compatibility (src/operators_lazytensor.jl:695-703)
@@ -622,6 +738,9 @@ void mul_left(bool vec, const Node* op, cd alpha, const cd* x, int64_t xr, int64
     }
     case K_LT:
       lazytensor_left(op, alpha, x, xc, beta, y);
+      return;
+    case K_FFT:
+      fft_left(vec, op, alpha, x, xc, beta, y);
       return;
     case K_LP: {  // src/operators_lazyproduct.jl:103-115, 131-146
       if (iszero(alpha)) {
@@ -683,6 +802,9 @@ void mul_right(bool vec, const Node* op, cd alpha, const cd* x, int64_t xr, int6
     case K_LT:
       lazytensor_right(op, alpha, x, xr, beta, y);
       return;
+    case K_FFT:
+      fft_right(vec, op, alpha, x, xr, beta, y);
+      return;
     case K_LP: {  // src/operators_lazyproduct.jl:117-129, 148-163
       if (iszero(alpha)) {
         zero_op_mul(y, yr * yc, beta);
@@ -738,6 +860,89 @@ void mul_right(bool vec, const Node* op, cd alpha, const cd* x, int64_t xr, int6
       eye_right(op, alpha, x, xr, beta, y);
       return;
   }
+}
+
+// ---------------------------------------------------------------------------
+// product states (src/states_lazyket.jl)
+// ---------------------------------------------------------------------------
+
+// LinearAlgebra's dot(x, A, y) for a data operator (src/operators_dense.jl:219-221):
+// column by column, s += (sum_i conj(x_i) A_ij) * y_j.
+cd dot3(const cd* x, const Node* A, const cd* y, int64_t d) {
+  cd s = kZero;
+  for (int64_t j = 0; j < d; ++j) {
+    if (iszero(y[j])) continue;
+    cd t = kZero;
+    for (int64_t i = 0; i < d; ++i) t = cadd(t, cmul(cconj(x[i]), leaf_at(A, i, j)));
+    s = cadd(s, cmul(t, y[j]));
+  }
+  return s;
+}
+
+cd dotc(const std::vector<cd>& a, const std::vector<cd>& b) {
+  cd s = kZero;
+  for (size_t i = 0; i < a.size(); ++i) s = cadd(s, cmul(cconj(a[i]), b[i]));
+  return s;
+}
+
+bool is_leaf(const Node* f) { return f->kind == K_SPARSE || f->kind == K_DENSE || f->kind == K_EYE; }
+
+// mul!(y::LazyKet, op::LazyTensor, x::LazyKet, alpha, 0) (src/states_lazyket.jl:131-150)
+void lazyket_mul(const Node* op, cd alpha, const std::vector<std::vector<cd>>& x,
+                 std::vector<std::vector<cd>>& y) {
+  if (op->kind != K_LT) fail(E_UNSUP, "mul! on a LazyKet needs a LazyTensor");
+  for (size_t i = 0; i < x.size(); ++i) {
+    int fi = -1;
+    for (size_t q = 0; q < op->indices.size(); ++q)
+      if (op->indices[q] == (int64_t)i + 1) fi = (int)q;
+    if (fi >= 0) {
+      const Node* f = op->ops[fi];
+      if (!is_leaf(f)) fail(E_UNSUP, "LazyKet factors must be data operators");
+      mul_left(true, f, kOne, x[i].data(), (int64_t)x[i].size(), 1, kZero, y[i].data(), (int64_t)y[i].size(), 1);
+    } else {
+      y[i] = x[i];
+    }
+  }
+  const cd s = cmul(op->factor, alpha);
+  for (cd& v : y[0]) v = cmul(v, s);
+}
+
+cd expect_lazyket(const Node* op, const std::vector<std::vector<cd>>& kets) {
+  switch (op->kind) {
+    case K_LT: {  // :64-84
+      cd e = op->factor;
+      for (size_t i = 0; i < op->ops.size(); ++i) {
+        const Node* f = op->ops[i];
+        if (!is_leaf(f)) fail(E_UNSUP, "LazyKet factors must be data operators");
+        const auto& k = kets[op->indices[i] - 1];
+        e = cmul(e, dot3(k.data(), f, k.data(), (int64_t)k.size()));
+      }
+      for (size_t i = 0; i < kets.size(); ++i) {
+        bool in = false;
+        for (int64_t q : op->indices) in |= (q == (int64_t)i + 1);
+        if (!in) e = cmul(e, dotc(kets[i], kets[i]));
+      }
+      return e;
+    }
+    case K_LP: {  // :86-107
+      std::vector<std::vector<cd>> t1 = kets, t2 = kets;
+      for (int64_t i = (int64_t)op->ops.size() - 1; i >= 0; --i) {
+        lazyket_mul(op->ops[i], kOne, t1, t2);
+        t1 = t2;
+      }
+      cd e = op->factor;
+      for (size_t j = 0; j < kets.size(); ++j) e = cmul(e, dotc(kets[j], t2[j]));
+      return e;
+    }
+    case K_LS: {  // :109-120
+      cd e = kZero;
+      for (size_t k = 0; k < op->ops.size(); ++k) e = cadd(e, cmul(op->factors[k], expect_lazyket(op->ops[k], kets)));
+      return e;
+    }
+    default:
+      fail(E_UNSUP, "expect on a LazyKet needs a LazyTensor, LazySum or LazyProduct");
+  }
+  return kZero;
 }
 
 template <class F>
@@ -838,6 +1043,22 @@ oref_node* oref_lazyproduct(int nops, oref_node* const* ops, double factor_re, d
   return p;
 }
 
+oref_node* oref_fft(int nsub, const int64_t* shape, int naxes, const int64_t* axes, int sign,
+                    const double* mul_before, const double* mul_after) {
+  auto* p = new Node;
+  p->kind = K_FFT;
+  p->shape_l.assign(shape, shape + nsub);
+  p->shape_r = p->shape_l;
+  p->m = p->n = prod(p->shape_l);
+  for (int a = 0; a < naxes; ++a) p->fft_axes.push_back((int)axes[a] - 1);
+  p->fft_sign = sign < 0 ? -1 : 1;
+  for (int64_t k = 0; k < p->m; ++k) {
+    p->mul_before.push_back({mul_before[2 * k], mul_before[2 * k + 1]});
+    p->mul_after.push_back({mul_after[2 * k], mul_after[2 * k + 1]});
+  }
+  return p;
+}
+
 int oref_lazysum_set_factors(oref_node* s, const double* factors) {
   if (s->kind != K_LS) return E_UNSUP;
   for (size_t i = 0; i < s->factors.size(); ++i) s->factors[i] = {factors[2 * i], factors[2 * i + 1]};
@@ -892,6 +1113,23 @@ int oref_mul_kets_threaded(const oref_node* op, double alpha_re, double alpha_im
       return rc[t];
     }
   return 0;
+}
+
+// expect(op, ψ::LazyKet) (src/states_lazyket.jl:64-125); kets: nsites site kets,
+// concatenated.  A LazyTensor's factors must be data operators.
+int oref_expect_lazyket(const oref_node* op, int nsites, const int64_t* dims, const double* kets,
+                        double* result) {
+  return guarded([&] {
+    std::vector<std::vector<cd>> psi(nsites);
+    const cd* k = reinterpret_cast<const cd*>(kets);
+    for (int i = 0; i < nsites; ++i) {
+      psi[i].assign(k, k + dims[i]);
+      k += dims[i];
+    }
+    const cd e = expect_lazyket(op, psi);
+    result[0] = e.re;
+    result[1] = e.im;
+  });
 }
 
 const char* oref_last_error(void) { return g_err.c_str(); }

@@ -48,6 +48,12 @@ oref_node* oref_lazysum(int64_t m, int64_t n, int nterms, const double* factors,
                         oref_node* const* ops);
 /* LazyProduct(operators, factor) (src/operators_lazyproduct.jl:33-52). */
 oref_node* oref_lazyproduct(int nops, oref_node* const* ops, double factor_re, double factor_im);
+/* FFTOperator (src/particle.jl:196-535) on a composite shape of nsub
+ * subsystems: the transformed subsystems axes (1-based, increasing), the sign
+ * of the transform applied to kets (fft_r!: -1 fft, +1 bfft) and the full
+ * phase arrays mul_before / mul_after (prod(shape) complex values each). */
+oref_node* oref_fft(int nsub, const int64_t* shape, int naxes, const int64_t* axes, int sign,
+                    const double* mul_before, const double* mul_after);
 /* Rewrite the factors of a LazySum in place (TimeDependentSum's
  * update_static_coefficients!, src/time_dependent_operator.jl:279-290). */
 int oref_lazysum_set_factors(oref_node* sum, const double* factors);
@@ -70,6 +76,11 @@ int oref_mul(int side, int is_vector, const oref_node* op, double alpha_re, doub
  * spread over nthreads host threads.  Used as the timed CPU baseline. */
 int oref_mul_kets_threaded(const oref_node* op, double alpha_re, double alpha_im, const double* x,
                            double beta_re, double beta_im, double* y, int64_t nvec, int nthreads);
+
+/* expect(op, LazyKet(basis, kets)) (src/states_lazyket.jl:64-125): kets are
+ * the nsites site kets (lengths dims) concatenated; result = one complex. */
+int oref_expect_lazyket(const oref_node* op, int nsites, const int64_t* dims, const double* kets,
+                        double* result);
 
 const char* oref_last_error(void);
 

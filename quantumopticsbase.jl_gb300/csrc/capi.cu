@@ -133,6 +133,25 @@ void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, i
     }
     return;
   }
+  if (P.kind == Plan::Kind::Fft) {
+    // FFTOperator mul! (src/particle.jl:438-535): one pass per transformed axis;
+    // the first reads x, the last writes alpha * ... + beta * y
+    const size_t na = P.fft.size();
+    const void* src = x;
+    int64_t ses = xes, scs = xcs;
+    for (size_t a = 0; a < na; ++a) {
+      if (a + 1 == na) {
+        launch_fft_pass(P.precision, P.fft[a], P.m, src, ses, scs, y, yes, ycs, ncols, alpha, beta, true, s);
+      } else {
+        void* t = ctx.ws.get(ws + (a % 2), (size_t)P.m * ncols * esz);
+        launch_fft_pass(P.precision, P.fft[a], P.m, src, ses, scs, t, 1, P.m, ncols, one, zero, false, s);
+        src = t;
+        ses = 1;
+        scs = P.m;
+      }
+    }
+    return;
+  }
   // LazyProduct (src/operators_lazyproduct.jl:103-164)
   if (is_zero(alpha)) {
     launch_scale(P.precision, y, P.m, ncols, yes, ycs, beta, s);

@@ -1,0 +1,294 @@
+// fft.cu -- FFTOperator (src/particle.jl:196-535): the transform between a
+// position grid and its momentum grid, applied to kets, bras and operators.
+//
+// The reference multiplies by a phase array (mul_before), runs FFTW's in-place
+// fft!/bfft! over the transformed dimensions, and multiplies by a second phase
+// array that includes 1/sqrt(N) (mul_after); bras and the rows of an operator
+// multiplied from the right go through conj -> opposite-sign transform -> conj,
+// which is the same-sign transform of the row with the two phase arrays
+// swapped (the DFT matrix is symmetric).  Both phase arrays are Kronecker
+// products of per-axis vectors, so a multi-dimensional transform is one pass per
+// axis, each pass multiplying by its axis's phases.
+//
+// Each pass is one kernel: a block per line (the n elements of one axis of
+// one vector), staged in shared memory; powers of two use the radix-2
+// Stockham autosort FFT (Van Loan, Computational Frameworks for the FFT, 1992:
+// log2 n stages, each reading one buffer and writing the other in natural
+// order), other lengths a direct DFT over a twiddle table.  The last pass
+// applies alpha and beta.
+#include <cmath>
+#include <vector>
+
+#include "qob_internal.h"
+
+namespace qob {
+namespace {
+
+template <typename R>
+struct CxT;
+template <>
+struct CxT<double> {
+  using T = double2;
+};
+template <>
+struct CxT<float> {
+  using T = float2;
+};
+
+template <typename CT>
+__device__ __forceinline__ CT cm(CT a, CT b) {
+  CT o;
+  o.x = a.x * b.x - a.y * b.y;
+  o.y = a.x * b.y + a.y * b.x;
+  return o;
+}
+
+// Element k of line `line`: the line is (vector c, position p among the len/n
+// lines of one vector); p = lo + stride * hi with lo < stride.
+__device__ __forceinline__ int64_t line_base(int64_t line, int64_t lines_per_vec, int64_t stride, int64_t n,
+                                             int64_t es, int64_t cs) {
+  const int64_t c = line / lines_per_vec;
+  const int64_t p = line - c * lines_per_vec;
+  const int64_t lo = p % stride, hi = p / stride;
+  return c * cs + (lo + hi * stride * n) * es;
+}
+
+template <typename CT, bool FINAL, int BMODE>
+__device__ __forceinline__ void store(CT* y, CT v, CT post, CT alpha, CT beta) {
+  CT o = cm(v, post);
+  if (FINAL) {
+    o = cm(o, alpha);
+    if (BMODE != 0) {
+      const CT b = cm(*y, beta);
+      o.x += b.x;
+      o.y += b.y;
+    }
+  }
+  *y = o;
+}
+
+// Radix-2 Stockham FFT of one line in shared memory (n a power of two, n >= 2).
+template <typename CT, bool FINAL, int BMODE>
+__global__ void __launch_bounds__(256) k_fft_pow2(int64_t n, int log2n, int64_t stride, int64_t lines_per_vec,
+                                                  const CT* __restrict__ x, int64_t xes, int64_t xcs,
+                                                  CT* __restrict__ y, int64_t yes, int64_t ycs,
+                                                  const CT* __restrict__ tw, const CT* __restrict__ pre,
+                                                  const CT* __restrict__ post, CT alpha, CT beta) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  CT* a = reinterpret_cast<CT*>(smem);
+  CT* b = a + n;
+  const int64_t line = blockIdx.x;
+  const CT* xl = x + line_base(line, lines_per_vec, stride, n, xes, xcs);
+  const int64_t se = stride * xes;
+  for (int64_t k = threadIdx.x; k < n; k += blockDim.x) a[k] = cm(xl[k * se], pre[k]);
+  __syncthreads();
+  const int64_t half = n >> 1;
+  for (int st = 0; st < log2n; ++st) {
+    const int64_t ns = int64_t(1) << st;  // half-length of the sub-transforms being merged
+    for (int64_t j = threadIdx.x; j < half; j += blockDim.x) {
+      const int64_t k = j & (ns - 1);
+      const CT t = tw[k << (log2n - 1 - st)];
+      const CT u = a[j];
+      const CT v = cm(a[j + half], t);
+      const int64_t i0 = 2 * j - k;
+      CT s0, s1;
+      s0.x = u.x + v.x;
+      s0.y = u.y + v.y;
+      s1.x = u.x - v.x;
+      s1.y = u.y - v.y;
+      b[i0] = s0;
+      b[i0 + ns] = s1;
+    }
+    __syncthreads();
+    CT* t = a;
+    a = b;
+    b = t;
+  }
+  CT* yl = y + line_base(line, lines_per_vec, stride, n, yes, ycs);
+  const int64_t so = stride * yes;
+  for (int64_t k = threadIdx.x; k < n; k += blockDim.x) store<CT, FINAL, BMODE>(yl + k * so, a[k], post[k], alpha, beta);
+}
+
+// Direct DFT of one line (any n): out_k = sum_j in_j * w^((j k) mod n).
+template <typename CT, bool FINAL, int BMODE>
+__global__ void __launch_bounds__(256) k_dft_line(int64_t n, int64_t stride, int64_t lines_per_vec,
+                                                  const CT* __restrict__ x, int64_t xes, int64_t xcs,
+                                                  CT* __restrict__ y, int64_t yes, int64_t ycs,
+                                                  const CT* __restrict__ tw, const CT* __restrict__ pre,
+                                                  const CT* __restrict__ post, CT alpha, CT beta) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  CT* a = reinterpret_cast<CT*>(smem);
+  const int64_t line = blockIdx.x;
+  const CT* xl = x + line_base(line, lines_per_vec, stride, n, xes, xcs);
+  const int64_t se = stride * xes;
+  for (int64_t k = threadIdx.x; k < n; k += blockDim.x) a[k] = cm(xl[k * se], pre[k]);
+  __syncthreads();
+  CT* yl = y + line_base(line, lines_per_vec, stride, n, yes, ycs);
+  const int64_t so = stride * yes;
+  for (int64_t k = threadIdx.x; k < n; k += blockDim.x) {
+    CT acc;
+    acc.x = 0;
+    acc.y = 0;
+    int64_t idx = 0;
+    for (int64_t j = 0; j < n; ++j) {
+      const CT t = cm(a[j], tw[idx]);
+      acc.x += t.x;
+      acc.y += t.y;
+      idx += k;
+      if (idx >= n) idx -= n;
+    }
+    store<CT, FINAL, BMODE>(yl + k * so, acc, post[k], alpha, beta);
+  }
+}
+
+template <typename R, bool FINAL, int BMODE>
+void launch_typed(const FftAxis& ax, int64_t len, const void* x, int64_t xes, int64_t xcs, void* y, int64_t yes,
+                  int64_t ycs, int64_t ncols, c128 alpha, c128 beta, cudaStream_t s) {
+  using CT = typename CxT<R>::T;
+  CT a, b;
+  a.x = (R)alpha.re;
+  a.y = (R)alpha.im;
+  b.x = (R)beta.re;
+  b.y = (R)beta.im;
+  const int64_t lines_per_vec = len / ax.n;
+  const int threads = (int)std::min<int64_t>(256, std::max<int64_t>(32, ax.pow2 ? ax.n / 2 : ax.n));
+  // whole vectors per launch, at most 2^31 - 1 lines (blocks)
+  const int64_t vec_per_launch = std::max<int64_t>(1, (int64_t)INT32_MAX / lines_per_vec);
+  for (int64_t c0 = 0; c0 < ncols; c0 += vec_per_launch) {
+    const int64_t nl = std::min<int64_t>(ncols - c0, vec_per_launch) * lines_per_vec;
+    const CT* xs = (const CT*)x + c0 * xcs;
+    CT* ys = (CT*)y + c0 * ycs;
+    if (ax.pow2) {
+      const size_t smem = 2 * (size_t)ax.n * sizeof(CT);
+      auto k = k_fft_pow2<CT, FINAL, BMODE>;
+      if (smem > 48 * 1024) QOB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      int log2n = 0;
+      while ((int64_t(1) << log2n) < ax.n) ++log2n;
+      k<<<(unsigned)nl, threads, smem, s>>>(ax.n, log2n, ax.stride, lines_per_vec, xs, xes, xcs, ys, yes, ycs,
+                                            (const CT*)ax.tw.p, (const CT*)ax.pre.p, (const CT*)ax.post.p, a, b);
+    } else {
+      const size_t smem = (size_t)ax.n * sizeof(CT);
+      auto k = k_dft_line<CT, FINAL, BMODE>;
+      if (smem > 48 * 1024) QOB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k<<<(unsigned)nl, threads, smem, s>>>(ax.n, ax.stride, lines_per_vec, xs, xes, xcs, ys, yes, ycs,
+                                            (const CT*)ax.tw.p, (const CT*)ax.pre.p, (const CT*)ax.post.p, a, b);
+    }
+    QOB_LAUNCHED();
+  }
+}
+
+void upload_prec(DeviceBuf& d, const std::vector<c128>& v, int precision) {
+  if (precision == QOB_C128) {
+    d.upload(v.data(), v.size() * sizeof(c128));
+  } else {
+    std::vector<c64> f(v.size());
+    for (size_t i = 0; i < v.size(); ++i) f[i] = {(float)v[i].re, (float)v[i].im};
+    d.upload(f.data(), f.size() * sizeof(c64));
+  }
+}
+
+}  // namespace
+
+void launch_fft_pass(int precision, const FftAxis& ax, int64_t len, const void* x, int64_t xes, int64_t xcs,
+                     void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta, bool final,
+                     cudaStream_t s) {
+  const bool b0 = beta.re == 0.0 && beta.im == 0.0;
+  if (precision == QOB_C128) {
+    if (!final) launch_typed<double, false, 0>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+    else if (b0) launch_typed<double, true, 0>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+    else launch_typed<double, true, 2>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+  } else {
+    if (!final) launch_typed<float, false, 0>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+    else if (b0) launch_typed<float, true, 0>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+    else launch_typed<float, true, 2>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+  }
+}
+
+// LEFT (kets, operator columns): pre = before, post = after.  RIGHT (bras,
+// operator rows): pre = after, post = before, same sign.
+std::unique_ptr<Plan> compile_fft(const NodeP& op, int side, int precision) {
+  auto P = std::make_unique<Plan>();
+  P->kind = Plan::Kind::Fft;
+  P->side = side;
+  P->precision = precision;
+  P->m = side == QOB_RIGHT ? op->n : op->m;
+  P->n = side == QOB_RIGHT ? op->m : op->n;
+  P->root = op.get();
+  const std::vector<int64_t>& shape = op->shape_l;
+  int64_t off = 0;
+  for (size_t a = 0; a < op->fft_sites.size(); ++a) {
+    const int site = op->fft_sites[a];
+    FftAxis ax;
+    ax.n = shape[site];
+    ax.stride = 1;
+    for (int q = 0; q < site; ++q) ax.stride *= shape[q];
+    ax.pow2 = (ax.n & (ax.n - 1)) == 0 && ax.n >= 2;
+    const size_t esz = precision == QOB_C128 ? 16 : 8;
+    const size_t smem = (ax.pow2 ? 2 : 1) * (size_t)ax.n * esz;
+    if (smem > 200 * 1024) fail(QOB_ERR_UNSUPPORTED, "FFT axis too long for one block's shared memory");
+    const double sgn = op->fft_sign[a] < 0 ? -1.0 : 1.0;
+    const int64_t ntw = ax.pow2 ? ax.n / 2 : ax.n;
+    std::vector<c128> tw((size_t)std::max<int64_t>(ntw, 1));
+    for (int64_t m = 0; m < ntw; ++m) {
+      const double th = 6.283185307179586476925286766559 * (double)m / (double)ax.n;
+      tw[(size_t)m] = {std::cos(th), sgn * std::sin(th)};
+    }
+    std::vector<c128> before(op->fft_before.begin() + off, op->fft_before.begin() + off + ax.n);
+    std::vector<c128> after(op->fft_after.begin() + off, op->fft_after.begin() + off + ax.n);
+    off += ax.n;
+    upload_prec(ax.tw, tw, precision);
+    upload_prec(ax.pre, side == QOB_RIGHT ? after : before, precision);
+    upload_prec(ax.post, side == QOB_RIGHT ? before : after, precision);
+    P->fft.push_back(std::move(ax));
+  }
+  return P;
+}
+
+}  // namespace qob
+
+namespace {
+qob_op* wrap_node(qob::NodeP n) {
+  auto* h = new qob_op;
+  h->node = std::move(n);
+  return h;
+}
+}  // namespace
+
+extern "C" int qob_op_fft(qob_ctx* ctx, int nsub, const int64_t* shape, int naxes, const int64_t* axes,
+                          const int* sign, const double* before, const double* after, qob_op** out) {
+  if (!ctx) return QOB_ERR_ARG;
+  try {
+    using namespace qob;
+    if (!out || nsub < 1 || nsub > kMaxSites || !shape || naxes < 1 || naxes > nsub || !axes || !sign || !before ||
+        !after)
+      fail(QOB_ERR_ARG, "qob_op_fft: bad arguments");
+    auto nd = std::make_shared<OpNode>();
+    nd->kind = Kind::Fft;
+    nd->shape_l.assign(shape, shape + nsub);
+    nd->shape_r = nd->shape_l;
+    int64_t len = 1;
+    for (int i = 0; i < nsub; ++i) {
+      if (shape[i] < 1) fail(QOB_ERR_ARG, "qob_op_fft: bad subsystem length");
+      len *= shape[i];
+    }
+    if (len > INT32_MAX) fail(QOB_ERR_UNSUPPORTED, "dimension exceeds 2^31-1");
+    nd->m = nd->n = len;
+    int64_t total = 0;
+    for (int a = 0; a < naxes; ++a) {
+      if (axes[a] < 1 || axes[a] > nsub || (a > 0 && axes[a] <= axes[a - 1]))
+        fail(QOB_ERR_ARG, "qob_op_fft: axes must be increasing 1-based subsystem indices");
+      nd->fft_sites.push_back((int)axes[a] - 1);
+      nd->fft_sign.push_back(sign[a] < 0 ? -1 : 1);
+      total += shape[axes[a] - 1];
+    }
+    for (int64_t k = 0; k < total; ++k) {
+      nd->fft_before.push_back({before[2 * k], before[2 * k + 1]});
+      nd->fft_after.push_back({after[2 * k], after[2 * k + 1]});
+    }
+    *out = wrap_node(nd);
+    return QOB_OK;
+  } catch (const qob::Error& e) {
+    ctx->c.err = e.msg;
+    return e.code;
+  }
+}

@@ -407,7 +407,8 @@ __global__ void __launch_bounds__(256) k_gather_j(GatherView g, SiteTable st,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const ET* ell = stage<ET>(smem_raw, g);
   const GGroup* sg = reinterpret_cast<const GGroup*>(smem_raw);
-  const int64_t J = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t blk = (int64_t)(((uint64_t)blockIdx.x * g.jmul) % (uint64_t)gridDim.x);
+  const int64_t J = blk * blockDim.x + threadIdx.x;
   if (J >= g.m) return;
   const int c0 = blockIdx.y * TC;
   const int nt = min(TC, ncols - c0);
@@ -445,7 +446,7 @@ __global__ void __launch_bounds__(256) k_gather_p(GatherView g, SiteTable st,
   const int lane = threadIdx.x & 31;
   for (int64_t c = lo + (threadIdx.x >> 5); c < hi; c += blockDim.x >> 5) {
     const int64_t tile = c / nj;
-    const int64_t J = (c - tile * nj) * 32 + lane;
+    const int64_t J = (int64_t)(((uint64_t)(c - tile * nj) * g.jmul) % (uint64_t)nj) * 32 + lane;
     if (J >= g.m) continue;
     const int c0 = (int)tile * TC;
     const int nt = min(TC, ncols - c0);
@@ -511,7 +512,9 @@ void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t x
     QOB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     QOB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk, threads, smem));
     if (occ > 0) {
-      pk<<<(unsigned)(sms * occ), threads, smem, s>>>(v, st, (const CT*)x, xcs, (CT*)y, ycs, (int)ncols, a, b);
+      GatherView w = v;
+      w.jmul = chunk_multiplier((v.m + 31) / 32);
+      pk<<<(unsigned)(sms * occ), threads, smem, s>>>(w, st, (const CT*)x, xcs, (CT*)y, ycs, (int)ncols, a, b);
       QOB_LAUNCHED();
       return;
     }
@@ -520,10 +523,12 @@ void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t x
   allow_smem(kern, smem);
   const int threads = v.block > 0 ? v.block : kThreads;
   const unsigned gx = (unsigned)((v.m + threads - 1) / threads);
+  GatherView w = v;
+  w.jmul = chunk_multiplier(gx);
   for (int64_t c0 = 0; c0 < ncols; c0 += (int64_t)65535 * TC) {  // grid.y limit
     const int64_t nc = std::min<int64_t>(ncols - c0, (int64_t)65535 * TC);
     kern<<<dim3(gx, (unsigned)((nc + TC - 1) / TC)), threads, smem, s>>>(
-        v, st, (const CT*)x + c0 * xcs, xcs, (CT*)y + c0 * ycs, ycs, (int)nc, a, b);
+        w, st, (const CT*)x + c0 * xcs, xcs, (CT*)y + c0 * ycs, ycs, (int)nc, a, b);
     QOB_LAUNCHED();
   }
 }

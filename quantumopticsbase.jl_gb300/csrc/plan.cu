@@ -736,6 +736,7 @@ static std::unique_ptr<Plan> compile_sum(Context& ctx, const NodeP& root, int si
             if (r.val[p].re != 0.0 || r.val[p].im != 0.0) g.raw.push_back({row, r.col[p], term, r.val[p]});
         break;
       }
+      case Kind::Fft:
       case Kind::LazyProduct: {
         SubPass sp;
         sp.coef = coef;
@@ -817,6 +818,7 @@ static void finalize_gather(GatherPlan& gp, GatherBuilder& B, const OpNode* root
 }
 
 std::unique_ptr<Plan> compile_plan(Context& ctx, const NodeP& op, int side, int precision) {
+  if (op->kind == Kind::Fft) return compile_fft(op, side, precision);
   if (op->kind == Kind::LazyProduct) {
     auto P = std::make_unique<Plan>();
     P->kind = Plan::Kind::Product;
@@ -956,6 +958,7 @@ void prepare_factor_rows(Plan& plan, const OpNode& root, const double* rows, int
 
 GatherView GatherPlan::view() const {
   GatherView v;
+  v.jmul = chunk_multiplier((m + 31) / 32);
   v.m = m;
   v.n = n;
   v.ngroups = ngroups;

@@ -53,7 +53,7 @@ void count_launch();
 // ---------------------------------------------------------------------------
 // operator tree (host)
 // ---------------------------------------------------------------------------
-enum class Kind { Sparse, Dense, Eye, LazyTensor, LazySum, LazyProduct };
+enum class Kind { Sparse, Dense, Eye, LazyTensor, LazySum, LazyProduct, Fft };
 
 struct OpNode {
   Kind kind;
@@ -71,6 +71,11 @@ struct OpNode {
   c128 factor{1.0, 0.0};
   std::vector<c128> factors;  // LazySum
   uint64_t factors_version = 0;
+  // Fft: DFT along fft_sites (0-based, increasing) of the composite shape shape_l,
+  // with per-axis sign (-1: e^{-2 pi i jk/N}, +1: e^{+2 pi i jk/N}) and phase
+  // vectors applied before / after (concatenated in axis order)
+  std::vector<int> fft_sites, fft_sign;
+  std::vector<c128> fft_before, fft_after;
 };
 using NodeP = std::shared_ptr<OpNode>;
 
@@ -157,6 +162,11 @@ struct GatherView {
   int32_t fast;      // 1: fastg holds {log2 div, mod - 1, first slot, 0} per group
   const int4* fastg; // compact form: one run of power-of-two subsystems, width 1
   int32_t block;     // threads per block of the index-lanes kernel (0: 256; < 0: persistent grid of -block)
+  // Blocks of output indices (k_gather_j) or warp-sized chunks (k_gather_p) are visited in the
+  // order c -> (c * jmul) mod count (jmul coprime to count, set per launch): consecutive blocks
+  // cover index ranges far apart, so the cost of a block -- which depends on the high index
+  // bits through the operator's sparsity -- averages out over the blocks an SM runs.
+  uint32_t jmul;
 };
 
 // A host-side record of how each stored entry is made from the terms, so a
@@ -272,8 +282,16 @@ struct SubPass {
   std::unique_ptr<Plan> plan;
 };
 
+// One axis of an FFT plan: lines of n elements at stride `stride` (in vector
+// elements); pre / post phases on the side's order; twiddles of the sign.
+struct FftAxis {
+  int64_t n = 0, stride = 1;
+  bool pow2 = true;
+  DeviceBuf tw, pre, post;  // plan precision: n/2 (power of two) or n twiddles; n phases each
+};
+
 struct Plan {
-  enum class Kind { Sum, Product } kind = Kind::Sum;
+  enum class Kind { Sum, Product, Fft } kind = Kind::Sum;
   int side = QOB_LEFT;
   int precision = QOB_C128;
   int64_t m = 0, n = 0;  // rows of the output vectors / of the input vectors
@@ -286,6 +304,8 @@ struct Plan {
   // Product
   c128 pfactor{1.0, 0.0};
   std::vector<std::unique_ptr<Plan>> chain;  // in application order
+  // Fft
+  std::vector<FftAxis> fft;
   // dependency record: (node, factors_version) of every LazySum inside
   std::vector<std::pair<const OpNode*, uint64_t>> deps;
   const OpNode* root = nullptr;
@@ -328,6 +348,12 @@ void launch_gather(const GatherPlan& g, int precision, const void* x, int64_t xe
                    cudaStream_t s);
 void launch_build_diag(const GatherPlan& g, cudaStream_t s);
 void launch_td_values(const GatherPlan& g, const double2* factors_dev, cudaStream_t s);
+// One FFT pass along an axis of every vector: y = alpha * post .* DFT(pre .* x) + beta * y
+// (beta ignored when final == false: y is overwritten).
+void launch_fft_pass(int precision, const FftAxis& ax, int64_t len, const void* x, int64_t xes, int64_t xcs,
+                     void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta, bool final,
+                     cudaStream_t s);
+std::unique_ptr<Plan> compile_fft(const NodeP& op, int side, int precision);
 int gather_tile(const GatherPlan& g, int64_t ncols);
 void launch_scale(int precision, void* y, int64_t rows, int64_t cols, int64_t ld_row,
                   int64_t ld_col, c128 beta, cudaStream_t s);
@@ -347,6 +373,23 @@ void reduce_dot(Context& ctx, int precision, const void* x, const void* y, int64
 void apply_plan(Context& ctx, Plan& plan, c128 alpha, const void* x, int64_t xes, int64_t xcs,
                 c128 beta, void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s,
                 int ws_base);
+
+// A multiplier coprime to n near n * (sqrt(5) - 1) / 2: c -> (c * mul) mod n
+// visits 0 .. n-1 in an order where neighbours are far apart (1 for n <= 2).
+inline uint32_t chunk_multiplier(int64_t n) {
+  if (n <= 2) return 1;
+  int64_t a = (int64_t)((double)n * 0.6180339887498949) | 1;
+  auto gcd = [](int64_t x, int64_t y) {
+    while (y) {
+      int64_t t = x % y;
+      x = y;
+      y = t;
+    }
+    return x;
+  };
+  while (gcd(a, n) != 1) a += 2;
+  return (uint32_t)(a % n);
+}
 
 // Lemire, Kaser & Kurz (2019) "Faster remainder by direct computation":
 // for 32-bit n and d > 1, n / d == umulhi64(M, n) and n % d ==

@@ -5,8 +5,8 @@ LazyTensor, LazySum, LazyProduct, TimeDependentSum) over the C-ABI library
 libqobgpu.so, whose hand-written sm_103a kernels do the work.  ``mul_`` is the
 reference's 5-argument ``mul!(result, a, b, alpha, beta)``.
 """
-from .bases import (Basis, CompositeBasis, FockBasis, GenericBasis, NLevelBasis, SpinBasis,
-                    comp_size)
+from .bases import (Basis, CompositeBasis, FockBasis, GenericBasis, MomentumBasis, NLevelBasis,
+                    PositionBasis, SpinBasis, comp_size, samplepoints, spacing)
 from .bases import tensor as tensor_basis
 from .operators import *  # noqa: F401,F403
 from .operators import __all__ as _ops_all

@@ -64,6 +64,8 @@ SIGNATURES = {
     "qob_batch_info": (I, [VP, VP, I64P]),
     "qob_batch_free": (I, [VP, VP]),
     "qob_rk4": (I, [VP, VP, I, VP, I64, D, I, I, VP]),
+    "qob_op_fft": (I, [VP, I, I64P, I, I64P, C.POINTER(C.c_int), DP, DP, C.POINTER(VP)]),
+    "qob_expect_lazyket": (I, [VP, VP, I, I, I64P, VP, I64, VP, VP]),
     "qob_rk4_td": (I, [VP, VP, I, VP, I64, D, I, VP, I64, I, VP]),
     "qob_server_create": (I, [VP, I, C.c_size_t, I, I, C.POINTER(VP)]),
     "qob_server_submit": (I, [VP, VP, VP, I64, I, D, I64P]),

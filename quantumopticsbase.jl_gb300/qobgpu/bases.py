@@ -8,7 +8,7 @@ src/states.jl:105; ``_comp_size``, src/operators_lazytensor.jl:517-518).
 from __future__ import annotations
 
 from fractions import Fraction
-from math import prod
+from math import pi, prod
 
 
 class Basis:
@@ -81,6 +81,55 @@ class SpinBasis(Basis):
 
     def _key(self):
         return ("SpinBasis", self.spinnumber)
+
+
+class PositionBasis(Basis):
+    """Real-space grid of N points x_i = xmin + i (xmax - xmin) / N, i = 0 .. N-1
+    (QuantumInterface's PositionBasis; spacing / samplepoints, src/particle.jl:70-96).
+    ``PositionBasis(b::MomentumBasis)`` is the grid the FFT pairs with b."""
+
+    def __init__(self, xmin, xmax=None, N=None):
+        if isinstance(xmin, MomentumBasis):
+            b = xmin
+            dp = (b.pmax - b.pmin) / b.N
+            xmin, xmax, N = -pi / dp, pi / dp, b.N
+        self.xmin, self.xmax, self.N = float(xmin), float(xmax), int(N)
+        self.shape = (self.N,)
+
+    def _key(self):
+        return ("PositionBasis", self.xmin, self.xmax, self.N)
+
+
+class MomentumBasis(Basis):
+    """Momentum grid of N points p_i = pmin + i (pmax - pmin) / N;
+    ``MomentumBasis(b::PositionBasis)`` is the grid the FFT pairs with b."""
+
+    def __init__(self, pmin, pmax=None, N=None):
+        if isinstance(pmin, PositionBasis):
+            b = pmin
+            dx = (b.xmax - b.xmin) / b.N
+            pmin, pmax, N = -pi / dx, pi / dx, b.N
+        self.pmin, self.pmax, self.N = float(pmin), float(pmax), int(N)
+        self.shape = (self.N,)
+
+    def _key(self):
+        return ("MomentumBasis", self.pmin, self.pmax, self.N)
+
+
+def spacing(b) -> float:
+    """(src/particle.jl:70-82)"""
+    if isinstance(b, PositionBasis):
+        return (b.xmax - b.xmin) / b.N
+    if isinstance(b, MomentumBasis):
+        return (b.pmax - b.pmin) / b.N
+    raise TypeError("spacing of a PositionBasis or MomentumBasis")
+
+
+def samplepoints(b):
+    """(src/particle.jl:84-96): [min + i * spacing for i = 0 .. N-1]."""
+    d = spacing(b)
+    lo = b.xmin if isinstance(b, PositionBasis) else b.pmin
+    return [lo + i * d for i in range(b.N)]
 
 
 class CompositeBasis(Basis):

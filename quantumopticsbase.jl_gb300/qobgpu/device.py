@@ -136,6 +136,17 @@ def _build(ctx: Context, op) -> Handle:
         return Handle(ctx, h, kids)
     if isinstance(op, O.TimeDependentSum):
         return handle(ctx, op.static_op)
+    from .particle import FFTOperator
+
+    if isinstance(op, FFTOperator):
+        shape = np.asarray(op.basis_l.shape, np.int64)
+        axes = np.asarray(op.axes, np.int64)
+        signs = (C.c_int * len(axes))(*([op.sign] * len(axes)))
+        before = np.ascontiguousarray(np.concatenate(op.before)).view(np.float64)
+        after = np.ascontiguousarray(np.concatenate(op.after)).view(np.float64)
+        h = _new(lib.qob_op_fft, ctx, len(shape), _c_array(shape, C.c_int64), len(axes), _c_array(axes, C.c_int64),
+                 signs, _c_array(before, C.c_double), _c_array(after, C.c_double))
+        return Handle(ctx, h)
     raise O.ArgumentError(f"no device form for {type(op).__name__}")
 
 

@@ -13,6 +13,7 @@ submission and completion:
                   Heisenberg chain on a 256 x 256 operator;
 * ``lindblad``    Lindblad right-hand side S rho, lazy Liouvillian of 8 / 10 / 12-spin
                   chains with sigma_- decay (and the materialised one at 8 spins);
+* ``particle``    split-operator particle Hamiltonian (FFT operators) on 4096 and 512 x 512 grids;
 * ``cavities256`` 256 two-mode cavity models (dims 81 ... 4225) in one launch;
 * ``served``      Poisson arrivals of 100-step RK4 requests (Heisenberg chains of
                   8 ... 16 spins, Jaynes-Cummings models of dim 512 ... 8192).
@@ -220,6 +221,51 @@ def lindblad(ctx, stream):
     return {"workload": "lindblad", "results": out}
 
 
+def particle(ctx, stream):
+    """Split-operator particle Hamiltonian H = Txp (p^2/2) Tpx + V(x) (LazySum of a
+    LazyProduct of FFT operators and diagonals, src/particle.jl) on a 1-D grid of
+    4096 points (1 and 64 kets) and a 2-D grid of 512 x 512 points (1 ket), and
+    the bare FFT transform Tpx on the same grids."""
+    import torch
+
+    from . import operators as O
+    from .bases import MomentumBasis, PositionBasis
+    from .bases import tensor as tensor_bases
+    from .particle import momentum, potentialoperator, transform
+
+    out = []
+    grids = [("1d_4096", [PositionBasis(-40.0, 40.0, 4096)]),
+             ("2d_512x512", [PositionBasis(-20.0, 20.0, 512), PositionBasis(-20.0, 20.0, 512)])]
+    for name, bxs in grids:
+        bps = [MomentumBasis(b) for b in bxs]
+        bX = bxs[0] if len(bxs) == 1 else tensor_bases(*bxs)
+        bP = bps[0] if len(bps) == 1 else tensor_bases(*bps)
+        Txp, Tpx = transform(bX, bP), transform(bP, bX)
+        n = len(bX)
+        # kinetic energy diagonal on the momentum grid, potential on the position grid
+        kin = np.zeros(n)
+        for i, b in enumerate(bps):
+            p = np.asarray(momentum(b).data.diagonal()).real
+            stride = int(np.prod([len(x) for x in bps[:i]]))
+            kin += np.tile(np.repeat(p * p / 2, stride), n // (stride * len(b)))
+        K = O.Operator(bP, bP, O.spdiagm(n, n, {0: kin.astype(complex)}))
+        V = potentialoperator(bX, (lambda x: 0.5 * x * x) if len(bxs) == 1 else (lambda x, y: 0.5 * (x * x + y * y)))
+        H = O.LazySum(bX, bX, [1.0, 1.0], (O.LazyProduct((Txp, K, Tpx)), V))
+        for op_name, op in (("H", H), ("Tpx", Tpx)):
+            h = handle(ctx, op)
+            for tdt, npdt in ((torch.complex128, np.complex128), (torch.complex64, np.complex64)):
+                for ncols in ((1, 64) if len(bxs) == 1 else (1,)):
+                    x = _cols(n, ncols, tdt, 50).contiguous() if ncols == 1 else _cols(n, ncols, tdt, 50)
+                    y = _cols(n, ncols, tdt, 51).contiguous() if ncols == 1 else _cols(n, ncols, tdt, 51)
+                    reps = 20
+                    ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, L.QOB_LEFT, n, n, ncols, x, y,
+                                                                 dtype_code(npdt), reps=reps))
+                    t = ms * 1e-3 / reps
+                    out.append({"grid": name, "operator": op_name, "dtype": np.dtype(npdt).name, "kets": ncols,
+                                "us_per_call": t * 1e6, "applies_per_s": ncols / t})
+    return {"workload": "particle", "results": out}
+
+
 def served(ctx, stream, nreq=192, rate=2000.0, seed=50):
     from .evolution import Server
 
@@ -293,7 +339,7 @@ def run_suite(device: int = 0):
 
     ctx = get_context(device)
     stream = torch.cuda.Stream(device)
-    for fn in (jc512, sparse4096, rho_h8, lindblad, cavities256, served, host_link):
+    for fn in (jc512, sparse4096, rho_h8, lindblad, particle, cavities256, served, host_link):
         t0 = time.perf_counter()
         line = fn(ctx, stream)
         line["seconds"] = time.perf_counter() - t0
