@@ -45,8 +45,8 @@ __global__ void __launch_bounds__(256) k_gather_batch(const BatchItemDev* __rest
     const int64_t jend = min((int64_t)td.y + tile, it.v.m);
     for (int64_t J = td.y + threadIdx.x; J < jend; J += blockDim.x) {
       AT acc[1];
-      gather::accumulate<R, REALV, true, false, 1>(it.v, st, sg, ell, (uint32_t)J, (const CT*)it.x, 1, 0, 1,
-                                                   acc);
+      gather::accumulate<R, REALV ? gather::kReal : gather::kComplex, true, false, 1>(
+          it.v, st, sg, ell, (uint32_t)J, (const CT*)it.x, 1, 0, 1, acc);
       CT* yp = (CT*)it.y + J;
       // beta == 0 overwrites y without reading it (NaN in y is ignored)
       const bool bz = it.beta.x == 0.0 && it.beta.y == 0.0;
@@ -83,7 +83,7 @@ const void* batch_kernel(int prec, bool real) {
 
 bool plan_fusable(const Plan& P) {
   return P.kind == Plan::Kind::Sum && P.gather && P.dense.empty() && P.modek.empty() && P.subs.empty() &&
-         P.gather->square && P.gather->ngroups <= 256 && P.nterms_total > 0;
+         P.gather->square && !P.gather->phased && P.gather->ngroups <= 256 && P.nterms_total > 0;
 }
 
 void build_tables(Context& ctx, BatchTables& T, const std::vector<BatchSpec>& specs, int prec, int tile) {

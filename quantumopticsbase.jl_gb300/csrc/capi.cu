@@ -141,10 +141,12 @@ void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, i
     int64_t ses = xes, scs = xcs;
     for (size_t a = 0; a < na; ++a) {
       if (a + 1 == na) {
-        launch_fft_pass(P.precision, P.fft[a], P.m, src, ses, scs, y, yes, ycs, ncols, alpha, beta, true, s);
+        void* scratch = P.fft[a].n1 > 0 ? ctx.ws.get(ws + 2, (size_t)P.m * ncols * esz) : nullptr;
+        launch_fft_pass(P.precision, P.fft[a], P.m, src, ses, scs, y, yes, ycs, ncols, alpha, beta, true, scratch,
+                        s);
       } else {
         void* t = ctx.ws.get(ws + (a % 2), (size_t)P.m * ncols * esz);
-        launch_fft_pass(P.precision, P.fft[a], P.m, src, ses, scs, t, 1, P.m, ncols, one, zero, false, s);
+        launch_fft_pass(P.precision, P.fft[a], P.m, src, ses, scs, t, 1, P.m, ncols, one, zero, false, nullptr, s);
         src = t;
         ses = 1;
         scs = P.m;

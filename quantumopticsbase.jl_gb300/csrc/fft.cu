@@ -67,27 +67,18 @@ __device__ __forceinline__ void store(CT* y, CT v, CT post, CT alpha, CT beta) {
   *y = o;
 }
 
-// Radix-2 Stockham FFT of one line in shared memory (n a power of two, n >= 2).
-template <typename CT, bool FINAL, int BMODE>
-__global__ void __launch_bounds__(256) k_fft_pow2(int64_t n, int log2n, int64_t stride, int64_t lines_per_vec,
-                                                  const CT* __restrict__ x, int64_t xes, int64_t xcs,
-                                                  CT* __restrict__ y, int64_t yes, int64_t ycs,
-                                                  const CT* __restrict__ tw, const CT* __restrict__ pre,
-                                                  const CT* __restrict__ post, CT alpha, CT beta) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  CT* a = reinterpret_cast<CT*>(smem);
-  CT* b = a + n;
-  const int64_t line = blockIdx.x;
-  const CT* xl = x + line_base(line, lines_per_vec, stride, n, xes, xcs);
-  const int64_t se = stride * xes;
-  for (int64_t k = threadIdx.x; k < n; k += blockDim.x) a[k] = cm(xl[k * se], pre[k]);
-  __syncthreads();
+// Radix-2 Stockham FFT in shared memory: a holds n = 2^log2n inputs, b is
+// scratch; twiddle m of the length-n transform is tw[m * tws].  Returns the
+// buffer that holds the output (natural order).
+template <typename CT>
+__device__ __forceinline__ CT* stockham(CT* a, CT* b, int64_t n, int log2n, const CT* __restrict__ tw,
+                                        int64_t tws) {
   const int64_t half = n >> 1;
   for (int st = 0; st < log2n; ++st) {
     const int64_t ns = int64_t(1) << st;  // half-length of the sub-transforms being merged
     for (int64_t j = threadIdx.x; j < half; j += blockDim.x) {
       const int64_t k = j & (ns - 1);
-      const CT t = tw[k << (log2n - 1 - st)];
+      const CT t = tw[(k << (log2n - 1 - st)) * tws];
       const CT u = a[j];
       const CT v = cm(a[j + half], t);
       const int64_t i0 = 2 * j - k;
@@ -104,6 +95,74 @@ __global__ void __launch_bounds__(256) k_fft_pow2(int64_t n, int log2n, int64_t 
     a = b;
     b = t;
   }
+  return a;
+}
+
+// Four-step FFT of long lines over many blocks (Bailey 1990): n = n1 * n2,
+// element j = j2 + n2 * j1.  Pass A: for each (line, j2) the length-n1 FFT
+// over j1, times w_n^(j2 k1), into scratch[line][j2 + n2 k1].  Pass B: for each
+// (line, k1) the length-n2 FFT over j2 gives element k = k1 + n1 k2.
+template <typename CT>
+__global__ void __launch_bounds__(256) k_fft4_a(int64_t n1, int log2n1, int64_t n2, int64_t stride,
+                                                int64_t lines_per_vec, const CT* __restrict__ x, int64_t xes,
+                                                int64_t xcs, CT* __restrict__ scratch,
+                                                const CT* __restrict__ twn, const CT* __restrict__ pre) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  CT* a = reinterpret_cast<CT*>(smem);
+  CT* b = a + n1;
+  const int64_t n = n1 * n2;
+  const int64_t line = blockIdx.x / n2, j2 = blockIdx.x - line * n2;
+  const CT* xl = x + line_base(line, lines_per_vec, stride, n, xes, xcs);
+  const int64_t se = stride * xes;
+  for (int64_t j1 = threadIdx.x; j1 < n1; j1 += blockDim.x) {
+    const int64_t j = j2 + n2 * j1;
+    a[j1] = cm(xl[j * se], pre[j]);
+  }
+  __syncthreads();
+  const CT* r = stockham(a, b, n1, log2n1, twn, n2);
+  CT* out = scratch + line * n;
+  for (int64_t k1 = threadIdx.x; k1 < n1; k1 += blockDim.x) out[j2 + n2 * k1] = cm(r[k1], twn[(j2 * k1) % n]);
+}
+
+template <typename CT, int BMODE>
+__global__ void __launch_bounds__(256) k_fft4_b(int64_t n1, int64_t n2, int log2n2, int64_t stride,
+                                                int64_t lines_per_vec, const CT* __restrict__ scratch,
+                                                CT* __restrict__ y, int64_t yes, int64_t ycs,
+                                                const CT* __restrict__ twn, const CT* __restrict__ post, CT alpha,
+                                                CT beta) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  CT* a = reinterpret_cast<CT*>(smem);
+  CT* b = a + n2;
+  const int64_t n = n1 * n2;
+  const int64_t line = blockIdx.x / n1, k1 = blockIdx.x - line * n1;
+  const CT* in = scratch + line * n + n2 * k1;
+  for (int64_t j2 = threadIdx.x; j2 < n2; j2 += blockDim.x) a[j2] = in[j2];
+  __syncthreads();
+  const CT* r = stockham(a, b, n2, log2n2, twn, n1);
+  CT* yl = y + line_base(line, lines_per_vec, stride, n, yes, ycs);
+  const int64_t so = stride * yes;
+  for (int64_t k2 = threadIdx.x; k2 < n2; k2 += blockDim.x) {
+    const int64_t k = k1 + n1 * k2;
+    store<CT, true, BMODE>(yl + k * so, r[k2], post[k], alpha, beta);
+  }
+}
+
+// Radix-2 Stockham FFT of one line in shared memory (n a power of two, n >= 2).
+template <typename CT, bool FINAL, int BMODE>
+__global__ void __launch_bounds__(256) k_fft_pow2(int64_t n, int log2n, int64_t stride, int64_t lines_per_vec,
+                                                  const CT* __restrict__ x, int64_t xes, int64_t xcs,
+                                                  CT* __restrict__ y, int64_t yes, int64_t ycs,
+                                                  const CT* __restrict__ tw, const CT* __restrict__ pre,
+                                                  const CT* __restrict__ post, CT alpha, CT beta) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  CT* a = reinterpret_cast<CT*>(smem);
+  CT* b = a + n;
+  const int64_t line = blockIdx.x;
+  const CT* xl = x + line_base(line, lines_per_vec, stride, n, xes, xcs);
+  const int64_t se = stride * xes;
+  for (int64_t k = threadIdx.x; k < n; k += blockDim.x) a[k] = cm(xl[k * se], pre[k]);
+  __syncthreads();
+  a = stockham(a, b, n, log2n, tw, 1);
   CT* yl = y + line_base(line, lines_per_vec, stride, n, yes, ycs);
   const int64_t so = stride * yes;
   for (int64_t k = threadIdx.x; k < n; k += blockDim.x) store<CT, FINAL, BMODE>(yl + k * so, a[k], post[k], alpha, beta);
@@ -143,7 +202,7 @@ __global__ void __launch_bounds__(256) k_dft_line(int64_t n, int64_t stride, int
 
 template <typename R, bool FINAL, int BMODE>
 void launch_typed(const FftAxis& ax, int64_t len, const void* x, int64_t xes, int64_t xcs, void* y, int64_t yes,
-                  int64_t ycs, int64_t ncols, c128 alpha, c128 beta, cudaStream_t s) {
+                  int64_t ycs, int64_t ncols, c128 alpha, c128 beta, void* scratch, cudaStream_t s) {
   using CT = typename CxT<R>::T;
   CT a, b;
   a.x = (R)alpha.re;
@@ -151,6 +210,28 @@ void launch_typed(const FftAxis& ax, int64_t len, const void* x, int64_t xes, in
   b.x = (R)beta.re;
   b.y = (R)beta.im;
   const int64_t lines_per_vec = len / ax.n;
+  int dev = 0, sms = 0;
+  QOB_CUDA(cudaGetDevice(&dev));
+  QOB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t lines = lines_per_vec * ncols;
+  if (FINAL && ax.n1 > 0 && scratch && lines < sms && lines * ax.n2 <= INT32_MAX) {
+    // few long lines: spread each over n2 + n1 blocks (two launches)
+    int l1 = 0, l2 = 0;
+    while ((int64_t(1) << l1) < ax.n1) ++l1;
+    while ((int64_t(1) << l2) < ax.n2) ++l2;
+    const int ta = (int)std::min<int64_t>(256, std::max<int64_t>(32, ax.n1 / 2));
+    const int tb = (int)std::min<int64_t>(256, std::max<int64_t>(32, ax.n2 / 2));
+    const size_t sa = 2 * (size_t)ax.n1 * sizeof(CT), sb = 2 * (size_t)ax.n2 * sizeof(CT);
+    k_fft4_a<CT><<<(unsigned)(lines * ax.n2), ta, sa, s>>>(ax.n1, l1, ax.n2, ax.stride, lines_per_vec, (const CT*)x,
+                                                          xes, xcs, (CT*)scratch, (const CT*)ax.tw_full.p,
+                                                          (const CT*)ax.pre.p);
+    QOB_LAUNCHED();
+    k_fft4_b<CT, BMODE><<<(unsigned)(lines * ax.n1), tb, sb, s>>>(ax.n1, ax.n2, l2, ax.stride, lines_per_vec,
+                                                                  (const CT*)scratch, (CT*)y, yes, ycs,
+                                                                  (const CT*)ax.tw_full.p, (const CT*)ax.post.p, a, b);
+    QOB_LAUNCHED();
+    return;
+  }
   const int threads = (int)std::min<int64_t>(256, std::max<int64_t>(32, ax.pow2 ? ax.n / 2 : ax.n));
   // whole vectors per launch, at most 2^31 - 1 lines (blocks)
   const int64_t vec_per_launch = std::max<int64_t>(1, (int64_t)INT32_MAX / lines_per_vec);
@@ -191,16 +272,16 @@ void upload_prec(DeviceBuf& d, const std::vector<c128>& v, int precision) {
 
 void launch_fft_pass(int precision, const FftAxis& ax, int64_t len, const void* x, int64_t xes, int64_t xcs,
                      void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta, bool final,
-                     cudaStream_t s) {
+                     void* scratch, cudaStream_t s) {
   const bool b0 = beta.re == 0.0 && beta.im == 0.0;
   if (precision == QOB_C128) {
-    if (!final) launch_typed<double, false, 0>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
-    else if (b0) launch_typed<double, true, 0>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
-    else launch_typed<double, true, 2>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+    if (!final) launch_typed<double, false, 0>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, scratch, s);
+    else if (b0) launch_typed<double, true, 0>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, scratch, s);
+    else launch_typed<double, true, 2>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, scratch, s);
   } else {
-    if (!final) launch_typed<float, false, 0>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
-    else if (b0) launch_typed<float, true, 0>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
-    else launch_typed<float, true, 2>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+    if (!final) launch_typed<float, false, 0>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, scratch, s);
+    else if (b0) launch_typed<float, true, 0>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, scratch, s);
+    else launch_typed<float, true, 2>(ax, len, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, scratch, s);
   }
 }
 
@@ -237,6 +318,18 @@ std::unique_ptr<Plan> compile_fft(const NodeP& op, int side, int precision) {
     std::vector<c128> after(op->fft_after.begin() + off, op->fft_after.begin() + off + ax.n);
     off += ax.n;
     upload_prec(ax.tw, tw, precision);
+    if (ax.pow2 && ax.n >= 512) {
+      int l = 0;
+      while ((int64_t(1) << l) < ax.n) ++l;
+      ax.n1 = int64_t(1) << (l / 2);
+      ax.n2 = ax.n / ax.n1;
+      std::vector<c128> full((size_t)ax.n);
+      for (int64_t m = 0; m < ax.n; ++m) {
+        const double th = 6.283185307179586476925286766559 * (double)m / (double)ax.n;
+        full[(size_t)m] = {std::cos(th), sgn * std::sin(th)};
+      }
+      upload_prec(ax.tw_full, full, precision);
+    }
     upload_prec(ax.pre, side == QOB_RIGHT ? after : before, precision);
     upload_prec(ax.post, side == QOB_RIGHT ? before : after, precision);
     P->fft.push_back(std::move(ax));

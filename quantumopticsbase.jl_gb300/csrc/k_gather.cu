@@ -17,7 +17,7 @@ extern template void dispatch<float>(const GatherView&, const SiteTable&, int, c
 
 namespace {
 
-constexpr int kGroupsPerLaunch = 256;  // 256 * sizeof(GGroup) = 40 KB of shared memory
+constexpr int kGroupsPerLaunch = 256;  // 256 * sizeof(GGroup) = 44 KB of shared memory
 
 // Merged diagonal: diag[J] = sum over groups of their local diagonal table.
 template <typename R, bool REALV>
@@ -73,9 +73,10 @@ __global__ void __launch_bounds__(256) k_td_values(int nslots, const TdSlot* __r
     im = __dadd_rn(im, __dadd_rn(__dmul_rn(cr, c.pv[1]), __dmul_rn(ci, c.pv[0])));
   }
   if (sl.dst_diag >= 0) dtab[sl.dst_diag] = make_double2(re, im);
+  const double sv = sl.part ? im : re;  // the stored number of a real-storage plan
   if (sl.dst_val >= 0) {
     if constexpr (REALV) {
-      static_cast<R*>(vals)[sl.dst_val] = (R)re;
+      static_cast<R*>(vals)[sl.dst_val] = (R)sv;
     } else {
       typename gather::Cx<R>::T o;
       o.x = (R)re;
@@ -85,13 +86,13 @@ __global__ void __launch_bounds__(256) k_td_values(int nslots, const TdSlot* __r
   }
   if (sl.dst_ell >= 0) {
     if constexpr (sizeof(R) == 8 && REALV) {
-      static_cast<EllD*>(ell)[sl.dst_ell].v = re;
+      static_cast<EllD*>(ell)[sl.dst_ell].v = sv;
     } else if constexpr (sizeof(R) == 8) {
       EllZ& e = static_cast<EllZ*>(ell)[sl.dst_ell];
       e.v[0] = re;
       e.v[1] = im;
     } else if constexpr (REALV) {
-      static_cast<EllF*>(ell)[sl.dst_ell].v = (float)re;
+      static_cast<EllF*>(ell)[sl.dst_ell].v = (float)sv;
     } else {
       EllC& e = static_cast<EllC*>(ell)[sl.dst_ell];
       e.v[0] = (float)re;
@@ -110,13 +111,14 @@ void launch_td_values(const GatherPlan& g, const double2* factors_dev, cudaStrea
   const TdContrib* co = (const TdContrib*)g.td_contrib.p;
   const TdTerm* te = (const TdTerm*)g.td_terms.p;
   double2* dt = (double2*)g.dvals.p;
+  const bool store_real = g.real_vals || g.phased;
   if (g.precision == QOB_C128) {
-    if (g.real_vals)
+    if (store_real)
       k_td_values<double, true><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, g.vals.p, g.ell.p, dt);
     else
       k_td_values<double, false><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, g.vals.p, g.ell.p, dt);
   } else {
-    if (g.real_vals)
+    if (store_real)
       k_td_values<float, true><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, g.vals.p, g.ell.p, dt);
     else
       k_td_values<float, false><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, g.vals.p, g.ell.p, dt);

@@ -57,7 +57,7 @@ struct Cx<float> {
   using T = float2;
 };
 
-template <typename R, bool REALV>
+template <typename R, int VM>
 struct Val {
   using T = typename Cx<R>::T;
 };
@@ -71,7 +71,7 @@ struct Val<float, true> {
 };
 
 // fixed-width slot type per precision / realness, and its value
-template <typename R, bool REALV>
+template <typename R, int VM>
 struct Ell;
 template <>
 struct Ell<double, true> {
@@ -94,6 +94,12 @@ struct Ell<float, false> {
   static __device__ __forceinline__ float2 v(const EllC& e) { return make_float2(e.v[0], e.v[1]); }
 };
 
+// Value modes of a plan: complex entries; real entries (and a real diagonal);
+// real entries of groups that are either real or purely imaginary, with a
+// per-group flag for the factor i, and a complex diagonal ("phased": e.g. the
+// -i H and +i H parts of a Liouvillian beside its real dissipator).
+constexpr int kComplex = 0, kReal = 1, kPhased = 2;
+
 // Nonzero tests on the bit patterns (sign bit shifted out, so -0 counts as
 // zero, NaN as nonzero): integer instructions, where a floating-point compare
 // of a double would occupy the FP64 pipe that bounds the ComplexF64 kernels.
@@ -112,6 +118,12 @@ struct AccD {
     re = fma(v, x.x, re);
     im = fma(v, x.y, im);
   }
+  // (i v) x for real v: the sign goes into the FMA operand
+  __device__ void mac_i(double v, double2 x) {
+    re = fma(-v, x.y, re);
+    im = fma(v, x.x, im);
+  }
+  __device__ void mac_i(double2 v, double2 x) { mac(make_double2(-v.y, v.x), x); }
   __device__ void mac(double2 v, double2 x) {
     re = fma(v.x, x.x, re);
     re = fma(-v.y, x.y, re);
@@ -145,9 +157,11 @@ struct AccF {
     im = si;
   }
   __device__ void mac(float v, float2 x) { add(v * x.x, v * x.y); }
+  __device__ void mac_i(float v, float2 x) { add(-v * x.y, v * x.x); }
   __device__ void mac(float2 v, float2 x) {
     add(__fmaf_rn(v.x, x.x, -v.y * x.y), __fmaf_rn(v.x, x.y, v.y * x.x));
   }
+  __device__ void mac_i(float2 v, float2 x) { mac(make_float2(-v.y, v.x), x); }
   __device__ void set(float v, float2 x) {
     re = v * x.x;
     im = v * x.y;
@@ -307,16 +321,17 @@ __device__ __forceinline__ bool group_row(const GGroup& G, const SiteTable& st, 
 
 // acc[t] = (H x)[J] for the nt vectors starting at xb (element stride es,
 // vector stride xcs).
-template <typename R, bool REALV, bool SQUARE, bool W1, int TC>
+template <typename R, int VM, bool SQUARE, bool W1, int TC>
 __device__ __forceinline__ void accumulate(const GatherView& g, const SiteTable& st, const GGroup* sg,
-                                           const typename Ell<R, REALV>::T* ell, uint32_t J,
+                                           const typename Ell<R, VM != kComplex>::T* ell, uint32_t J,
                                            const typename Cx<R>::T* xb, int64_t es, int64_t xcs, int nt,
                                            typename AccOf<R>::T (&acc)[TC]) {
-  using VT = typename Val<R, REALV>::T;
-  using ET = typename Ell<R, REALV>::T;
+  using VT = typename Val<R, VM != kComplex>::T;  // stored entries
+  using DT = typename Val<R, VM == kReal>::T;     // merged diagonal
+  using ET = typename Ell<R, VM != kComplex>::T;
   using CT = typename Cx<R>::T;
   if (g.has_diag) {
-    const VT d = static_cast<const VT*>(g.diag)[J];
+    const DT d = static_cast<const DT*>(g.diag)[J];
     const CT* xp = xb + (int64_t)J * es;
 #pragma unroll
     for (int t = 0; t < TC; ++t)
@@ -334,12 +349,18 @@ __device__ __forceinline__ void accumulate(const GatherView& g, const SiteTable&
       const int4 f = fg[gi];
       const uint32_t r = (J >> f.x) & (uint32_t)f.y;
       const ET s = ell[f.z + r];
-      const VT v = Ell<R, REALV>::v(s);
+      const VT v = Ell<R, VM != kComplex>::v(s);
       const CT* xp = xb + ((int64_t)(J - (r << f.x)) + s.col) * es;
       if (nz(v)) {
+        if (VM == kPhased && f.w != 0) {
 #pragma unroll
-        for (int t = 0; t < TC; ++t)
-          if (t < nt) acc[t].mac(v, ld(xp + t * xcs));
+          for (int t = 0; t < TC; ++t)
+            if (t < nt) acc[t].mac_i(v, ld(xp + t * xcs));
+        } else {
+#pragma unroll
+          for (int t = 0; t < TC; ++t)
+            if (t < nt) acc[t].mac(v, ld(xp + t * xcs));
+        }
       }
     }
     return;
@@ -352,12 +373,18 @@ __device__ __forceinline__ void accumulate(const GatherView& g, const SiteTable&
       uint32_t r, sub;
       local_row(G, J, r, sub);
       const ET s = ell[G.ell_off + r];
-      const VT v = Ell<R, REALV>::v(s);
+      const VT v = Ell<R, VM != kComplex>::v(s);
       const CT* xp = xb + ((int64_t)(J - sub) + s.col) * es;
       if (nz(v)) {
+        if (VM == kPhased && G.imag != 0) {
 #pragma unroll
-        for (int t = 0; t < TC; ++t)
-          if (t < nt) acc[t].mac(v, ld(xp + t * xcs));
+          for (int t = 0; t < TC; ++t)
+            if (t < nt) acc[t].mac_i(v, ld(xp + t * xcs));
+        } else {
+#pragma unroll
+          for (int t = 0; t < TC; ++t)
+            if (t < nt) acc[t].mac(v, ld(xp + t * xcs));
+        }
       }
     }
     return;
@@ -368,16 +395,23 @@ __device__ __forceinline__ void accumulate(const GatherView& g, const SiteTable&
     uint32_t r;
     int64_t base;
     if (!group_row<SQUARE>(G, st, J, r, base)) continue;
+    const bool im = VM == kPhased && G.imag != 0;
     if (G.width > 0) {
       const ET* e = ell + G.ell_off + (int64_t)r * G.width;
       for (int k = 0; k < G.width; ++k) {
         const ET s = e[k];
-        const VT v = Ell<R, REALV>::v(s);
+        const VT v = Ell<R, VM != kComplex>::v(s);
         if (nz(v)) {
           const CT* xp = xb + (base + s.col) * es;
+          if (im) {
 #pragma unroll
-          for (int t = 0; t < TC; ++t)
-            if (t < nt) acc[t].mac(v, ld(xp + t * xcs));
+            for (int t = 0; t < TC; ++t)
+              if (t < nt) acc[t].mac_i(v, ld(xp + t * xcs));
+          } else {
+#pragma unroll
+            for (int t = 0; t < TC; ++t)
+              if (t < nt) acc[t].mac(v, ld(xp + t * xcs));
+          }
         }
       }
     } else {
@@ -386,9 +420,15 @@ __device__ __forceinline__ void accumulate(const GatherView& g, const SiteTable&
       for (int p = p0; p < p1; ++p) {
         const CT* xp = xb + (base + __ldg(g.coloff + p)) * es;
         const VT v = vals[p];
+        if (im) {
 #pragma unroll
-        for (int t = 0; t < TC; ++t)
-          if (t < nt) acc[t].mac(v, ld(xp + t * xcs));
+          for (int t = 0; t < TC; ++t)
+            if (t < nt) acc[t].mac_i(v, ld(xp + t * xcs));
+        } else {
+#pragma unroll
+          for (int t = 0; t < TC; ++t)
+            if (t < nt) acc[t].mac(v, ld(xp + t * xcs));
+        }
       }
     }
   }
@@ -396,14 +436,14 @@ __device__ __forceinline__ void accumulate(const GatherView& g, const SiteTable&
 
 // Output index J fastest across threads: one thread per (J, tile of TC vectors);
 // the vectors are contiguous (element stride 1).
-template <typename R, bool REALV, bool SQUARE, bool W1, int TC, int BMODE>
+template <typename R, int VM, bool SQUARE, bool W1, int TC, int BMODE>
 __global__ void __launch_bounds__(256) k_gather_j(GatherView g, SiteTable st,
                                                   const typename Cx<R>::T* __restrict__ x, int64_t xcs,
                                                   typename Cx<R>::T* __restrict__ y, int64_t ycs, int ncols,
                                                   typename Cx<R>::T alpha, typename Cx<R>::T beta) {
   using CT = typename Cx<R>::T;
   using AT = typename AccOf<R>::T;
-  using ET = typename Ell<R, REALV>::T;
+  using ET = typename Ell<R, VM != kComplex>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const ET* ell = stage<ET>(smem_raw, g);
   const GGroup* sg = reinterpret_cast<const GGroup*>(smem_raw);
@@ -414,7 +454,7 @@ __global__ void __launch_bounds__(256) k_gather_j(GatherView g, SiteTable st,
   const int nt = min(TC, ncols - c0);
   const CT* xb = x + (int64_t)c0 * xcs;
   AT acc[TC];
-  accumulate<R, REALV, SQUARE, W1, TC>(g, st, sg, ell, (uint32_t)J, xb, 1, xcs, nt, acc);
+  accumulate<R, VM, SQUARE, W1, TC>(g, st, sg, ell, (uint32_t)J, xb, 1, xcs, nt, acc);
   CT* yb = y + J + (int64_t)c0 * ycs;
 #pragma unroll
   for (int t = 0; t < TC; ++t)
@@ -428,14 +468,14 @@ __global__ void __launch_bounds__(256) k_gather_j(GatherView g, SiteTable st,
 // wave or less the hardware may place up to the occupancy limit on some SMs
 // and fewer on others; here the work per SM differs by at most one chunk per
 // block.
-template <typename R, bool REALV, bool SQUARE, bool W1, int TC, int BMODE>
+template <typename R, int VM, bool SQUARE, bool W1, int TC, int BMODE>
 __global__ void __launch_bounds__(256) k_gather_p(GatherView g, SiteTable st,
                                                   const typename Cx<R>::T* __restrict__ x, int64_t xcs,
                                                   typename Cx<R>::T* __restrict__ y, int64_t ycs, int ncols,
                                                   typename Cx<R>::T alpha, typename Cx<R>::T beta) {
   using CT = typename Cx<R>::T;
   using AT = typename AccOf<R>::T;
-  using ET = typename Ell<R, REALV>::T;
+  using ET = typename Ell<R, VM != kComplex>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const ET* ell = stage<ET>(smem_raw, g);
   const GGroup* sg = reinterpret_cast<const GGroup*>(smem_raw);
@@ -452,7 +492,7 @@ __global__ void __launch_bounds__(256) k_gather_p(GatherView g, SiteTable st,
     const int nt = min(TC, ncols - c0);
     const CT* xb = x + (int64_t)c0 * xcs;
     AT acc[TC];
-    accumulate<R, REALV, SQUARE, W1, TC>(g, st, sg, ell, (uint32_t)J, xb, 1, xcs, nt, acc);
+    accumulate<R, VM, SQUARE, W1, TC>(g, st, sg, ell, (uint32_t)J, xb, 1, xcs, nt, acc);
     CT* yb = y + J + (int64_t)c0 * ycs;
 #pragma unroll
     for (int t = 0; t < TC; ++t)
@@ -463,14 +503,14 @@ __global__ void __launch_bounds__(256) k_gather_p(GatherView g, SiteTable st,
 // Vectors with a stride between their elements (the rows of an operator
 // multiplied from the right, a strided bra): the vectors run across threads,
 // all threads of a block share one output index J.
-template <typename R, bool REALV, bool SQUARE, int BMODE>
+template <typename R, int VM, bool SQUARE, int BMODE>
 __global__ void __launch_bounds__(256) k_gather_c(GatherView g, SiteTable st,
                                                   const typename Cx<R>::T* __restrict__ x, int64_t xes,
                                                   int64_t xcs, typename Cx<R>::T* __restrict__ y,
                                                   int64_t yes, int64_t ycs, int ncols, typename Cx<R>::T alpha,
                                                   typename Cx<R>::T beta) {
   using AT = typename AccOf<R>::T;
-  using ET = typename Ell<R, REALV>::T;
+  using ET = typename Ell<R, VM != kComplex>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const ET* ell = stage<ET>(smem_raw, g);
   const GGroup* sg = reinterpret_cast<const GGroup*>(smem_raw);
@@ -478,7 +518,7 @@ __global__ void __launch_bounds__(256) k_gather_c(GatherView g, SiteTable st,
   const int64_t c = blockIdx.y * (int64_t)blockDim.x + threadIdx.x;
   if (c >= ncols) return;
   AT acc[1];
-  accumulate<R, REALV, SQUARE, false, 1>(g, st, sg, ell, (uint32_t)J, x + c * xcs, xes, xcs, 1, acc);
+  accumulate<R, VM, SQUARE, false, 1>(g, st, sg, ell, (uint32_t)J, x + c * xcs, xes, xcs, 1, acc);
   combine<BMODE>(y + J * yes + c * ycs, acc[0].total(), alpha, beta);
 }
 
@@ -498,13 +538,13 @@ void allow_smem(K kernel, size_t smem) {
     QOB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 }
 
-template <typename R, bool REALV, bool SQUARE, bool W1, int TC, int BMODE>
+template <typename R, int VM, bool SQUARE, bool W1, int TC, int BMODE>
 void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t xcs, void* y, int64_t ycs,
               int64_t ncols, typename Cx<R>::T a, typename Cx<R>::T b, size_t smem, cudaStream_t s) {
   using CT = typename Cx<R>::T;
   if (v.block < 0 && ncols <= (int64_t)INT32_MAX) {
     // persistent grid: SMs x resident blocks of -v.block threads
-    auto pk = k_gather_p<R, REALV, SQUARE, W1, TC, BMODE>;
+    auto pk = k_gather_p<R, VM, SQUARE, W1, TC, BMODE>;
     allow_smem(pk, smem);
     const int threads = -v.block;
     int dev = 0, sms = 0, occ = 0;
@@ -519,12 +559,15 @@ void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t x
       return;
     }
   }
-  auto kern = k_gather_j<R, REALV, SQUARE, W1, TC, BMODE>;
+  auto kern = k_gather_j<R, VM, SQUARE, W1, TC, BMODE>;
   allow_smem(kern, smem);
   const int threads = v.block > 0 ? v.block : kThreads;
   const unsigned gx = (unsigned)((v.m + threads - 1) / threads);
   GatherView w = v;
-  w.jmul = chunk_multiplier(gx);
+  // a few waves of blocks: permuted so every SM's share mixes the whole index
+  // range; many waves: in order (the hardware balances them, and neighbouring
+  // blocks share the gathered input in L2)
+  w.jmul = gx <= 4096 ? chunk_multiplier(gx) : 1;
   for (int64_t c0 = 0; c0 < ncols; c0 += (int64_t)65535 * TC) {  // grid.y limit
     const int64_t nc = std::min<int64_t>(ncols - c0, (int64_t)65535 * TC);
     kern<<<dim3(gx, (unsigned)((nc + TC - 1) / TC)), threads, smem, s>>>(
@@ -533,30 +576,30 @@ void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t x
   }
 }
 
-template <typename R, bool REALV, bool SQUARE, bool W1, int BMODE>
+template <typename R, int VM, bool SQUARE, bool W1, int BMODE>
 void launch_tc(const GatherView& v, const SiteTable& st, int tc, const void* x, int64_t xcs, void* y,
                int64_t ycs, int64_t ncols, typename Cx<R>::T a, typename Cx<R>::T b, size_t smem, cudaStream_t s) {
   switch (tc) {
     case 8:
-      launch_j<R, REALV, SQUARE, W1, 8, BMODE>(v, st, x, xcs, y, ycs, ncols, a, b, smem, s);
+      launch_j<R, VM, SQUARE, W1, 8, BMODE>(v, st, x, xcs, y, ycs, ncols, a, b, smem, s);
       break;
     case 4:
-      launch_j<R, REALV, SQUARE, W1, 4, BMODE>(v, st, x, xcs, y, ycs, ncols, a, b, smem, s);
+      launch_j<R, VM, SQUARE, W1, 4, BMODE>(v, st, x, xcs, y, ycs, ncols, a, b, smem, s);
       break;
     case 2:
-      launch_j<R, REALV, SQUARE, W1, 2, BMODE>(v, st, x, xcs, y, ycs, ncols, a, b, smem, s);
+      launch_j<R, VM, SQUARE, W1, 2, BMODE>(v, st, x, xcs, y, ycs, ncols, a, b, smem, s);
       break;
     default:
-      launch_j<R, REALV, SQUARE, W1, 1, BMODE>(v, st, x, xcs, y, ycs, ncols, a, b, smem, s);
+      launch_j<R, VM, SQUARE, W1, 1, BMODE>(v, st, x, xcs, y, ycs, ncols, a, b, smem, s);
   }
 }
 
-template <typename R, bool REALV, bool SQUARE, int BMODE>
+template <typename R, int VM, bool SQUARE, int BMODE>
 void dispatch_layout(const GatherView& v, const SiteTable& st, int tc, const void* x, int64_t xes,
                      int64_t xcs, void* y, int64_t yes, int64_t ycs, int64_t ncols, typename Cx<R>::T a, typename Cx<R>::T b,
                      cudaStream_t s) {
   using CT = typename Cx<R>::T;
-  using ET = typename Ell<R, REALV>::T;
+  using ET = typename Ell<R, VM != kComplex>::T;
   GatherView w = v;
   size_t smem = (size_t)v.ngroups * (sizeof(GGroup) + (v.fast ? sizeof(int4) : 0));
   const size_t ell_bytes = (size_t)v.ell_slots * sizeof(ET);
@@ -564,11 +607,11 @@ void dispatch_layout(const GatherView& v, const SiteTable& st, int tc, const voi
   if (w.ell_smem) smem += ell_bytes;
   if (xes == 1 && yes == 1) {
     if (SQUARE && v.all_w1)
-      launch_tc<R, REALV, SQUARE, true, BMODE>(w, st, tc, x, xcs, y, ycs, ncols, a, b, smem, s);
+      launch_tc<R, VM, SQUARE, true, BMODE>(w, st, tc, x, xcs, y, ycs, ncols, a, b, smem, s);
     else
-      launch_tc<R, REALV, SQUARE, false, BMODE>(w, st, tc, x, xcs, y, ycs, ncols, a, b, smem, s);
+      launch_tc<R, VM, SQUARE, false, BMODE>(w, st, tc, x, xcs, y, ycs, ncols, a, b, smem, s);
   } else {
-    auto kern = k_gather_c<R, REALV, SQUARE, BMODE>;
+    auto kern = k_gather_c<R, VM, SQUARE, BMODE>;
     allow_smem(kern, smem);
     const int threads = ncols >= 256 ? 256 : (int)((ncols + 31) / 32 * 32);
     for (int64_t c0 = 0; c0 < ncols; c0 += (int64_t)65535 * threads) {  // grid.y limit
@@ -581,7 +624,7 @@ void dispatch_layout(const GatherView& v, const SiteTable& st, int tc, const voi
   }
 }
 
-template <typename R, bool REALV, bool SQUARE>
+template <typename R, int VM, bool SQUARE>
 void dispatch_beta(const GatherView& v, const SiteTable& st, int tc, const void* x, int64_t xes, int64_t xcs,
                    void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta, cudaStream_t s) {
   typename Cx<R>::T a, b;
@@ -590,11 +633,11 @@ void dispatch_beta(const GatherView& v, const SiteTable& st, int tc, const void*
   b.x = (R)beta.re;
   b.y = (R)beta.im;
   if (beta.re == 0.0 && beta.im == 0.0)
-    dispatch_layout<R, REALV, SQUARE, 0>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, a, b, s);
+    dispatch_layout<R, VM, SQUARE, 0>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, a, b, s);
   else if (beta.im == 0.0)
-    dispatch_layout<R, REALV, SQUARE, 3>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, a, b, s);
+    dispatch_layout<R, VM, SQUARE, 3>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, a, b, s);
   else
-    dispatch_layout<R, REALV, SQUARE, 2>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, a, b, s);
+    dispatch_layout<R, VM, SQUARE, 2>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, a, b, s);
 }
 
 // One launch (or one column chunk per grid limit) of the fused gather in
@@ -604,14 +647,16 @@ void dispatch(const GatherView& v, const SiteTable& st, int tc, const void* x, i
               void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta, cudaStream_t s) {
   if (v.real_vals) {
     if (v.square)
-      dispatch_beta<R, true, true>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+      dispatch_beta<R, kReal, true>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
     else
-      dispatch_beta<R, true, false>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+      dispatch_beta<R, kReal, false>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+  } else if (v.phased) {  // phased plans have a merged diagonal, hence a square basis
+    dispatch_beta<R, kPhased, true>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
   } else {
     if (v.square)
-      dispatch_beta<R, false, true>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+      dispatch_beta<R, kComplex, true>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
     else
-      dispatch_beta<R, false, false>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
+      dispatch_beta<R, kComplex, false>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, beta, s);
   }
 }
 

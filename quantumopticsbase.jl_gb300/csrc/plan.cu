@@ -358,6 +358,7 @@ struct GatherHost {
   std::vector<uint8_t> live;  // current nonzero pattern of off-diagonal slots
   // where each slot's value is stored on the device (-1: not stored)
   std::vector<int32_t> dst_val, dst_ell, dst_diag;
+  std::vector<uint8_t> group_imag;  // phased plans: group stores imaginary parts
 };
 
 // ---------------------------------------------------------------------------
@@ -381,10 +382,11 @@ static std::vector<c128> eval_slots(const GatherHost& H, const std::vector<TermC
 
 // keep: off-diagonal slots stored even where their value is zero (a factor
 // table's union pattern); complex: store complex values even if all are real.
-static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c128>& val,
+static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c128>& val_in,
                              int precision, const std::vector<uint8_t>* keep = nullptr,
                              bool complex = false) {
   const bool square = H.S.square;
+  const std::vector<c128>& val = val_in;
   // live pattern of off-diagonal slots
   H.live.assign(H.slots.size(), 0);
   for (size_t s = 0; s < H.slots.size(); ++s)
@@ -398,6 +400,30 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
     if (val[s].im != 0.0) real = false;
   gp.real_vals = real;
   gp.td_ready = false;  // destinations change with the structure
+  // phased: every group's stored values either all real or all imaginary (the
+  // diagonal may be complex); the stored value is then one real number
+  H.group_imag.assign(H.groups.size(), 0);
+  bool phased = !real && !complex && square;
+  if (phased) {
+    std::vector<uint8_t> has_re(H.groups.size(), 0), has_im(H.groups.size(), 0);
+    for (size_t s = 0; s < H.slots.size(); ++s) {
+      if (H.slots[s].diag || !H.live[s]) continue;
+      if (val[s].re != 0.0) has_re[H.slots[s].group] = 1;
+      if (val[s].im != 0.0) has_im[H.slots[s].group] = 1;
+    }
+    for (size_t gi = 0; gi < H.groups.size() && phased; ++gi) {
+      if (has_re[gi] && has_im[gi]) phased = false;
+      H.group_imag[gi] = has_im[gi];
+    }
+    if (!phased) H.group_imag.assign(H.groups.size(), 0);
+  }
+  gp.phased = phased;
+  const bool store_real = real || phased;
+  // the stored number of each off-diagonal slot (phased: the imaginary part in imaginary groups)
+  auto stored = [&](size_t s) -> c128 {
+    if (phased && !H.slots[s].diag) return H.group_imag[H.slots[s].group] ? c128{val[s].im, 0.0} : c128{val[s].re, 0.0};
+    return val[s];
+  };
   // per group: live entries ordered by (r, coloff)
   std::vector<GGroup> descs;
   std::vector<int32_t> rowptr, coloff, pos_slot;
@@ -416,6 +442,7 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
     if (nlive > 0) {
       const GroupBuild& g = H.groups[gi];
       GGroup d = make_desc(g, H.S, (int32_t)rowptr.size());
+      d.imag = H.group_imag[gi];
       std::vector<int32_t> cnt(g.nrows + 1, 0);
       for (size_t s = s0; s < s1; ++s)
         if (H.live[s]) cnt[H.slots[s].r + 1]++;
@@ -427,7 +454,7 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
           H.dst_val[s] = (int32_t)vals.size();
           pos_slot.push_back((int32_t)s);
           coloff.push_back((int32_t)H.slots[s].coloff);
-          vals.push_back(val[s]);
+          vals.push_back(stored(s));
         }
       // rows with at most kMaxEllWidth entries also get fixed-width slots
       int32_t width = 0;
@@ -461,7 +488,7 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
   std::vector<int4> fastg;
   for (auto& d : descs) {
     if (!(d.pow2 && d.nblk == 1 && d.width == 1)) gp.fast = false;
-    fastg.push_back(make_int4((int)(d.shifts[0] & 0xffu), (int)(d.mod[0] - 1u), d.ell_off, 0));
+    fastg.push_back(make_int4((int)(d.shifts[0] & 0xffu), (int)(d.mod[0] - 1u), d.ell_off, d.imag));
   }
   if (gp.fast) upload_vec(gp.fastg, fastg);
   gp.square = square;
@@ -470,7 +497,7 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
   upload_vec(gp.coloff, coloff);
   // values in the plan precision, real or complex
   if (precision == QOB_C128) {
-    if (real) {
+    if (store_real) {
       std::vector<double> v(vals.size());
       for (size_t i = 0; i < vals.size(); ++i) v[i] = vals[i].re;
       upload_vec(gp.vals, v);
@@ -478,7 +505,7 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
       upload_vec(gp.vals, vals);
     }
   } else {
-    if (real) {
+    if (store_real) {
       std::vector<float> v(vals.size());
       for (size_t i = 0; i < vals.size(); ++i) v[i] = (float)vals[i].re;
       upload_vec(gp.vals, v);
@@ -491,7 +518,7 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
   // fixed-width slots in the plan precision
   gp.ell_slots = (int32_t)ell.size();
   if (precision == QOB_C128) {
-    if (real) {
+    if (store_real) {
       std::vector<EllD> e(ell.size());
       for (size_t i = 0; i < ell.size(); ++i) e[i] = {ell[i].col, 0, ell[i].v.re};
       upload_vec(gp.ell, e);
@@ -501,7 +528,7 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
       upload_vec(gp.ell, e);
     }
   } else {
-    if (real) {
+    if (store_real) {
       std::vector<EllF> e(ell.size());
       for (size_t i = 0; i < ell.size(); ++i) e[i] = {ell[i].col, (float)ell[i].v.re};
       upload_vec(gp.ell, e);
@@ -861,6 +888,7 @@ static void build_td_tables(GatherPlan& gp, const GatherHost& H, size_t nfactors
     d.dst_val = H.dst_val[s];
     d.dst_ell = H.dst_ell[s];
     d.dst_diag = H.dst_diag[s];
+    d.part = (gp.phased && !H.slots[s].diag && H.group_imag[H.slots[s].group]) ? 1 : 0;
     for (int64_t k = 0; k < H.slots[s].count; ++k) {
       const Contribution& c = H.contrib[H.slots[s].first + k];
       TdContrib t{};
@@ -899,6 +927,10 @@ static bool structure_holds(const GatherPlan& gp, const GatherHost& H, const std
   for (size_t s = 0; s < H.slots.size(); ++s) {
     if (gp.real_vals && val[s].im != 0.0) return false;
     if (!H.slots[s].diag && !H.live[s] && (val[s].re != 0.0 || val[s].im != 0.0)) return false;
+    if (gp.phased && !H.slots[s].diag) {
+      const bool im = H.group_imag[H.slots[s].group] != 0;
+      if (im ? val[s].re != 0.0 : val[s].im != 0.0) return false;
+    }
   }
   return true;
 }
@@ -964,6 +996,7 @@ GatherView GatherPlan::view() const {
   v.ngroups = ngroups;
   v.square = square ? 1 : 0;
   v.real_vals = real_vals ? 1 : 0;
+  v.phased = phased ? 1 : 0;
   v.has_diag = has_diag ? 1 : 0;
   v.groups = (const GGroup*)groups.p;
   v.rowptr = (const int32_t*)rowptr.p;

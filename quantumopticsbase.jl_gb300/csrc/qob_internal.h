@@ -103,6 +103,8 @@ struct GGroup {
   uint64_t mdiv[kMaxBlocks];  // Lemire magic numbers of div / mod
   uint64_t mmod[kMaxBlocks];
   uint32_t shifts[kMaxBlocks];  // log2 div | log2 mod << 8 | log2 lstride << 16
+  int32_t imag;  // phased plans: 1 when the group's stored (real) values stand for i times them
+  int32_t pad_[3];
 };
 
 // Fixed-width row slots: a row's entries padded with value 0 to the group's
@@ -128,7 +130,9 @@ struct EllC {  // FP32, complex value
   float v[2];
 };
 
-static_assert(sizeof(GGroup) % 8 == 0, "GGroup is copied to shared memory in 8-byte words");
+static_assert(sizeof(GGroup) % 16 == 0,
+              "GGroup is copied to shared memory in 8-byte words and the 16-byte items staged after the "
+              "descriptors (compact int4 records, ELL slots) must stay 16-byte aligned");
 
 // Per-subsystem data for bases whose left and right shapes differ.
 struct SiteTable {
@@ -160,7 +164,8 @@ struct GatherView {
   int32_t all_ell;   // 1: every group has fixed-width slots
   int32_t all_w1;    // 1: every group has exactly one slot per row
   int32_t fast;      // 1: fastg holds {log2 div, mod - 1, first slot, 0} per group
-  const int4* fastg; // compact form: one run of power-of-two subsystems, width 1
+  const int4* fastg; // compact form: one run of power-of-two subsystems, width 1 (w: the group's imag flag)
+  int32_t phased;    // 1: real stored values with per-group imag flags, complex diagonal
   int32_t block;     // threads per block of the index-lanes kernel (0: 256; < 0: persistent grid of -block)
   // Blocks of output indices (k_gather_j) or warp-sized chunks (k_gather_p) are visited in the
   // order c -> (c * jmul) mod count (jmul coprime to count, set per launch): consecutive blocks
@@ -190,7 +195,7 @@ struct TdSlot {
   int32_t dst_val;       // index into vals[] or -1
   int32_t dst_ell;       // ELL slot or -1
   int32_t dst_diag;      // index into the local diagonal tables or -1
-  int32_t pad;
+  int32_t part;          // phased plans: 1 stores the imaginary part in vals[] / ell[]
 };
 struct TdContrib {
   int32_t term;
@@ -227,6 +232,7 @@ struct GatherPlan {
   int64_t m = 0, n = 0;
   bool square = true;
   bool real_vals = true;
+  bool phased = false;  // real stored values, per-group imag flags, complex diagonal
   bool has_diag = false;
   int precision = QOB_C128;
   int ngroups = 0;
@@ -288,6 +294,9 @@ struct FftAxis {
   int64_t n = 0, stride = 1;
   bool pow2 = true;
   DeviceBuf tw, pre, post;  // plan precision: n/2 (power of two) or n twiddles; n phases each
+  // four-step split n = n1 * n2 for long power-of-two axes (0: none); all n twiddles
+  int64_t n1 = 0, n2 = 0;
+  DeviceBuf tw_full;
 };
 
 struct Plan {
@@ -350,9 +359,11 @@ void launch_build_diag(const GatherPlan& g, cudaStream_t s);
 void launch_td_values(const GatherPlan& g, const double2* factors_dev, cudaStream_t s);
 // One FFT pass along an axis of every vector: y = alpha * post .* DFT(pre .* x) + beta * y
 // (beta ignored when final == false: y is overwritten).
+// scratch (len * ncols elements, may be null) lets few long lines run as a
+// four-step FFT over many blocks.
 void launch_fft_pass(int precision, const FftAxis& ax, int64_t len, const void* x, int64_t xes, int64_t xcs,
                      void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta, bool final,
-                     cudaStream_t s);
+                     void* scratch, cudaStream_t s);
 std::unique_ptr<Plan> compile_fft(const NodeP& op, int side, int precision);
 int gather_tile(const GatherPlan& g, int64_t ncols);
 void launch_scale(int precision, void* y, int64_t rows, int64_t cols, int64_t ld_row,
