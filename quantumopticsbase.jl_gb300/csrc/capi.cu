@@ -53,6 +53,10 @@ Context::~Context() {
   if (reduce_host) cudaFreeHost(reduce_host);
   for (auto s : copy_stream)
     if (s) cudaStreamDestroy(s);
+  for (int k = 0; k < kPipeChunks; ++k) {
+    if (pipe_in[k]) cudaEventDestroy(pipe_in[k]);
+    if (pipe_done[k]) cudaEventDestroy(pipe_done[k]);
+  }
 }
 
 namespace {
@@ -586,39 +590,51 @@ int qob_mul_host(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, d
                  const void* x, int64_t x_rows, int64_t x_cols, double beta_re, double beta_im, void* y,
                  int64_t y_rows, int64_t y_cols) {
   const bool has_beta = beta_re != 0.0 || beta_im != 0.0;
-  // Several kets from the left: pipeline chunks of columns over two streams so
-  // the copies of one chunk overlap the kernels of the other.
+  // Several kets from the left: chunks of columns through a three-stream
+  // pipeline -- host-to-device copies back to back on one stream (the link is
+  // the bottleneck), each chunk's kernels on a second stream once its copy is
+  // in, its result copied back on a third -- so the copy engine for inputs
+  // never waits behind an output copy.
   if (side == QOB_LEFT && x_cols >= 8 && x_cols == y_cols) {
     return guard(ctx, [&] {
       if (!ctx || !op || !x || !y) fail(QOB_ERR_ARG, "null argument");
       check_dtype(dtype);
       if (x_rows != op->node->n || y_rows != op->node->m)
         fail(QOB_ERR_DIM, "A and B dimensions do not match. Can't do `A*B`");
+      Context& c = ctx->c;
       const size_t esz = dtype == QOB_C128 ? 16 : 8;
       const size_t xb = (size_t)x_rows * x_cols * esz, yb = (size_t)y_rows * y_cols * esz;
-      if (ctx->c.host_x.bytes < xb) ctx->c.host_x.alloc(xb);
-      if (ctx->c.host_y.bytes < yb) ctx->c.host_y.alloc(yb);
-      for (int k = 0; k < 2; ++k)
-        if (!ctx->c.copy_stream[k]) QOB_CUDA(cudaStreamCreateWithFlags(&ctx->c.copy_stream[k], cudaStreamNonBlocking));
-      Plan& P = get_plan(ctx->c, op, QOB_LEFT, dtype);
+      if (c.host_x.bytes < xb) c.host_x.alloc(xb);
+      if (c.host_y.bytes < yb) c.host_y.alloc(yb);
+      for (int k = 0; k < 3; ++k)
+        if (!c.copy_stream[k]) QOB_CUDA(cudaStreamCreateWithFlags(&c.copy_stream[k], cudaStreamNonBlocking));
+      for (int k = 0; k < Context::kPipeChunks; ++k) {
+        if (!c.pipe_in[k]) QOB_CUDA(cudaEventCreateWithFlags(&c.pipe_in[k], cudaEventDisableTiming));
+        if (!c.pipe_done[k]) QOB_CUDA(cudaEventCreateWithFlags(&c.pipe_done[k], cudaEventDisableTiming));
+      }
+      Plan& P = get_plan(c, op, QOB_LEFT, dtype);
+      cudaStream_t sin = c.copy_stream[0], scomp = c.copy_stream[1], sout = c.copy_stream[2];
       const int64_t nchunk = std::min<int64_t>(4, x_cols / 4);
       const int64_t per = (x_cols + nchunk - 1) / nchunk;
-      for (int64_t c0 = 0, k = 0; c0 < x_cols; c0 += per, ++k) {
+      int64_t k = 0;
+      for (int64_t c0 = 0; c0 < x_cols; c0 += per, ++k) {
         const int64_t nc = std::min(per, x_cols - c0);
-        cudaStream_t s = ctx->c.copy_stream[k % 2];
-        char* dx = static_cast<char*>(ctx->c.host_x.p) + (size_t)c0 * x_rows * esz;
-        char* dy = static_cast<char*>(ctx->c.host_y.p) + (size_t)c0 * y_rows * esz;
+        char* dx = static_cast<char*>(c.host_x.p) + (size_t)c0 * x_rows * esz;
+        char* dy = static_cast<char*>(c.host_y.p) + (size_t)c0 * y_rows * esz;
         const char* hx = static_cast<const char*>(x) + (size_t)c0 * x_rows * esz;
         char* hy = static_cast<char*>(y) + (size_t)c0 * y_rows * esz;
-        QOB_CUDA(cudaMemcpyAsync(dx, hx, (size_t)nc * x_rows * esz, cudaMemcpyHostToDevice, s));
-        if (has_beta) QOB_CUDA(cudaMemcpyAsync(dy, hy, (size_t)nc * y_rows * esz, cudaMemcpyHostToDevice, s));
-        // the two streams use workspace slots of their own
-        apply_plan(ctx->c, P, {alpha_re, alpha_im}, dx, 1, x_rows, {beta_re, beta_im}, dy, 1, y_rows, nc, s,
-                   24 + 8 * (int)(k % 2));
-        QOB_CUDA(cudaMemcpyAsync(hy, dy, (size_t)nc * y_rows * esz, cudaMemcpyDeviceToHost, s));
+        QOB_CUDA(cudaMemcpyAsync(dx, hx, (size_t)nc * x_rows * esz, cudaMemcpyHostToDevice, sin));
+        if (has_beta) QOB_CUDA(cudaMemcpyAsync(dy, hy, (size_t)nc * y_rows * esz, cudaMemcpyHostToDevice, sin));
+        QOB_CUDA(cudaEventRecord(c.pipe_in[k], sin));
+        QOB_CUDA(cudaStreamWaitEvent(scomp, c.pipe_in[k], 0));
+        apply_plan(c, P, {alpha_re, alpha_im}, dx, 1, x_rows, {beta_re, beta_im}, dy, 1, y_rows, nc, scomp, 24);
+        QOB_CUDA(cudaEventRecord(c.pipe_done[k], scomp));
+        QOB_CUDA(cudaStreamWaitEvent(sout, c.pipe_done[k], 0));
+        QOB_CUDA(cudaMemcpyAsync(hy, dy, (size_t)nc * y_rows * esz, cudaMemcpyDeviceToHost, sout));
       }
-      QOB_CUDA(cudaStreamSynchronize(ctx->c.copy_stream[0]));
-      QOB_CUDA(cudaStreamSynchronize(ctx->c.copy_stream[1]));
+      QOB_CUDA(cudaStreamSynchronize(sout));
+      QOB_CUDA(cudaStreamSynchronize(scomp));
+      QOB_CUDA(cudaStreamSynchronize(sin));
     });
   }
   int rc = guard(ctx, [&] {

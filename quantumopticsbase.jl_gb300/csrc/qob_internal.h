@@ -336,7 +336,11 @@ struct Context {
   DeviceBuf reduce_buf;
   void* reduce_host = nullptr;  // pinned
   DeviceBuf host_x, host_y;     // staging for qob_mul_host
-  cudaStream_t copy_stream[2] = {nullptr, nullptr};  // qob_mul_host's copy/compute pipeline
+  // qob_mul_host's pipeline: copies in, kernels, copies out on three streams,
+  // linked per chunk by events
+  cudaStream_t copy_stream[3] = {nullptr, nullptr, nullptr};
+  static constexpr int kPipeChunks = 8;
+  cudaEvent_t pipe_in[kPipeChunks] = {}, pipe_done[kPipeChunks] = {};
   ~Context();
 };
 
