@@ -290,6 +290,27 @@ def run_own(args, rank, world, local_rank):
             lib.qob_graph_free(ctx.ptr, graph)
         return ms, launches, (t_host0, t_host1), (xs, ys)
 
+    def step_stats(tdt, code, n=200):
+        """Per-step device times (CUDA events around each single application):
+        cold -- the batches rotate (inputs beyond L2); warm -- one batch again and again."""
+        xs, ys = batches(tdt)
+        argl = [mul_args(xs[b], ys[b], code) for b in range(ROTATE)]
+        out = {}
+        for name, pick in (("cold", lambda i: argl[i % ROTATE]), ("warm", lambda i: argl[0])):
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+            with torch.cuda.stream(stream):
+                for i in range(5):
+                    raise_for(lib.qob_mul(*pick(i)), ctx)
+                for i in range(n):
+                    evs[i][0].record(stream)
+                    raise_for(lib.qob_mul(*pick(i)), ctx)
+                    evs[i][1].record(stream)
+            stream.synchronize()
+            t = sorted(a.elapsed_time(b) for a, b in evs)
+            out[name + "_median_ms"] = t[n // 2]
+            out[name + "_p99_ms"] = t[min(n - 1, int(0.99 * n))]
+        return out
+
     def tune(dt):
         times = (C.c_double * 12)()
         chosen = C.c_int()
@@ -303,6 +324,7 @@ def run_own(args, rank, world, local_rank):
     tuning = {"c128": tune(np.complex128), "c64": tune(np.complex64)}
     K, W = args.steps, max(3, args.warmup)
     ms64, launches64, win64, _ = timed(torch.complex128, dtype_code(np.complex128), K, W)
+    stats64 = step_stats(torch.complex128, dtype_code(np.complex128))
     value = BATCH * K * world / (ms64 / 1e3)
 
     # ComplexF32 mode on the same workload, error against the oracle on one ket
@@ -344,6 +366,8 @@ def run_own(args, rank, world, local_rank):
                      "ncu_kernel": prof.get("kernel"),
                      "binding": "fp64 FMA throughput (GB300 FP64 ~1.25 TFLOP/s), see fp64_compute"},
         "fp64_compute": fp64,
+        "step_ms": dict(stats64, note="200 single applications timed one by one with CUDA events: cold = "
+                                      "rotating batches (inputs from HBM), warm = one batch repeated (L2-resident)"),
         "plan": plan,
         "tuning": tuning,
         "gpu_launches": launches64,

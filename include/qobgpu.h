@@ -235,6 +235,11 @@ int qob_batch_create(qob_ctx* ctx, int dtype, qob_batch** out);
 int qob_batch_add(qob_ctx* ctx, qob_batch* batch, qob_op* op, double alpha_re, double alpha_im,
                   const void* x, void* y, double beta_re, double beta_im);
 int qob_batch_run(qob_ctx* ctx, qob_batch* batch, void* stream);
+/* One-shot batched application (creates, runs and frees a batch):
+ * y_i = alpha_i op_i x_i + beta_i y_i for i < n on device kets of `dtype`;
+ * alphas / betas: n interleaved complex doubles each.  Synchronous on stream. */
+int qob_apply_batched(qob_ctx* ctx, int dtype, int n, qob_op* const* ops, const void* const* xs,
+                      void* const* ys, const double* alphas, const double* betas, void* stream);
 /* Time tile lengths 128 / 256 / 512 / 1024 (times_ms[0..3]) and keep the
  * fastest; runs the batch 28 times, so the outputs are overwritten. */
 int qob_batch_tune(qob_ctx* ctx, qob_batch* batch, double* times_ms, int* chosen);
@@ -242,6 +247,20 @@ int qob_batch_tune(qob_ctx* ctx, qob_batch* batch, double* times_ms, int* chosen
  * [4] blocks of the persistent grid. */
 int qob_batch_info(qob_ctx* ctx, qob_batch* batch, int64_t* info);
 int qob_batch_free(qob_ctx* ctx, qob_batch* batch);
+
+/* ---------------------------------------------------------------------------
+ * Device states for callers that do not manage device memory themselves
+ * (the reference's arrays are Julia-owned; a C caller can use these instead of
+ * CUDA calls of its own).  A state holds dim x ncols complex values of dtype,
+ * column-major, zero-initialised; uploads and downloads are synchronous on
+ * `stream`.
+ * ------------------------------------------------------------------------- */
+int qob_state_alloc(qob_ctx* ctx, int dtype, int64_t dim, int64_t ncols, void** state);
+int qob_state_free(qob_ctx* ctx, void* state);
+int qob_state_upload(qob_ctx* ctx, int dtype, void* state, const void* host, int64_t dim, int64_t ncols,
+                     void* stream);
+int qob_state_download(qob_ctx* ctx, int dtype, const void* state, void* host, int64_t dim, int64_t ncols,
+                       void* stream);
 
 /* ---------------------------------------------------------------------------
  * Expectation values on product states (LazyKet, src/states_lazyket.jl:64-125).

@@ -297,3 +297,29 @@ int qob_batch_free(qob_ctx* ctx, qob_batch* b) {
 }
 
 }  // extern "C"
+
+// One-shot form of the batch API: n applications y_i = alpha_i op_i x_i + beta_i y_i
+// (kets, device memory) in one fused launch where the plans allow.  The batch's
+// tables are built and freed inside the call; synchronous on `stream`.
+extern "C" int qob_apply_batched(qob_ctx* ctx, int dtype, int n, qob_op* const* ops, const void* const* xs,
+                                 void* const* ys, const double* alphas, const double* betas, void* stream) {
+  if (!ctx) return QOB_ERR_ARG;
+  if (n < 0 || (n > 0 && (!ops || !xs || !ys || !alphas || !betas))) {
+    ctx->c.err = "qob_apply_batched: bad arguments";
+    return QOB_ERR_ARG;
+  }
+  qob_batch* b = nullptr;
+  int rc = qob_batch_create(ctx, dtype, &b);
+  for (int i = 0; rc == QOB_OK && i < n; ++i)
+    rc = qob_batch_add(ctx, b, ops[i], alphas[2 * i], alphas[2 * i + 1], xs[i], ys[i], betas[2 * i], betas[2 * i + 1]);
+  if (rc == QOB_OK && n > 0) rc = qob_batch_run(ctx, b, stream);
+  if (rc == QOB_OK) {
+    const cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) {
+      ctx->c.err = cudaGetErrorString(e);
+      rc = QOB_ERR_CUDA;
+    }
+  }
+  if (b) qob_batch_free(ctx, b);
+  return rc;
+}

@@ -736,3 +736,57 @@ int qob_expect(qob_ctx* ctx, qob_op* op, int dtype, const void* psi, int64_t n, 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// device states for callers without their own device memory management: a
+// state is dim x ncols complex values of one dtype, column-major
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int qob_state_alloc(qob_ctx* ctx, int dtype, int64_t dim, int64_t ncols, void** out) {
+  return guard(ctx, [&] {
+    if (!ctx || !out || dim < 0 || ncols < 0) fail(QOB_ERR_ARG, "qob_state_alloc: bad arguments");
+    check_dtype(dtype);
+    QOB_CUDA(cudaSetDevice(ctx->c.device));
+    const size_t bytes = std::max<size_t>((size_t)dim * ncols * (dtype == QOB_C128 ? 16 : 8), 16);
+    void* p = nullptr;
+    const cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      fail(QOB_ERR_OOM, "qob_state_alloc: out of device memory");
+    }
+    QOB_CUDA(e);
+    QOB_CUDA(cudaMemset(p, 0, bytes));
+    *out = p;
+  });
+}
+
+int qob_state_free(qob_ctx* ctx, void* state) {
+  return guard(ctx, [&] {
+    if (state) QOB_CUDA(cudaFree(state));
+  });
+}
+
+int qob_state_upload(qob_ctx* ctx, int dtype, void* state, const void* host, int64_t dim, int64_t ncols,
+                     void* stream) {
+  return guard(ctx, [&] {
+    if (!ctx || !state || (!host && dim * ncols > 0)) fail(QOB_ERR_ARG, "qob_state_upload: bad arguments");
+    check_dtype(dtype);
+    const size_t bytes = (size_t)dim * ncols * (dtype == QOB_C128 ? 16 : 8);
+    QOB_CUDA(cudaMemcpyAsync(state, host, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    QOB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  });
+}
+
+int qob_state_download(qob_ctx* ctx, int dtype, const void* state, void* host, int64_t dim, int64_t ncols,
+                       void* stream) {
+  return guard(ctx, [&] {
+    if (!ctx || !state || (!host && dim * ncols > 0)) fail(QOB_ERR_ARG, "qob_state_download: bad arguments");
+    check_dtype(dtype);
+    const size_t bytes = (size_t)dim * ncols * (dtype == QOB_C128 ? 16 : 8);
+    QOB_CUDA(cudaMemcpyAsync(host, state, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    QOB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  });
+}
+
+}  // extern "C"

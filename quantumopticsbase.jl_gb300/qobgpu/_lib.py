@@ -64,6 +64,11 @@ SIGNATURES = {
     "qob_batch_info": (I, [VP, VP, I64P]),
     "qob_batch_free": (I, [VP, VP]),
     "qob_rk4": (I, [VP, VP, I, VP, I64, D, I, I, VP]),
+    "qob_apply_batched": (I, [VP, I, I, C.POINTER(VP), C.POINTER(VP), C.POINTER(VP), DP, DP, VP]),
+    "qob_state_alloc": (I, [VP, I, I64, I64, C.POINTER(VP)]),
+    "qob_state_free": (I, [VP, VP]),
+    "qob_state_upload": (I, [VP, I, VP, VP, I64, I64, VP]),
+    "qob_state_download": (I, [VP, I, VP, VP, I64, I64, VP]),
     "qob_op_fft": (I, [VP, I, I64P, I, I64P, C.POINTER(C.c_int), DP, DP, C.POINTER(VP)]),
     "qob_expect_lazyket": (I, [VP, VP, I, I, I64P, VP, I64, VP, VP]),
     "qob_rk4_td": (I, [VP, VP, I, VP, I64, D, I, VP, I64, I, VP]),
