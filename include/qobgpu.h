@@ -307,12 +307,13 @@ int qob_rk4_td(qob_ctx* ctx, qob_op* H, int dtype, void* psi, int64_t n, double 
  * dpsi/dt = -i H psi.  States and operators stay resident on the device; a
  * queued request is admitted when fewer than max_active run and its device
  * memory (4 state vectors) fits both mem_budget and the free device memory;
- * requests larger than mem_budget are rejected (status -QOB_ERR_OOM).  Each
- * engine iteration advances every active request by one step in eight batched
- * launches, so requests that arrive while others run join at the next
- * iteration.  A request's result does not depend on the others in flight.
- * Either run the engine on its own thread (qob_server_start / _stop) or drive
- * it with qob_server_step.
+ * requests larger than mem_budget are rejected (status -QOB_ERR_OOM).  A step
+ * of every active request is eight batched launches, recorded once per set of
+ * active requests into a CUDA graph and replayed; an engine iteration on the
+ * worker thread (qob_server_start / _stop) runs up to 16 steps (4 while
+ * requests wait, never past a request's last step), qob_server_step runs one.
+ * Requests that arrive while others run join at the next iteration.  A
+ * request's result does not depend on the others in flight.
  * status: 0 queued, 1 running, 2 done, < 0 failed (-error code).
  * times[0..2]: submit, admit and completion time (seconds, steady clock).
  * stats[0..7]: queued, active, completed, rejected, request-steps, engine

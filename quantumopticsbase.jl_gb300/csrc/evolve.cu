@@ -18,9 +18,12 @@
 //
 // The server (qob_server_*) keeps states and operators resident on the
 // device, admits queued requests when a slot and device memory (its own
-// budget and cudaMemGetInfo) allow, advances every active request by one RK4
-// step per engine iteration, and retires finished ones with their latency
-// record.  Requests that arrive while others run join at the next iteration.
+// budget and cudaMemGetInfo) allow, advances every active request by RK4
+// steps -- replayed from a CUDA graph of one step of the current ensemble,
+// up to 16 per iteration on the worker thread (4 while requests wait, never
+// past a request's last step), one per qob_server_step -- and retires finished
+// ones with their latency record.  Requests that arrive while others run join
+// at the next iteration.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -280,6 +283,10 @@ struct qob_server {
   cudaStream_t stream = nullptr;
   qob::Ensemble ens;
   bool dirty = true;
+  // one RK4 step of the current ensemble as a CUDA graph: recorded on the
+  // second iteration after a rebuild (the first sizes every buffer), replayed after
+  int graph_state = 0;  // 0: next step runs directly, 1: next step is recorded, 2: replay
+  cudaGraphExec_t graph = nullptr;
   std::thread worker;
   bool stop = false;
   bool running = false;
@@ -313,14 +320,52 @@ void admit(qob_server* S) {
   }
 }
 
-// One engine iteration: admit, one RK4 step of every active request, retire.
-// Returns the number of active requests after the step.
-int iterate(qob_server* S) {
+void drop_graph(qob_server* S) {
+  if (S->graph) cudaGraphExecDestroy(S->graph);
+  S->graph = nullptr;
+  S->graph_state = 0;
+}
+
+// One RK4 step of the ensemble: directly, recorded into a graph, or replayed.
+void run_step(qob_server* S) {
+  qob::Context& ctx = S->ctx->c;
+  if (S->graph_state == 2) {
+    QOB_CUDA(cudaGraphLaunch(S->graph, S->stream));
+    return;
+  }
+  if (S->graph_state == 0) {
+    qob::ensemble_step(ctx, S->ens, S->stream);
+    S->graph_state = 1;
+    return;
+  }
+  cudaGraph_t g = nullptr;
+  QOB_CUDA(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal));
+  try {
+    qob::ensemble_step(ctx, S->ens, S->stream);
+  } catch (...) {
+    cudaStreamEndCapture(S->stream, &g);
+    if (g) cudaGraphDestroy(g);
+    throw;
+  }
+  QOB_CUDA(cudaStreamEndCapture(S->stream, &g));
+  const cudaError_t e = cudaGraphInstantiate(&S->graph, g, 0);
+  cudaGraphDestroy(g);
+  QOB_CUDA(e);
+  S->graph_state = 2;
+  QOB_CUDA(cudaGraphLaunch(S->graph, S->stream));
+}
+
+// One engine iteration: admit, up to max_steps RK4 steps of every active
+// request (never past a request's last step), retire.  Returns the number of
+// active requests after the iteration.
+int iterate(qob_server* S, int max_steps) {
   std::vector<Request*> act;
+  bool waiting = false;
   {
     std::lock_guard<std::mutex> lk(S->mu);
     admit(S);
     act = S->active;
+    waiting = !S->queue.empty();
   }
   if (act.empty()) return 0;
   qob::Context& ctx = S->ctx->c;
@@ -332,16 +377,20 @@ int iterate(qob_server* S) {
       states.push_back({r->plan, base, base + sz, base + 2 * sz, base + 3 * sz, r->n, r->dt});
     }
     S->ens.renormalise = S->renormalise;
+    drop_graph(S);
     qob::ensemble_build(ctx, S->ens, states, S->dtype);
     S->dirty = false;
   }
-  qob::ensemble_step(ctx, S->ens, S->stream);
+  int k = waiting ? std::min(max_steps, 4) : max_steps;  // queued requests join soon
+  for (Request* r : act) k = std::min(k, r->nsteps - r->step);
+  k = std::max(k, 1);
+  for (int i = 0; i < k; ++i) run_step(S);
   QOB_CUDA(cudaStreamSynchronize(S->stream));
   S->iterations++;
   std::vector<Request*> finished;
   for (Request* r : act) {
-    r->step++;
-    S->steps_run++;
+    r->step += k;
+    S->steps_run += k;
     if (r->step >= r->nsteps) finished.push_back(r);
   }
   for (Request* r : finished) {
@@ -381,7 +430,7 @@ void worker_loop(qob_server* S) {
     int code = 0;
     std::string msg;
     try {
-      iterate(S);
+      iterate(S, 16);
     } catch (const qob::Error& e) {
       code = e.code;
       msg = e.msg;
@@ -474,7 +523,7 @@ int qob_server_submit(qob_server* S, qob_op* H, const void* psi0, int64_t n, int
 int qob_server_step(qob_server* S, int* nactive) {
   return sguard(S, [&] {
     if (S->running) qob::fail(QOB_ERR_STATE, "the server's worker thread is running");
-    const int a = iterate(S);
+    const int a = iterate(S, 1);
     if (nactive) *nactive = a;
   });
 }
@@ -549,6 +598,7 @@ int qob_server_destroy(qob_server* S) {
   cudaSetDevice(S->ctx->c.device);
   for (Request* r : S->active)
     if (r->dev) cudaFreeAsync(r->dev, S->stream);
+  drop_graph(S);
   if (S->stream) {
     cudaStreamSynchronize(S->stream);
     cudaStreamDestroy(S->stream);
