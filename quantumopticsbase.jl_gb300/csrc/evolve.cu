@@ -621,8 +621,49 @@ int qob_rk4(qob_ctx* ctx, qob_op* H, int dtype, void* psi, int64_t n, double dt,
     qob::Ensemble E;
     E.renormalise = renormalise != 0;
     qob::ensemble_build(ctx->c, E, {qob::EvolveState{&P, psi, w, w + sz, w + 2 * sz, n, dt}}, dtype);
-    for (int s = 0; s < nsteps; ++s) qob::ensemble_step(ctx->c, E, (cudaStream_t)stream);
-    QOB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    cudaStream_t st = (cudaStream_t)stream;
+    // the first step runs directly (it sizes every buffer); the rest replay a
+    // CUDA graph of one step on the context's own stream (the call is
+    // synchronous, so the caller's stream is drained first)
+    int s = 0;
+    if (nsteps > 0) {
+      qob::ensemble_step(ctx->c, E, st);
+      s = 1;
+    }
+    if (nsteps - s >= 4) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      QOB_CUDA(cudaStreamIsCapturing(st, &cs));
+      if (cs == cudaStreamCaptureStatusNone) {
+        QOB_CUDA(cudaStreamSynchronize(st));
+        if (!ctx->c.copy_stream[1]) QOB_CUDA(cudaStreamCreateWithFlags(&ctx->c.copy_stream[1], cudaStreamNonBlocking));
+        st = ctx->c.copy_stream[1];
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        QOB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        try {
+          qob::ensemble_step(ctx->c, E, st);
+        } catch (...) {
+          cudaStreamEndCapture(st, &g);
+          if (g) cudaGraphDestroy(g);
+          throw;
+        }
+        QOB_CUDA(cudaStreamEndCapture(st, &g));
+        const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        QOB_CUDA(e);
+        for (; s < nsteps; ++s) {
+          const cudaError_t le = cudaGraphLaunch(ge, st);
+          if (le != cudaSuccess) {
+            cudaGraphExecDestroy(ge);
+            QOB_CUDA(le);
+          }
+        }
+        QOB_CUDA(cudaStreamSynchronize(st));
+        cudaGraphExecDestroy(ge);
+      }
+    }
+    for (; s < nsteps; ++s) qob::ensemble_step(ctx->c, E, st);
+    QOB_CUDA(cudaStreamSynchronize(st));
     return QOB_OK;
   } catch (const qob::Error& e) {
     ctx->c.err = e.msg;
