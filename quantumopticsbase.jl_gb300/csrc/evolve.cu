@@ -674,7 +674,8 @@ int qob_rk4(qob_ctx* ctx, qob_op* H, int dtype, void* psi, int64_t n, double dt,
 // RK4 with time-dependent LazySum factors: row r of `factors` holds the factors
 // at t0 + r*dt/2.  Stage 1 of step s uses row 2s, stages 2 and 3 row 2s+1,
 // stage 4 row 2s+2; the values are re-evaluated on the device before each
-// stage whose row differs from the previous one.
+// stage whose row differs from the previous one, from a device-side step
+// counter, so steps after the first replay one recorded CUDA graph.
 int qob_rk4_td(qob_ctx* ctx, qob_op* H, int dtype, void* psi, int64_t n, double dt, int nsteps,
                const double* factors, int64_t nrows, int renormalise, void* stream) {
   if (!ctx) return QOB_ERR_ARG;
@@ -701,16 +702,63 @@ int qob_rk4_td(qob_ctx* ctx, qob_op* H, int dtype, void* psi, int64_t n, double 
     qob::Ensemble E;
     E.renormalise = renormalise != 0;
     qob::ensemble_build(ctx->c, E, {qob::EvolveState{&P, psi, w, w + sz, w + 2 * sz, n, dt}}, dtype);
-    int step = 0;
+    // the step counter lives on the device, so a recorded step reads the rows
+    // of the step it runs in: stage 2 row 2s+1, stage 4 row 2s+2 (stage 1
+    // keeps row 2s from the previous step's stage 4; step 0 refreshes it)
+    qob::DeviceBuf stepbuf;
+    const long long zero = 0;
+    stepbuf.upload(&zero, sizeof(zero));
+    long long* dstep = static_cast<long long*>(stepbuf.p);
+    bool first = true;
     std::function<void(int)> hook = [&](int mode) {
       if (!P.gather) return;
-      int64_t row = -1;
-      if (mode == 1 && step == 0) row = 0;
-      if (mode == 2) row = 2 * (int64_t)step + 1;
-      if (mode == 4) row = 2 * (int64_t)step + 2;
-      if (row >= 0) qob::device_refresh(*P.gather, rows + row * nf, st);
+      if (mode == 1 && first) qob::device_refresh(*P.gather, rows, st, dstep, 0, (long long)nf);
+      if (mode == 2) qob::device_refresh(*P.gather, rows, st, dstep, 1, (long long)nf);
+      if (mode == 4) qob::device_refresh(*P.gather, rows, st, dstep, 2, (long long)nf);
     };
-    for (step = 0; step < nsteps; ++step) qob::ensemble_step(ctx->c, E, st, &hook);
+    auto one_step = [&](cudaStream_t s2) {
+      qob::ensemble_step(ctx->c, E, s2, &hook);
+      qob::launch_td_advance(dstep, s2);
+    };
+    int s = 0;
+    if (nsteps > 0) {
+      one_step(st);
+      first = false;
+      s = 1;
+    }
+    if (nsteps - s >= 4) {  // the rest: replays of a recorded step on the context's stream
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      QOB_CUDA(cudaStreamIsCapturing(st, &cs));
+      if (cs == cudaStreamCaptureStatusNone) {
+        QOB_CUDA(cudaStreamSynchronize(st));
+        if (!ctx->c.copy_stream[1]) QOB_CUDA(cudaStreamCreateWithFlags(&ctx->c.copy_stream[1], cudaStreamNonBlocking));
+        st = ctx->c.copy_stream[1];
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        QOB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        try {
+          one_step(st);
+        } catch (...) {
+          cudaStreamEndCapture(st, &g);
+          if (g) cudaGraphDestroy(g);
+          throw;
+        }
+        QOB_CUDA(cudaStreamEndCapture(st, &g));
+        const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        QOB_CUDA(e);
+        for (; s < nsteps; ++s) {
+          const cudaError_t le = cudaGraphLaunch(ge, st);
+          if (le != cudaSuccess) {
+            cudaGraphExecDestroy(ge);
+            QOB_CUDA(le);
+          }
+        }
+        QOB_CUDA(cudaStreamSynchronize(st));
+        cudaGraphExecDestroy(ge);
+      }
+    }
+    for (; s < nsteps; ++s) one_step(st);
     QOB_CUDA(cudaStreamSynchronize(st));
     // the values now belong to the last row: the next use re-evaluates them
     // from the operator's own factors

@@ -48,14 +48,20 @@ __global__ void k_build_diag(int64_t m, int ndg, const GGroup* __restrict__ dg,
 // Stored values re-evaluated from the root LazySum's factors: one thread per
 // merged slot, value = sum over its contributions of (f[top] * inner) * pv,
 // summed in the order of the host record (the order of the LazySum's terms).
+// The factor row is f_base + (2 * *step + off) * nf when `step` (a device
+// counter of RK4 steps) is given, else f_base: recorded graphs read the row of
+// the current step.
 template <typename R, bool REALV>
 __global__ void __launch_bounds__(256) k_td_values(int nslots, const TdSlot* __restrict__ slots,
                                                    const TdContrib* __restrict__ contrib,
                                                    const TdTerm* __restrict__ terms,
-                                                   const double2* __restrict__ f, void* vals, void* ell,
+                                                   const double2* __restrict__ f_base,
+                                                   const long long* __restrict__ step, long long off,
+                                                   long long nf, void* vals, void* ell,
                                                    double2* __restrict__ dtab) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nslots) return;
+  const double2* f = step ? f_base + (2 * *step + off) * nf : f_base;
   const TdSlot sl = slots[s];
   double re = 0.0, im = 0.0;
   for (int k = 0; k < sl.count; ++k) {
@@ -101,9 +107,18 @@ __global__ void __launch_bounds__(256) k_td_values(int nslots, const TdSlot* __r
   }
 }
 
+// Next RK4 step of a recorded time-dependent step graph.
+__global__ void k_td_advance(long long* step) { *step += 1; }
+
 }  // namespace
 
-void launch_td_values(const GatherPlan& g, const double2* factors_dev, cudaStream_t s) {
+void launch_td_advance(long long* step, cudaStream_t s) {
+  k_td_advance<<<1, 1, 0, s>>>(step);
+  QOB_LAUNCHED();
+}
+
+void launch_td_values(const GatherPlan& g, const double2* factors_dev, cudaStream_t s, const long long* step,
+                      long long off, long long nf) {
   if (g.td_nslots == 0) return;
   const int threads = 256;
   const unsigned blocks = (unsigned)((g.td_nslots + threads - 1) / threads);
@@ -114,14 +129,14 @@ void launch_td_values(const GatherPlan& g, const double2* factors_dev, cudaStrea
   const bool store_real = g.real_vals || g.phased;
   if (g.precision == QOB_C128) {
     if (store_real)
-      k_td_values<double, true><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, g.vals.p, g.ell.p, dt);
+      k_td_values<double, true><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, step, off, nf, g.vals.p, g.ell.p, dt);
     else
-      k_td_values<double, false><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, g.vals.p, g.ell.p, dt);
+      k_td_values<double, false><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, step, off, nf, g.vals.p, g.ell.p, dt);
   } else {
     if (store_real)
-      k_td_values<float, true><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, g.vals.p, g.ell.p, dt);
+      k_td_values<float, true><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, step, off, nf, g.vals.p, g.ell.p, dt);
     else
-      k_td_values<float, false><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, g.vals.p, g.ell.p, dt);
+      k_td_values<float, false><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, step, off, nf, g.vals.p, g.ell.p, dt);
   }
   QOB_LAUNCHED();
 }

@@ -915,9 +915,10 @@ static void build_td_tables(GatherPlan& gp, const GatherHost& H, size_t nfactors
   gp.td_ready = true;
 }
 
-void device_refresh(GatherPlan& g, const double2* factors_dev, cudaStream_t s) {
+void device_refresh(GatherPlan& g, const double2* factors_dev, cudaStream_t s, const long long* step,
+                    long long off, long long nf) {
   if (!g.td_ready) fail(QOB_ERR_STATE, "device refresh without its tables");
-  launch_td_values(g, factors_dev, s);
+  launch_td_values(g, factors_dev, s, step, off, nf);
   if (g.has_diag) launch_build_diag(g, s);
 }
 

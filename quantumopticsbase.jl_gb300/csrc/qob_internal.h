@@ -353,14 +353,19 @@ bool plan_is_current(const Plan& plan);
 void prepare_factor_rows(Plan& plan, const OpNode& root, const double* rows, int64_t nrows);
 // Re-evaluate the gather values on the device from factors in device memory
 // (nfactors complex values) and rebuild the merged diagonal, on stream s.
-void device_refresh(GatherPlan& g, const double2* factors_dev, cudaStream_t s);
+void device_refresh(GatherPlan& g, const double2* factors_dev, cudaStream_t s, const long long* step = nullptr,
+                    long long off = 0, long long nf = 0);
 
 // kernels (launchers)
 void launch_gather(const GatherPlan& g, int precision, const void* x, int64_t xes, int64_t xcs,
                    void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta,
                    cudaStream_t s);
 void launch_build_diag(const GatherPlan& g, cudaStream_t s);
-void launch_td_values(const GatherPlan& g, const double2* factors_dev, cudaStream_t s);
+// Factors at factors_dev, or, with a device step counter, at row 2 * *step + off
+// of the table factors_dev (nf factors per row).
+void launch_td_values(const GatherPlan& g, const double2* factors_dev, cudaStream_t s,
+                      const long long* step = nullptr, long long off = 0, long long nf = 0);
+void launch_td_advance(long long* step, cudaStream_t s);
 // One FFT pass along an axis of every vector: y = alpha * post .* DFT(pre .* x) + beta * y
 // (beta ignored when final == false: y is overwritten).
 // scratch (len * ncols elements, may be null) lets few long lines run as a
