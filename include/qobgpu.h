@@ -324,6 +324,15 @@ int qob_server_create(qob_ctx* ctx, int dtype, size_t mem_budget, int max_active
                       qob_server** out);
 int qob_server_submit(qob_server* server, qob_op* H, const void* psi0, int64_t n, int nsteps,
                       double dt, int64_t* id);
+/* A request with a time-dependent H (TimeDependentSum): H is the LazySum of its
+ * operators and factors holds its coefficients at t0 + r*dt/2 for r = 0 ..
+ * 2*nsteps (nrows rows of nterms interleaved complex doubles, host memory), as
+ * qob_rk4_td takes them.  The request gets a compiled form of its own; its
+ * values are re-evaluated on the device inside the recorded steps.  Every term
+ * must compile into the fused gather (else the request fails with
+ * -QOB_ERR_UNSUPPORTED at admission). */
+int qob_server_submit_td(qob_server* server, qob_op* H, const void* psi0, int64_t n, int nsteps, double dt,
+                         const double* factors, int64_t nrows, int64_t* id);
 int qob_server_step(qob_server* server, int* nactive);
 int qob_server_start(qob_server* server);
 int qob_server_stop(qob_server* server);

@@ -263,6 +263,13 @@ struct Request {
   void* dev = nullptr;
   size_t bytes = 0;
   qob::Plan* plan = nullptr;
+  // time-dependent requests: a plan of their own (its values follow the
+  // request's coefficient rows), the rows on the device, a device step counter
+  bool td = false;
+  std::vector<double> rows_host;  // (2*nsteps+1) x nf interleaved complex
+  int64_t nf = 0;
+  std::unique_ptr<qob::Plan> own_plan;
+  qob::DeviceBuf rows, step_ctr;
 };
 
 }  // namespace
@@ -287,6 +294,7 @@ struct qob_server {
   // second iteration after a rebuild (the first sizes every buffer), replayed after
   int graph_state = 0;  // 0: next step runs directly, 1: next step is recorded, 2: replay
   cudaGraphExec_t graph = nullptr;
+  std::vector<Request*> td_members;  // time-dependent requests of the current ensemble
   std::thread worker;
   bool stop = false;
   bool running = false;
@@ -311,7 +319,36 @@ void admit(qob_server* S) {
     r->bytes = need;
     S->mem_used += need;
     QOB_CUDA(cudaMemcpyAsync(r->dev, r->psi0.data(), r->psi0.size(), cudaMemcpyHostToDevice, S->stream));
-    r->plan = &qob::batch_plan(S->ctx->c, r->op, S->dtype);
+    if (r->td) {
+      try {
+        qob::Context& c = S->ctx->c;
+        r->own_plan = qob::compile_plan(c, r->op->node, QOB_LEFT, S->dtype);
+        qob::Plan& P = *r->own_plan;
+        if (P.kind != qob::Plan::Kind::Sum || !P.dense.empty() || !P.modek.empty() || !P.subs.empty() || !P.gather)
+          qob::fail(QOB_ERR_UNSUPPORTED, "time-dependent requests need every term in the fused gather");
+        qob::prepare_factor_rows(P, *r->op->node, r->rows_host.data(), 2 * (int64_t)r->nsteps + 1);
+        r->rows.upload(r->rows_host.data(), std::max<size_t>(r->rows_host.size(), 2) * sizeof(double));
+        const long long zero = 0;
+        r->step_ctr.upload(&zero, sizeof(zero));
+        // the values of row 0 (stage 1 of the first step)
+        qob::device_refresh(*P.gather, (const double2*)r->rows.p, S->stream, (const long long*)r->step_ctr.p, 0,
+                            (long long)r->nf);
+        r->plan = &P;
+      } catch (const qob::Error& e) {  // this request fails, the server goes on
+        QOB_CUDA(cudaFreeAsync(r->dev, S->stream));
+        r->dev = nullptr;
+        S->mem_used -= need;
+        r->own_plan.reset();
+        r->status = -e.code;
+        r->t_done = now_s();
+        S->rejected++;
+        S->queue.pop_front();
+        S->cv.notify_all();
+        continue;
+      }
+    } else {
+      r->plan = &qob::batch_plan(S->ctx->c, r->op, S->dtype);
+    }
     r->status = 1;
     r->t_admit = now_s();
     S->queue.pop_front();
@@ -326,22 +363,40 @@ void drop_graph(qob_server* S) {
   S->graph_state = 0;
 }
 
+// The launches of one RK4 step: time-dependent members re-evaluate their values
+// before stages 2 and 4 (rows 2s+1, 2s+2 by their device step counters) and
+// advance the counters at the end.
+void step_launches(qob_server* S) {
+  qob::Context& ctx = S->ctx->c;
+  if (S->td_members.empty()) {
+    qob::ensemble_step(ctx, S->ens, S->stream);
+    return;
+  }
+  std::function<void(int)> hook = [&](int mode) {
+    if (mode != 2 && mode != 4) return;
+    for (Request* r : S->td_members)
+      qob::device_refresh(*r->own_plan->gather, (const double2*)r->rows.p, S->stream,
+                          (const long long*)r->step_ctr.p, mode == 2 ? 1 : 2, (long long)r->nf);
+  };
+  qob::ensemble_step(ctx, S->ens, S->stream, &hook);
+  for (Request* r : S->td_members) qob::launch_td_advance(static_cast<long long*>(r->step_ctr.p), S->stream);
+}
+
 // One RK4 step of the ensemble: directly, recorded into a graph, or replayed.
 void run_step(qob_server* S) {
-  qob::Context& ctx = S->ctx->c;
   if (S->graph_state == 2) {
     QOB_CUDA(cudaGraphLaunch(S->graph, S->stream));
     return;
   }
   if (S->graph_state == 0) {
-    qob::ensemble_step(ctx, S->ens, S->stream);
+    step_launches(S);
     S->graph_state = 1;
     return;
   }
   cudaGraph_t g = nullptr;
   QOB_CUDA(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal));
   try {
-    qob::ensemble_step(ctx, S->ens, S->stream);
+    step_launches(S);
   } catch (...) {
     cudaStreamEndCapture(S->stream, &g);
     if (g) cudaGraphDestroy(g);
@@ -378,6 +433,9 @@ int iterate(qob_server* S, int max_steps) {
     }
     S->ens.renormalise = S->renormalise;
     drop_graph(S);
+    S->td_members.clear();
+    for (Request* r : act)
+      if (r->td) S->td_members.push_back(r);
     qob::ensemble_build(ctx, S->ens, states, S->dtype);
     S->dirty = false;
   }
@@ -405,6 +463,10 @@ int iterate(qob_server* S, int max_steps) {
       QOB_CUDA(cudaFreeAsync(r->dev, S->stream));
       S->mem_used -= r->bytes;
       r->dev = nullptr;
+      r->own_plan.reset();  // the step graph that used it is dropped before the next step
+      r->rows = qob::DeviceBuf();
+      r->step_ctr = qob::DeviceBuf();
+      r->rows_host.clear();
       r->status = 2;
       r->t_done = t;
       S->completed++;
@@ -509,6 +571,41 @@ int qob_server_submit(qob_server* S, qob_op* H, const void* psi0, int64_t n, int
     r->id = S->next_id++;
     *id = r->id;
     if (4 * bytes > S->budget) {  // can never be admitted
+      r->status = -QOB_ERR_OOM;
+      r->t_done = r->t_submit;
+      S->rejected++;
+    } else {
+      S->queue.push_back(r.get());
+    }
+    S->all[r->id] = std::move(r);
+    S->cv.notify_all();
+  });
+}
+
+int qob_server_submit_td(qob_server* S, qob_op* H, const void* psi0, int64_t n, int nsteps, double dt,
+                         const double* factors, int64_t nrows, int64_t* id) {
+  return sguard(S, [&] {
+    if (!H || !psi0 || n < 1 || nsteps < 0 || !id) qob::fail(QOB_ERR_ARG, "qob_server_submit_td: bad arguments");
+    if (H->node->kind != qob::Kind::LazySum) qob::fail(QOB_ERR_ARG, "time-dependent requests need a LazySum");
+    if (nrows != 2 * (int64_t)nsteps + 1) qob::fail(QOB_ERR_ARG, "qob_server_submit_td: nrows must be 2*nsteps+1");
+    const int64_t nf = (int64_t)H->node->factors.size();
+    if (nf > 0 && !factors) qob::fail(QOB_ERR_ARG, "qob_server_submit_td: null factor table");
+    if (H->node->m != n || H->node->n != n) qob::fail(QOB_ERR_DIM, "Hamiltonian and state dimensions differ");
+    auto r = std::make_unique<Request>();
+    r->op = H;
+    r->n = n;
+    r->nsteps = nsteps;
+    r->dt = dt;
+    r->td = true;
+    r->nf = nf;
+    if (nf > 0) r->rows_host.assign(factors, factors + 2 * nrows * nf);
+    const size_t bytes = (size_t)n * elem_bytes(S->dtype);
+    r->psi0.assign(static_cast<const char*>(psi0), static_cast<const char*>(psi0) + bytes);
+    r->t_submit = now_s();
+    std::lock_guard<std::mutex> lk(S->mu);
+    r->id = S->next_id++;
+    *id = r->id;
+    if (4 * bytes > S->budget) {
       r->status = -QOB_ERR_OOM;
       r->t_done = r->t_submit;
       S->rejected++;

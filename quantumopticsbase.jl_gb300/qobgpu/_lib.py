@@ -74,6 +74,7 @@ SIGNATURES = {
     "qob_rk4_td": (I, [VP, VP, I, VP, I64, D, I, VP, I64, I, VP]),
     "qob_server_create": (I, [VP, I, C.c_size_t, I, I, C.POINTER(VP)]),
     "qob_server_submit": (I, [VP, VP, VP, I64, I, D, I64P]),
+    "qob_server_submit_td": (I, [VP, VP, VP, I64, I, D, VP, I64, I64P]),
     "qob_server_step": (I, [VP, C.POINTER(C.c_int)]),
     "qob_server_start": (I, [VP]),
     "qob_server_stop": (I, [VP]),

@@ -114,13 +114,21 @@ class Server:
         self._ops = {}
         self._sizes = {}
 
-    def submit(self, H, psi0: np.ndarray, nsteps: int, dt: float) -> int:
+    def submit(self, H, psi0: np.ndarray, nsteps: int, dt: float, t0: float = 0.0) -> int:
+        """Queue nsteps RK4 steps of psi0 under H; a TimeDependentSum is evolved
+        with its coefficients at every stage time from t0 (qob_server_submit_td)."""
         h = handle(self.ctx, H)
         self._ops[id(H)] = (H, h)
         a = np.ascontiguousarray(psi0, dtype=self.dtype)
         rid = C.c_int64()
-        raise_for(L.lib().qob_server_submit(self.ptr, h.ptr, a.ctypes.data_as(C.c_void_p), a.shape[0], int(nsteps),
-                                            float(dt), C.byref(rid)), self.ctx)
+        if isinstance(H, O.TimeDependentSum):
+            rows = np.ascontiguousarray(factor_rows(H, t0, dt, nsteps))
+            raise_for(L.lib().qob_server_submit_td(self.ptr, h.ptr, a.ctypes.data_as(C.c_void_p), a.shape[0],
+                                                   int(nsteps), float(dt), rows.ctypes.data_as(C.c_void_p),
+                                                   rows.shape[0], C.byref(rid)), self.ctx)
+        else:
+            raise_for(L.lib().qob_server_submit(self.ptr, h.ptr, a.ctypes.data_as(C.c_void_p), a.shape[0],
+                                                int(nsteps), float(dt), C.byref(rid)), self.ctx)
         self._sizes[rid.value] = a.shape[0]
         return rid.value
 

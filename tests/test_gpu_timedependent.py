@@ -170,3 +170,42 @@ def test_rk4_time_dependent_argument_checks():
     rc = L.lib().qob_rk4_td(ctx.ptr, hs.ptr, L.QOB_C128, C.c_void_p(d.data_ptr()), 16, 1e-3, 2,
                             rows.ctypes.data_as(C.c_void_p), 5, 0, None)
     assert rc == L.QOB_ERR_ARG  # not a LazySum
+
+
+@pytest.mark.parametrize("threaded", [False, True])
+def test_server_time_dependent_requests_in_a_mix(threaded):
+    """Time-dependent requests served beside a static one: each matches the
+    host RK4 with set_time! per stage, and equals qob_rk4_td run alone bitwise."""
+    import torch
+
+    from qobgpu.evolution import Server, rk4
+
+    static = heisenberg_chain(8, seed=31)
+    tds = [td_heisenberg(8, seed=32), td_driven_jc(7, 7, seed=33)]
+    rng = Q.Rng(304)
+    psis = [rng.ket_data(len(H.basis_l)) for H in [static] + tds]
+    dt, nsteps, t0 = 2e-3, 40, 0.1
+    alone = []
+    for H, p in zip(tds, psis[1:]):
+        d = torch.as_tensor(p.copy(), device="cuda:0")
+        rk4(H, d, dt, nsteps, t0=t0)
+        alone.append(d.cpu().numpy())
+    refs = [rk4_host_td(H, p, dt, nsteps, t0) for H, p in zip(tds, psis[1:])]
+    S = Server(np.complex128)
+    rid_static = S.submit(static, psis[0], nsteps + 7, dt)
+    ids = [S.submit(H, p, nsteps, dt, t0=t0) for H, p in zip(tds, psis[1:])]
+    if threaded:
+        S.start()
+        for i in ids + [rid_static]:
+            S.wait(i, 120.0)
+        S.stop()
+    else:
+        while S.step():
+            pass
+    for i, a, r in zip(ids, alone, refs):
+        st, _, got = S.poll(i)
+        assert st == 2
+        assert rel_l2(got, r) < 1e-12
+        assert np.array_equal(got, a), "served result differs from the same evolution run alone"
+    assert S.poll(rid_static)[0] == 2
+    S.close()
