@@ -127,6 +127,27 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
+def max_over_ranks(value: float, world: int, device=None) -> float:
+    """The largest per-rank value (the slowest rank's time) on every rank; the
+    process group's backend decides where the reduction runs (NCCL: the GPU)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    if device is None:
+        device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """Units per second over all ranks for weak scaling (every rank does the
+    same work; the slowest rank's time bounds the job)."""
+    return units_per_rank * world / seconds
+
+
 def cpu_baseline(H, seconds: float):
     """The oracle port (restated reference mul!) on this host: single thread,
     kets applied one at a time until `seconds` pass; then all threads."""
@@ -279,13 +300,7 @@ def run_own(args, rank, world, local_rank):
         e1.synchronize()
         torch.cuda.synchronize(dev)
         t_host1 = time.time()
-        ms = e0.elapsed_time(e1)
-        if world > 1:
-            import torch.distributed as dist
-
-            t = torch.tensor([ms], device=f"cuda:{dev}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(e0.elapsed_time(e1), world, f"cuda:{dev}")
         if graph is not None:
             lib.qob_graph_free(ctx.ptr, graph)
         return ms, launches, (t_host0, t_host1), (xs, ys)
@@ -325,11 +340,11 @@ def run_own(args, rank, world, local_rank):
     K, W = args.steps, max(3, args.warmup)
     ms64, launches64, win64, _ = timed(torch.complex128, dtype_code(np.complex128), K, W)
     stats64 = step_stats(torch.complex128, dtype_code(np.complex128))
-    value = BATCH * K * world / (ms64 / 1e3)
+    value = whole_job_rate(BATCH * K, world, ms64 / 1e3)
 
     # ComplexF32 mode on the same workload, error against the oracle on one ket
     ms32, _, _, _ = timed(torch.complex64, dtype_code(np.complex64), K, W)
-    value32 = BATCH * K * world / (ms32 / 1e3)
+    value32 = whole_job_rate(BATCH * K, world, ms32 / 1e3)
     err32 = fp32_error(H, dev) if rank == 0 else None
 
     # end to end through the host-buffer C call with pinned host memory
@@ -422,13 +437,7 @@ def end_to_end(lib, ctx, hd, dim, K, dev, world):
     for _ in range(K):
         raise_for(lib.qob_mul_host(*args), ctx)
     torch.cuda.synchronize(dev)
-    dt = time.perf_counter() - t0
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([dt], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dt = float(t.item())
+    dt = max_over_ranks(time.perf_counter() - t0, world, f"cuda:{dev}")
     nbytes = BATCH * dim * 16
     return {"value": BATCH * K * world / dt, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
             "d2h_bytes_per_step": nbytes, "gpu_launches": lib.qob_kernel_launches() - n0,
