@@ -64,6 +64,7 @@ def parse():
     p.add_argument("--no-graph", action="store_true", help="direct launches (used for ncu captures)")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--suite", action="store_true", help="secondary workloads, one JSON line each")
+    p.add_argument("--only", nargs="*", default=None, help="with --suite: these workloads only")
     return p.parse_args()
 
 
@@ -457,7 +458,7 @@ def main():
     if args.suite:
         from qobgpu.suite import run_suite
 
-        return run_suite(local_rank)
+        return run_suite(local_rank, args.only)
     run_own(args, rank, world, local_rank)
 
 

@@ -69,18 +69,34 @@ __device__ __forceinline__ void store(CT* y, CT v, CT post, CT alpha, CT beta) {
 
 // Radix-2 Stockham FFT in shared memory: a holds n = 2^log2n inputs, b is
 // scratch; twiddle m of the length-n transform is tw[m * tws].  Returns the
-// buffer that holds the output (natural order).
+// buffer that holds the output (natural order).  The trivial twiddles (1 in
+// every stage's first butterfly and in the first stage, +-i in the second
+// stage) are applied without multiplications.
 template <typename CT>
 __device__ __forceinline__ CT* stockham(CT* a, CT* b, int64_t n, int log2n, const CT* __restrict__ tw,
                                         int64_t tws) {
   const int64_t half = n >> 1;
+  // sign of the transform: w^(n/4) = +i (bfft) or -i (fft)
+  const bool plus_i = log2n >= 2 ? tw[(int64_t(1) << (log2n - 2)) * tws].y > 0 : true;
   for (int st = 0; st < log2n; ++st) {
     const int64_t ns = int64_t(1) << st;  // half-length of the sub-transforms being merged
     for (int64_t j = threadIdx.x; j < half; j += blockDim.x) {
       const int64_t k = j & (ns - 1);
-      const CT t = tw[(k << (log2n - 1 - st)) * tws];
       const CT u = a[j];
-      const CT v = cm(a[j + half], t);
+      CT v = a[j + half];
+      if (st == 1 && k == 1) {
+        // twiddle w^(n/4) = +i or -i exactly: a swap and a sign change
+        const CT r = v;
+        if (plus_i) {
+          v.x = -r.y;
+          v.y = r.x;
+        } else {
+          v.x = r.y;
+          v.y = -r.x;
+        }
+      } else if (st >= 2 && k != 0) {
+        v = cm(v, tw[(k << (log2n - 1 - st)) * tws]);  // k == 0: twiddle 1
+      }
       const int64_t i0 = 2 * j - k;
       CT s0, s1;
       s0.x = u.x + v.x;

@@ -334,12 +334,17 @@ def host_link(ctx, stream):
     return {"workload": "host_link", "bytes_per_copy": n * 16, "results": out}
 
 
-def run_suite(device: int = 0):
+WORKLOADS = ("jc512", "sparse4096", "rho_h8", "lindblad", "particle", "cavities256", "served", "host_link")
+
+
+def run_suite(device: int = 0, only=None):
+    """Run the workloads (all, or the names in `only`), one JSON line each."""
     import torch
 
     ctx = get_context(device)
     stream = torch.cuda.Stream(device)
-    for fn in (jc512, sparse4096, rho_h8, lindblad, particle, cavities256, served, host_link):
+    names = [w for w in WORKLOADS if not only or w in only]
+    for fn in (globals()[w] for w in names):
         t0 = time.perf_counter()
         line = fn(ctx, stream)
         line["seconds"] = time.perf_counter() - t0

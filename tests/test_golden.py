@@ -24,11 +24,15 @@ def _operands(name):
 
 
 def test_fixture_inputs_regenerate_identically():
-    """The seeded generator reproduces the stored inputs (platform independence)."""
+    """The seeded generator reproduces the stored inputs: bit for bit on the
+    platform that wrote them, and to a few ulp elsewhere (Box-Muller goes
+    through the C library's log / sin / cos, whose last bit may differ between
+    CPU architectures).  Every parity test reads the stored arrays."""
     for i, name in enumerate(NAMES):
         build, form = CASES[name]
         x, y = make_inputs(build(), form, 900 + i)
-        assert np.array_equal(x, GOLD[name + "__x"]) and np.array_equal(y, GOLD[name + "__y"]), name
+        for got, ref in ((x, GOLD[name + "__x"]), (y, GOLD[name + "__y"])):
+            assert np.allclose(got, ref, rtol=1e-14, atol=0), name
 
 
 @pytest.mark.parametrize("name", NAMES)
