@@ -328,13 +328,14 @@ def run_own(args, rank, world, local_rank):
         return out
 
     def tune(dt):
-        times = (C.c_double * 12)()
+        times = (C.c_double * 20)()
         chosen = C.c_int()
         raise_for(lib.qob_op_tune(ctx.ptr, hd.ptr, L.QOB_LEFT, dtype_code(dt), BATCH, times, C.byref(chosen)), ctx)
-        return {"kets_per_thread": chosen.value & 0xFFFF, "threads_per_block": (chosen.value >> 16) & 0x3FFF,
-                "persistent": bool(chosen.value >> 30),
-                "ms_by_kets_per_thread_and_block": {f"{1 << (k // 3)}x{('128', '256', 'P256')[k % 3]}": times[k]
-                                                    for k in range(12)}}
+        v = chosen.value
+        return {"kets_per_thread": v & 0xFFFF, "threads_per_block": (v >> 16) & 0x3FF,
+                "ket_sets_per_warp": 1 << ((v >> 26) & 0x7), "persistent": bool(v >> 30),
+                "ms_by_kets_per_thread_and_shape": {
+                    f"{1 << (k // 5)}x{('128', '256', 'P256', '128s4', '256s4')[k % 5]}": times[k] for k in range(20)}}
 
     prepare(H, L.QOB_LEFT, np.complex64, dev)
     tuning = {"c128": tune(np.complex128), "c64": tune(np.complex64)}
@@ -376,9 +377,10 @@ def run_own(args, rank, world, local_rank):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src, "traffic": prof.get("dram_bytes_per_launch"),
                      "algorithmic_bytes_per_launch": bytes_per_ket * BATCH,
-                     "kernel": "{}<double, real values, square, {} kets/thread, real beta> x {} threads".format(
-                         "k_gather_p" if tuning["c128"]["persistent"] else "k_gather_j",
-                         tuning["c128"]["kets_per_thread"], tuning["c128"]["threads_per_block"]),
+                     "kernel": "{}<double, real values, square, {} kets/thread, real beta> x {} threads, {} ket sets/warp"
+                               .format("k_gather_p" if tuning["c128"]["persistent"] else "k_gather_j",
+                                       tuning["c128"]["kets_per_thread"], tuning["c128"]["threads_per_block"],
+                                       tuning["c128"]["ket_sets_per_warp"]),
                      "ncu_kernel": prof.get("kernel"),
                      "binding": "fp64 FMA throughput (GB300 FP64 ~1.25 TFLOP/s), see fp64_compute"},
         "fp64_compute": fp64,

@@ -144,22 +144,29 @@ int qob_op_shape(qob_ctx* ctx, const qob_op* op, int64_t* rows, int64_t* cols);
 int qob_op_prepare(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t* info);
 
 /* Autotuner: time the fused kernel with 1, 2, 4 and 8 vectors per thread and
- * three launch shapes -- blocks of 128 or 256 threads over the output indices,
- * or a persistent grid of (SMs x resident blocks) 256-thread blocks that split
- * the work evenly -- for applications of op to ncols vectors (side, dtype as
+ * five launch shapes for applications of op to ncols vectors (side, dtype as
  * in qob_mul) and keep the fastest for later calls with this operator, side
- * and dtype.  times_ms[3k + b] = milliseconds per application with 2^k vectors
- * per thread and shape b (0: 128, 1: 256, 2: persistent), -1 when not tried
- * (12 entries); *chosen = vectors per thread | (threads per block << 16) |
- * (1 << 30 when persistent), 0 when the operator has no fused part.  Either
- * pointer may be NULL.  Allocates and frees two scratch arrays; synchronous. */
+ * and dtype.  Shapes b: 0 / 1 = blocks of 128 / 256 threads over the output
+ * indices; 2 = a persistent grid of (SMs x resident blocks) 256-thread blocks
+ * that split the work evenly; 3 / 4 = blocks of 128 / 256 threads whose warps
+ * cover 8 output indices x 4 sets of vectors (entries that vary with the low
+ * index bits then diverge over fewer lanes).  times_ms[5k + b] = milliseconds
+ * per application with 2^k vectors per thread and shape b, -1 when not tried
+ * (20 entries); *chosen = vectors per thread | (threads per block << 16) |
+ * (log2 vector sets per warp << 26) | (1 << 30 when persistent), 0 when the
+ * operator has no fused part.  Either pointer may be NULL.  Vector sets (x
+ * and y) of 16 MB or more are timed with inputs not in L2 (up to 8 scratch
+ * copies, at least 256 MB in all, used in turn), smaller ones L2-resident.
+ * Allocates and frees the scratch arrays; synchronous. */
 int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, double* times_ms,
                 int* chosen);
 
 /* Fix the launch shape instead of tuning: vectors_per_thread 1, 2, 4 or 8;
- * block 128 or 256 threads, or -256 for the persistent grid (as chosen by
- * qob_op_tune).  Kept until the next tune or recompilation. */
-int qob_op_set_launch(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_per_thread, int block);
+ * block 128 or 256 threads, or -256 for the persistent grid; lane_split 1, 2,
+ * 4 or 8 vector sets per warp (not used by the persistent grid).  Kept until
+ * the next tune or recompilation. */
+int qob_op_set_launch(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_per_thread, int block,
+                      int lane_split);
 
 /* ---------------------------------------------------------------------------
  * Application: the 5-argument mul!.

@@ -475,18 +475,30 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
     check_dtype(dtype);
     Plan& P = get_plan(ctx->c, op, side, dtype);
     const int tiles[4] = {1, 2, 4, 8};
-    const int blocks[3] = {128, 256, -256};  // -256: persistent grid of 256-thread blocks
-    double t[12];
+    // launch shapes: 128 / 256 threads, the persistent grid of 256-thread
+    // blocks, and 128 / 256 threads with four vector sets per warp
+    constexpr int kShapes = 5;
+    const int blocks[kShapes] = {128, 256, -256, 128, 256};
+    const int splits[kShapes] = {1, 1, 1, 4, 4};
+    double t[4 * kShapes];
     for (double& v : t) v = -1.0;
-    int best = 0, best_block = 256;
+    int best = 0, best_block = 256, best_split = 1;
     if (P.gather && P.kind == Plan::Kind::Sum) {
       GatherPlan& g = *P.gather;
       const size_t esz = dtype == QOB_C128 ? 16 : 8;
+      // Vector sets of 16 MB or more are tuned as a stream of such sets would
+      // run -- inputs not in L2: up to 8 copies, at least 256 MB in all, used
+      // in turn; smaller sets are tuned L2-resident, as they would be used.
+      const size_t xsz = (size_t)P.n * ncols * esz, ysz = (size_t)P.m * ncols * esz;
+      const size_t set = xsz + ysz;
+      const int copies = set >= (size_t(16) << 20) ? (int)std::min<size_t>(8, ((size_t(256) << 20) + set - 1) / set) : 1;
       DeviceBuf x, y;
-      x.alloc((size_t)P.n * ncols * esz);
-      y.alloc((size_t)P.m * ncols * esz);
+      x.alloc(xsz * copies);
+      y.alloc(ysz * copies);
       QOB_CUDA(cudaMemset(x.p, 0, x.bytes));
       QOB_CUDA(cudaMemset(y.p, 0, y.bytes));
+      auto xc = [&](int i) { return static_cast<char*>(x.p) + (size_t)(i % copies) * xsz; };
+      auto yc = [&](int i) { return static_cast<char*>(y.p) + (size_t)(i % copies) * ysz; };
       // vectors as the reference lays them out: columns for LEFT, rows for RIGHT
       const int64_t xes = side == QOB_LEFT ? 1 : ncols, xcs = side == QOB_LEFT ? P.n : 1;
       const int64_t yes = side == QOB_LEFT ? 1 : ncols, ycs = side == QOB_LEFT ? P.m : 1;
@@ -494,49 +506,61 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
       QOB_CUDA(cudaEventCreate(&e0));
       QOB_CUDA(cudaEventCreate(&e1));
       double best_t = 1e300;
-      for (int k = 0; k < 12; ++k) {
-        const int tc = tiles[k / 3], blk = blocks[k % 3];
+      for (int k = 0; k < 4 * kShapes; ++k) {
+        const int tc = tiles[k / kShapes], blk = blocks[k % kShapes], ls = splits[k % kShapes];
         if (tc > ncols || (tc > 1 && side == QOB_RIGHT && ncols > 1)) continue;
+        if (ls > 1 && (tc * ls > ncols || side == QOB_RIGHT)) continue;
         g.tc = tc;
         g.block = blk;
+        g.lane_split = ls;
         for (int i = 0; i < 2; ++i)
-          apply_plan(ctx->c, P, {1.0, 0.0}, x.p, xes, xcs, {0.3, 0.0}, y.p, yes, ycs, ncols, 0, 0);
+          apply_plan(ctx->c, P, {1.0, 0.0}, xc(i), xes, xcs, {0.3, 0.0}, yc(i), yes, ycs, ncols, 0, 0);
+        const int reps = std::max(5, copies);
         QOB_CUDA(cudaEventRecord(e0, 0));
-        for (int i = 0; i < 5; ++i)
-          apply_plan(ctx->c, P, {1.0, 0.0}, x.p, xes, xcs, {0.3, 0.0}, y.p, yes, ycs, ncols, 0, 0);
+        for (int i = 0; i < reps; ++i)
+          apply_plan(ctx->c, P, {1.0, 0.0}, xc(i + 2), xes, xcs, {0.3, 0.0}, yc(i + 2), yes, ycs, ncols, 0, 0);
         QOB_CUDA(cudaEventRecord(e1, 0));
         QOB_CUDA(cudaEventSynchronize(e1));
         float ms = 0.f;
         QOB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        t[k] = ms / 5.0;
+        t[k] = ms / reps;
         if (t[k] < best_t) {
           best_t = t[k];
           best = tc;
           best_block = blk;
+          best_split = ls;
         }
       }
       g.tc = best;
       g.block = best_block;
+      g.lane_split = best_split;
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
     }
     if (times_ms)
-      for (int k = 0; k < 12; ++k) times_ms[k] = t[k];
-    if (chosen) *chosen = best | ((best_block < 0 ? -best_block : best_block) << 16) | (best_block < 0 ? (1 << 30) : 0);
+      for (int k = 0; k < 4 * kShapes; ++k) times_ms[k] = t[k];
+    int lg = 0;
+    while ((1 << lg) < best_split) ++lg;
+    if (chosen)
+      *chosen = best | ((best_block < 0 ? -best_block : best_block) << 16) | (lg << 26) | (best_block < 0 ? (1 << 30) : 0);
   });
 }
 
-int qob_op_set_launch(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_per_thread, int block) {
+int qob_op_set_launch(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_per_thread, int block,
+                      int lane_split) {
   return guard(ctx, [&] {
     if (!ctx || !op || (side != QOB_LEFT && side != QOB_RIGHT)) fail(QOB_ERR_ARG, "qob_op_set_launch: bad arguments");
     check_dtype(dtype);
     if (vectors_per_thread != 1 && vectors_per_thread != 2 && vectors_per_thread != 4 && vectors_per_thread != 8)
       fail(QOB_ERR_ARG, "vectors per thread must be 1, 2, 4 or 8");
     if (block != 128 && block != 256 && block != -256) fail(QOB_ERR_ARG, "block must be 128, 256 or -256");
+    if (lane_split != 1 && lane_split != 2 && lane_split != 4 && lane_split != 8)
+      fail(QOB_ERR_ARG, "lane_split must be 1, 2, 4 or 8");
     Plan& P = get_plan(ctx->c, op, side, dtype);
     if (P.gather) {
       P.gather->tc = vectors_per_thread;
       P.gather->block = block;
+      P.gather->lane_split = lane_split;
     }
   });
 }

@@ -447,18 +447,27 @@ __global__ void __launch_bounds__(256) k_gather_j(GatherView g, SiteTable st,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const ET* ell = stage<ET>(smem_raw, g);
   const GGroup* sg = reinterpret_cast<const GGroup*>(smem_raw);
+  // lane split ls: a warp covers 32/ls consecutive output indices and ls
+  // interleaved sets of TC vectors (vectors q, q + ls, ...), so operator
+  // entries that vary with the low index bits diverge over fewer lanes; each
+  // load still reads whole 32-byte sectors (32/ls consecutive elements per vector)
+  const int ls = g.lane_split;
+  const int jw = 32 / ls;
+  const int lane = threadIdx.x & 31;
   const int64_t blk = (int64_t)(((uint64_t)blockIdx.x * g.jmul) % (uint64_t)gridDim.x);
-  const int64_t J = blk * blockDim.x + threadIdx.x;
+  const int64_t J = blk * (blockDim.x / ls) + (threadIdx.x >> 5) * jw + (lane % jw);
   if (J >= g.m) return;
-  const int c0 = blockIdx.y * TC;
-  const int nt = min(TC, ncols - c0);
+  const int c0 = blockIdx.y * TC * ls + lane / jw;
+  const int nt = c0 < ncols ? min(TC, (ncols - c0 + ls - 1) / ls) : 0;
+  if (nt <= 0) return;
+  const int64_t vs_x = (int64_t)ls * xcs, vs_y = (int64_t)ls * ycs;
   const CT* xb = x + (int64_t)c0 * xcs;
   AT acc[TC];
-  accumulate<R, VM, SQUARE, W1, TC>(g, st, sg, ell, (uint32_t)J, xb, 1, xcs, nt, acc);
+  accumulate<R, VM, SQUARE, W1, TC>(g, st, sg, ell, (uint32_t)J, xb, 1, vs_x, nt, acc);
   CT* yb = y + J + (int64_t)c0 * ycs;
 #pragma unroll
   for (int t = 0; t < TC; ++t)
-    if (t < nt) combine<BMODE>(yb + t * ycs, acc[t].total(), alpha, beta);
+    if (t < nt) combine<BMODE>(yb + t * vs_y, acc[t].total(), alpha, beta);
 }
 
 // The same work as k_gather_j on a grid of exactly (SMs x resident blocks per
@@ -562,15 +571,19 @@ void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t x
   auto kern = k_gather_j<R, VM, SQUARE, W1, TC, BMODE>;
   allow_smem(kern, smem);
   const int threads = v.block > 0 ? v.block : kThreads;
-  const unsigned gx = (unsigned)((v.m + threads - 1) / threads);
+  const int ls = v.lane_split > 0 ? v.lane_split : 1;
+  const int64_t jpb = threads / ls;  // output indices per block
+  const unsigned gx = (unsigned)((v.m + jpb - 1) / jpb);
   GatherView w = v;
+  w.lane_split = ls;
   // a few waves of blocks: permuted so every SM's share mixes the whole index
   // range; many waves: in order (the hardware balances them, and neighbouring
   // blocks share the gathered input in L2)
   w.jmul = gx <= 4096 ? chunk_multiplier(gx) : 1;
-  for (int64_t c0 = 0; c0 < ncols; c0 += (int64_t)65535 * TC) {  // grid.y limit
-    const int64_t nc = std::min<int64_t>(ncols - c0, (int64_t)65535 * TC);
-    kern<<<dim3(gx, (unsigned)((nc + TC - 1) / TC)), threads, smem, s>>>(
+  const int64_t per_y = (int64_t)TC * ls;  // vectors per grid row
+  for (int64_t c0 = 0; c0 < ncols; c0 += (int64_t)65535 * per_y) {  // grid.y limit
+    const int64_t nc = std::min<int64_t>(ncols - c0, (int64_t)65535 * per_y);
+    kern<<<dim3(gx, (unsigned)((nc + per_y - 1) / per_y)), threads, smem, s>>>(
         w, st, (const CT*)x + c0 * xcs, xcs, (CT*)y + c0 * ycs, ycs, (int)nc, a, b);
     QOB_LAUNCHED();
   }

@@ -1012,6 +1012,7 @@ GatherView GatherPlan::view() const {
   v.fast = fast ? 1 : 0;
   v.fastg = (const int4*)fastg.p;
   v.block = block;
+  v.lane_split = lane_split;
   return v;
 }
 

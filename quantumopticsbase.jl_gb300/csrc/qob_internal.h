@@ -172,6 +172,7 @@ struct GatherView {
   // cover index ranges far apart, so the cost of a block -- which depends on the high index
   // bits through the operator's sparsity -- averages out over the blocks an SM runs.
   uint32_t jmul;
+  int32_t lane_split;  // k_gather_j: vector sets per warp (1, 2, 4 or 8; 32/lane_split indices per warp)
 };
 
 // A host-side record of how each stored entry is made from the terms, so a
@@ -246,6 +247,7 @@ struct GatherPlan {
   DeviceBuf fastg;
   int tc = 0;     // vectors per thread chosen by qob_op_tune (0: automatic)
   int block = 0;  // threads per block chosen by qob_op_tune (0: 256; < 0: persistent grid of -block)
+  int lane_split = 1;  // vector sets per warp chosen by qob_op_tune
   DeviceBuf dgroups, dvals;  // diagonal sources: groups + local diagonal tables
   int ndgroups = 0;
   SiteTable sites{};

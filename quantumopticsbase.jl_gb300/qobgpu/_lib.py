@@ -50,7 +50,7 @@ SIGNATURES = {
     "qob_op_shape": (I, [VP, VP, I64P, I64P]),
     "qob_op_prepare": (I, [VP, VP, I, I, I64P]),
     "qob_op_tune": (I, [VP, VP, I, I, I64, DP, C.POINTER(C.c_int)]),
-    "qob_op_set_launch": (I, [VP, VP, I, I, I, I]),
+    "qob_op_set_launch": (I, [VP, VP, I, I, I, I, I]),
     "qob_mul": (I, [VP, I, I, VP, I, D, D, VP, I64, I64, I64, D, D, VP, I64, I64, I64, VP]),
     "qob_mul_host": (I, [VP, I, I, VP, I, D, D, VP, I64, I64, D, D, VP, I64, I64]),
     "qob_norm": (I, [VP, I, VP, I64, DP, VP]),

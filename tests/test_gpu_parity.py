@@ -69,12 +69,13 @@ def test_heisenberg_14_spins_batch():
     check(out, H, psi, AL, BE, TOL64)
 
 
-@pytest.mark.parametrize("block", [128, 256, -256])
+@pytest.mark.parametrize("block,split", [(128, 1), (256, 1), (-256, 1), (128, 4), (256, 2), (128, 8)])
 @pytest.mark.parametrize("tc", [1, 2, 4, 8])
-def test_every_launch_shape(tc, block):
+def test_every_launch_shape(tc, block, split):
     """Each vectors-per-thread tile and launch shape (-256: the persistent grid of
-    SMs x resident blocks) on the 10-spin chain (a compact-form plan) and the
-    Jaynes-Cummings model (generic groups), 37 kets (ragged last tile)."""
+    SMs x resident blocks; split: vector sets per warp) on the 10-spin chain (a
+    compact-form plan) and the Jaynes-Cummings model (generic groups), 37 kets
+    (ragged last tiles)."""
     from qobgpu import _lib as L
     from qobgpu.device import dtype_code, get_context, handle, raise_for
 
@@ -86,7 +87,8 @@ def test_every_launch_shape(tc, block):
         Y = O.Operator(H.basis_l, Q.GenericBasis(nb), rng.kets_data(len(H.basis_l), nb))
         for dtype, tol in ((np.complex128, TOL64), (np.complex64, TOL32)):
             h = handle(ctx, H)
-            raise_for(L.lib().qob_op_set_launch(ctx.ptr, h.ptr, L.QOB_LEFT, dtype_code(dtype), tc, block), ctx)
+            raise_for(L.lib().qob_op_set_launch(ctx.ptr, h.ptr, L.QOB_LEFT, dtype_code(dtype), tc, block, split),
+                      ctx)
             check(Y, H, X, AL, BE, tol, dtype)
             check(Y, H, X, AL, 0.0, tol, dtype)
 

@@ -209,3 +209,26 @@ def test_server_time_dependent_requests_in_a_mix(threaded):
         assert np.array_equal(got, a), "served result differs from the same evolution run alone"
     assert S.poll(rid_static)[0] == 2
     S.close()
+
+
+def test_server_time_dependent_request_that_cannot_compile_fails_alone():
+    """A time-dependent request whose terms do not all fit the fused gather (a
+    LazyProduct term) fails with -QOB_ERR_UNSUPPORTED at admission; the
+    requests beside it complete."""
+    from qobgpu import _lib as L
+    from qobgpu.evolution import Server
+
+    H = heisenberg_chain(6, seed=41)
+    b = H.basis_l
+    prod = O.LazyProduct((H.operators[0], H.operators[1]))
+    bad = O.TimeDependentSum([1.0, lambda t: np.cos(t)], (H.operators[2], prod))
+    good = td_heisenberg(6, seed=42)
+    rng = Q.Rng(305)
+    S = Server(np.complex128)
+    r_bad = S.submit(bad, rng.ket_data(len(b)), 10, 1e-3)
+    r_good = S.submit(good, rng.ket_data(len(b)), 10, 1e-3)
+    while S.step():
+        pass
+    assert S.poll(r_bad)[0] == -L.QOB_ERR_UNSUPPORTED
+    assert S.poll(r_good)[0] == 2
+    S.close()
