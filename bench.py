@@ -63,6 +63,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-graph", action="store_true", help="direct launches (used for ncu captures)")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--shape", default=None,
+                   help="fixed launch shapes instead of tuning, e.g. c128=4x256s4,c64=4x128 (used for ncu captures)")
     p.add_argument("--suite", action="store_true", help="secondary workloads, one JSON line each")
     p.add_argument("--only", nargs="*", default=None, help="with --suite: these workloads only")
     return p.parse_args()
@@ -337,8 +339,23 @@ def run_own(args, rank, world, local_rank):
                 "ms_by_kets_per_thread_and_shape": {
                     f"{1 << (k // 5)}x{('128', '256', 'P256', '128s4', '256s4')[k % 5]}": times[k] for k in range(20)}}
 
+    def fix(dt, spec):
+        """A launch shape given as <kets per thread>x<threads>[s<ket sets per warp>], P for persistent."""
+        kt, rest = spec.split("x")
+        split = int(rest.split("s")[1]) if "s" in rest else 1
+        blk = rest.split("s")[0]
+        block = -int(blk[1:]) if blk.startswith("P") else int(blk)
+        raise_for(lib.qob_op_set_launch(ctx.ptr, hd.ptr, L.QOB_LEFT, dtype_code(dt), int(kt), block, split), ctx)
+        return {"kets_per_thread": int(kt), "threads_per_block": abs(block), "ket_sets_per_warp": split,
+                "persistent": block < 0, "fixed": spec}
+
     prepare(H, L.QOB_LEFT, np.complex64, dev)
-    tuning = {"c128": tune(np.complex128), "c64": tune(np.complex64)}
+    if args.shape:
+        spec = dict(kv.split("=") for kv in args.shape.split(","))
+        tuning = {k: fix(dt, spec[k]) if k in spec else tune(dt)
+                  for k, dt in (("c128", np.complex128), ("c64", np.complex64))}
+    else:
+        tuning = {"c128": tune(np.complex128), "c64": tune(np.complex64)}
     K, W = args.steps, max(3, args.warmup)
     ms64, launches64, win64, _ = timed(torch.complex128, dtype_code(np.complex128), K, W)
     stats64 = step_stats(torch.complex128, dtype_code(np.complex128))
@@ -417,6 +434,12 @@ def fp32_error(H, dev):
 
 
 def end_to_end(lib, ctx, hd, dim, K, dev, world):
+    """K steps through the host-buffer C calls, each step its own pair of
+    page-locked host batches (x and y of 64 kets; 4 pairs in turn): x and y go
+    in, y comes back, every step.  The headline form streams the steps through
+    qob_mul_host_async (a step's copies in overlap the previous step's kernels
+    and copy out; a pair is reused once its earlier call's ticket has been
+    waited on); the synchronous qob_mul_host is timed beside it."""
     import ctypes as C
 
     import torch
@@ -424,27 +447,52 @@ def end_to_end(lib, ctx, hd, dim, K, dev, world):
     from qobgpu import _lib as L
     from qobgpu.device import raise_for
 
-    xh = torch.randn(BATCH, dim, dtype=torch.complex128).pin_memory()
-    yh = torch.randn(BATCH, dim, dtype=torch.complex128).pin_memory()
-    args = (ctx.ptr, L.QOB_LEFT, 0, hd.ptr, L.QOB_C128, ALPHA.real, ALPHA.imag, C.c_void_p(xh.data_ptr()), dim,
-            BATCH, BETA, 0.0, C.c_void_p(yh.data_ptr()), dim, BATCH)
-    for _ in range(3):
-        raise_for(lib.qob_mul_host(*args), ctx)
-    if world > 1:
-        import torch.distributed as dist
+    R = 4
+    gen = torch.Generator().manual_seed(4321)
+    xh = [torch.randn(BATCH, dim, dtype=torch.complex128, generator=gen).pin_memory() for _ in range(R)]
+    yh = [torch.randn(BATCH, dim, dtype=torch.complex128, generator=gen).pin_memory() for _ in range(R)]
 
-        dist.barrier()
-    torch.cuda.synchronize(dev)
-    n0 = lib.qob_kernel_launches()
-    t0 = time.perf_counter()
-    for _ in range(K):
-        raise_for(lib.qob_mul_host(*args), ctx)
-    torch.cuda.synchronize(dev)
-    dt = max_over_ranks(time.perf_counter() - t0, world, f"cuda:{dev}")
+    def args(b):
+        return (ctx.ptr, L.QOB_LEFT, 0, hd.ptr, L.QOB_C128, ALPHA.real, ALPHA.imag, C.c_void_p(xh[b].data_ptr()), dim,
+                BATCH, BETA, 0.0, C.c_void_p(yh[b].data_ptr()), dim, BATCH)
+
+    argl = [args(b) for b in range(R)]
+
+    def run_sync(steps):
+        for i in range(steps):
+            raise_for(lib.qob_mul_host(*argl[i % R]), ctx)
+
+    def run_async(steps):
+        tickets = [0] * R
+        t = C.c_uint64()
+        for i in range(steps):
+            b = i % R
+            raise_for(lib.qob_host_wait(ctx.ptr, tickets[b]), ctx)
+            raise_for(lib.qob_mul_host_async(*argl[b], C.byref(t)), ctx)
+            tickets[b] = t.value
+        raise_for(lib.qob_host_wait(ctx.ptr, t.value), ctx)
+
+    def timed(run):
+        run(3)
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        n0 = lib.qob_kernel_launches()
+        t0 = time.perf_counter()
+        run(K)
+        torch.cuda.synchronize(dev)
+        dt = max_over_ranks(time.perf_counter() - t0, world, f"cuda:{dev}")
+        return BATCH * K * world / dt, lib.qob_kernel_launches() - n0
+
+    v_async, l_async = timed(run_async)
+    v_sync, _ = timed(run_sync)
     nbytes = BATCH * dim * 16
-    return {"value": BATCH * K * world / dt, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
-            "d2h_bytes_per_step": nbytes, "gpu_launches": lib.qob_kernel_launches() - n0,
-            "api": "qob_mul_host (pinned host buffers; x and beta-scaled y copied in, y copied out each step)"}
+    return {"value": v_async, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": nbytes,
+            "gpu_launches": l_async, "sync_value": v_sync,
+            "api": "qob_mul_host_async + qob_host_wait (page-locked host batches, 4 pairs in turn; x and the "
+                   "beta-scaled y copied in, y copied out every step); sync_value: qob_mul_host, one call at a time"}
 
 
 def main():

@@ -155,9 +155,12 @@ int qob_op_prepare(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t* info)
  * (20 entries); *chosen = vectors per thread | (threads per block << 16) |
  * (log2 vector sets per warp << 26) | (1 << 30 when persistent), 0 when the
  * operator has no fused part.  Either pointer may be NULL.  Vector sets (x
- * and y) of 16 MB or more are timed with inputs not in L2 (up to 8 scratch
+ * and y) of 16 MB or more are timed with inputs not in L2 (up to 16 scratch
  * copies, at least 256 MB in all, used in turn), smaller ones L2-resident.
- * Allocates and frees the scratch arrays; synchronous. */
+ * Each shape is timed over launches replayed from a CUDA graph on a stream of
+ * the context's own (no host launch overhead in the times, as in the recorded
+ * loops of qob_rk4 / the server).  Allocates and frees the scratch arrays;
+ * synchronous. */
 int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, double* times_ms,
                 int* chosen);
 
@@ -189,12 +192,33 @@ int qob_mul(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, double
             double beta_re, double beta_im, void* y, int64_t y_rows, int64_t y_cols, int64_t y_ld,
             void* stream);
 
-/* Same as qob_mul for HOST x and y: the library copies x to the device, applies
- * the operator and copies y back (the path a caller without device buffers
- * uses).  Synchronous. */
+/* Same as qob_mul for HOST x and y (column-major, leading dimension = rows):
+ * the library copies x (and y when beta != 0) to the device, applies the
+ * operator and copies y back -- the path a caller without device buffers uses.
+ * Several kets from the left go through in up to four chunks of columns whose
+ * copies and kernels overlap.  Synchronous: returns with y written. */
 int qob_mul_host(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, double alpha_re,
                  double alpha_im, const void* x, int64_t x_rows, int64_t x_cols, double beta_re,
                  double beta_im, void* y, int64_t y_rows, int64_t y_cols);
+
+/* Stream-ordered qob_mul_host for a stream of batches: enqueues the copies
+ * in, the application and the copy of y back out, and returns at once with a
+ * ticket.  After qob_host_wait(ctx, ticket) returns, y holds the result and x
+ * and y may be reused; until then the caller leaves both untouched.  Calls run
+ * in the order made, and each call's copies in overlap the previous call's
+ * kernels and copy out (two device staging sets are used in turn), so a stream
+ * of batches moves at the host link's rate.  With page-locked host memory the
+ * copies are asynchronous; with pageable memory the driver stages them and the
+ * call returns once they are done.  Errors of the argument checks return at
+ * once; errors of the device work return from qob_host_wait. */
+int qob_mul_host_async(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, double alpha_re,
+                       double alpha_im, const void* x, int64_t x_rows, int64_t x_cols, double beta_re,
+                       double beta_im, void* y, int64_t y_rows, int64_t y_cols, uint64_t* ticket);
+
+/* Blocks until the qob_mul_host_async call that returned `ticket` and every
+ * earlier one have finished.  Ticket 0 returns at once; a ticket not yet handed
+ * out is QOB_ERR_ARG. */
+int qob_host_wait(qob_ctx* ctx, uint64_t ticket);
 
 /* ---------------------------------------------------------------------------
  * FP64 reductions (norm, inner product, expectation value) on device vectors;

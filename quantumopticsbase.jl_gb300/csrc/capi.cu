@@ -57,6 +57,10 @@ Context::~Context() {
     if (pipe_in[k]) cudaEventDestroy(pipe_in[k]);
     if (pipe_done[k]) cudaEventDestroy(pipe_done[k]);
   }
+  for (auto e : stage_free)
+    if (e) cudaEventDestroy(e);
+  for (auto e : ticket_done)
+    if (e) cudaEventDestroy(e);
 }
 
 namespace {
@@ -487,16 +491,20 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
       GatherPlan& g = *P.gather;
       const size_t esz = dtype == QOB_C128 ? 16 : 8;
       // Vector sets of 16 MB or more are tuned as a stream of such sets would
-      // run -- inputs not in L2: up to 8 copies, at least 256 MB in all, used
+      // run -- inputs not in L2: up to 16 copies, at least 256 MB in all, used
       // in turn; smaller sets are tuned L2-resident, as they would be used.
       const size_t xsz = (size_t)P.n * ncols * esz, ysz = (size_t)P.m * ncols * esz;
       const size_t set = xsz + ysz;
-      const int copies = set >= (size_t(16) << 20) ? (int)std::min<size_t>(8, ((size_t(256) << 20) + set - 1) / set) : 1;
+      const int copies = set >= (size_t(16) << 20) ? (int)std::min<size_t>(16, ((size_t(256) << 20) + set - 1) / set) : 1;
       DeviceBuf x, y;
       x.alloc(xsz * copies);
       y.alloc(ysz * copies);
-      QOB_CUDA(cudaMemset(x.p, 0, x.bytes));
-      QOB_CUDA(cudaMemset(y.p, 0, y.bytes));
+      // timed on a stream of the context's own, the launches replayed from a
+      // CUDA graph: no host launch overhead in the times, as in a recorded loop
+      if (!ctx->c.copy_stream[1]) QOB_CUDA(cudaStreamCreateWithFlags(&ctx->c.copy_stream[1], cudaStreamNonBlocking));
+      cudaStream_t ts = ctx->c.copy_stream[1];
+      QOB_CUDA(cudaMemsetAsync(x.p, 0, x.bytes, ts));
+      QOB_CUDA(cudaMemsetAsync(y.p, 0, y.bytes, ts));
       auto xc = [&](int i) { return static_cast<char*>(x.p) + (size_t)(i % copies) * xsz; };
       auto yc = [&](int i) { return static_cast<char*>(y.p) + (size_t)(i % copies) * ysz; };
       // vectors as the reference lays them out: columns for LEFT, rows for RIGHT
@@ -514,13 +522,30 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
         g.block = blk;
         g.lane_split = ls;
         for (int i = 0; i < 2; ++i)
-          apply_plan(ctx->c, P, {1.0, 0.0}, xc(i), xes, xcs, {0.3, 0.0}, yc(i), yes, ycs, ncols, 0, 0);
-        const int reps = std::max(5, copies);
-        QOB_CUDA(cudaEventRecord(e0, 0));
-        for (int i = 0; i < reps; ++i)
-          apply_plan(ctx->c, P, {1.0, 0.0}, xc(i + 2), xes, xcs, {0.3, 0.0}, yc(i + 2), yes, ycs, ncols, 0, 0);
-        QOB_CUDA(cudaEventRecord(e1, 0));
-        QOB_CUDA(cudaEventSynchronize(e1));
+          apply_plan(ctx->c, P, {1.0, 0.0}, xc(i), xes, xcs, {0.3, 0.0}, yc(i), yes, ycs, ncols, ts, 0);
+        const int reps = std::max(8, copies);
+        cudaGraph_t gr = nullptr;
+        QOB_CUDA(cudaStreamBeginCapture(ts, cudaStreamCaptureModeThreadLocal));
+        try {
+          for (int i = 0; i < reps; ++i)
+            apply_plan(ctx->c, P, {1.0, 0.0}, xc(i + 2), xes, xcs, {0.3, 0.0}, yc(i + 2), yes, ycs, ncols, ts, 0);
+        } catch (...) {
+          cudaStreamEndCapture(ts, &gr);  // leave the stream usable
+          if (gr) cudaGraphDestroy(gr);
+          throw;
+        }
+        QOB_CUDA(cudaStreamEndCapture(ts, &gr));
+        cudaGraphExec_t ge = nullptr;
+        const cudaError_t ie = cudaGraphInstantiate(&ge, gr, 0);
+        cudaGraphDestroy(gr);
+        QOB_CUDA(ie);
+        QOB_CUDA(cudaGraphLaunch(ge, ts));  // untimed replay
+        QOB_CUDA(cudaEventRecord(e0, ts));
+        QOB_CUDA(cudaGraphLaunch(ge, ts));
+        QOB_CUDA(cudaEventRecord(e1, ts));
+        const cudaError_t se = cudaEventSynchronize(e1);
+        cudaGraphExecDestroy(ge);
+        QOB_CUDA(se);
         float ms = 0.f;
         QOB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
         t[k] = ms / reps;
@@ -565,47 +590,136 @@ int qob_op_set_launch(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors
   });
 }
 
+namespace {
+
+// The vector layout of y = alpha * op * x + beta * y: vectors are the columns
+// of x and y (side LEFT, kets) or their rows (side RIGHT, bras); checks the
+// dimensions as the reference's mul! does (src/operators.jl).
+struct MulShape {
+  int64_t ncols = 0, xes = 1, xcs = 1, yes = 1, ycs = 1;
+  bool empty = false;
+};
+
+MulShape mul_shape(const qob_op* op, int side, int is_vector, int64_t x_rows, int64_t x_cols, int64_t x_ld,
+                   int64_t y_rows, int64_t y_cols, int64_t y_ld) {
+  if (!op) fail(QOB_ERR_ARG, "null context or operator");
+  if (side != QOB_LEFT && side != QOB_RIGHT) fail(QOB_ERR_ARG, "side must be QOB_LEFT or QOB_RIGHT");
+  const int64_t m = op->node->m, n = op->node->n;
+  MulShape sh;
+  if (side == QOB_LEFT) {
+    if (x_rows != n) fail(QOB_ERR_DIM, "A and B dimensions do not match. Can't do `A*B`");
+    if (y_rows != m || y_cols != x_cols) fail(QOB_ERR_DIM, "Output dimensions do not match A*B. Can't do `R.=A*B`");
+    if (is_vector && x_cols != 1) fail(QOB_ERR_ARG, "a Ket has one column");
+    if (x_ld < std::max<int64_t>(x_rows, 1) || y_ld < std::max<int64_t>(y_rows, 1))
+      fail(QOB_ERR_ARG, "leading dimension smaller than the number of rows");
+    sh.ncols = x_cols;
+    sh.xcs = x_ld;
+    sh.ycs = y_ld;
+  } else {
+    if (x_cols != m) fail(QOB_ERR_DIM, "A and B dimensions do not match. Can't do `A*B`");
+    if (y_cols != n || y_rows != x_rows) fail(QOB_ERR_DIM, "Output dimensions do not match A*B. Can't do `R.=A*B`");
+    if (is_vector && x_rows != 1) fail(QOB_ERR_ARG, "a Bra has one row");
+    if (x_ld < std::max<int64_t>(x_rows, 1) || y_ld < std::max<int64_t>(y_rows, 1))
+      fail(QOB_ERR_ARG, "leading dimension smaller than the number of rows");
+    sh.ncols = x_rows;
+    sh.xes = x_ld;
+    sh.yes = y_ld;
+  }
+  sh.empty = sh.ncols == 0 || (side == QOB_LEFT ? m : n) == 0;
+  if (!sh.empty && sh.ncols > 65535 && side == QOB_RIGHT) fail(QOB_ERR_UNSUPPORTED, "more than 65535 rows");
+  return sh;
+}
+
+// Enqueues one host call: copies in on copy_stream[0], the application on
+// copy_stream[1], the copy of y back on copy_stream[2], linked per chunk by
+// events.  Several kets from the left go through in up to four chunks of
+// columns, so that the copies of one chunk overlap the kernels of another;
+// other shapes in one chunk.  The call uses staging set (host_calls % 2) once
+// the copy out of the call before the previous one has left it.  Returns the
+// call's ticket.
+uint64_t enqueue_host(Context& c, int side, int is_vector, qob_op* op, int dtype, c128 alpha, const void* x,
+                      int64_t x_rows, int64_t x_cols, c128 beta, void* y, int64_t y_rows, int64_t y_cols) {
+  check_dtype(dtype);
+  const MulShape sh = mul_shape(op, side, is_vector, x_rows, x_cols, std::max<int64_t>(x_rows, 1), y_rows, y_cols,
+                                std::max<int64_t>(y_rows, 1));
+  const bool has_beta = beta.re != 0.0 || beta.im != 0.0;
+  {
+    const size_t esz = dtype == QOB_C128 ? 16 : 8;
+    if (!sh.empty && overlaps(x, (size_t)x_rows * x_cols * esz, y, (size_t)y_rows * y_cols * esz))
+      fail(QOB_ERR_ALIAS, "output matrix must not be aliased with input matrix");
+  }
+  for (int k = 0; k < 3; ++k)
+    if (!c.copy_stream[k]) QOB_CUDA(cudaStreamCreateWithFlags(&c.copy_stream[k], cudaStreamNonBlocking));
+  for (int k = 0; k < Context::kPipeChunks; ++k) {
+    if (!c.pipe_in[k]) QOB_CUDA(cudaEventCreateWithFlags(&c.pipe_in[k], cudaEventDisableTiming));
+    if (!c.pipe_done[k]) QOB_CUDA(cudaEventCreateWithFlags(&c.pipe_done[k], cudaEventDisableTiming));
+  }
+  for (int k = 0; k < 2; ++k)
+    if (!c.stage_free[k]) QOB_CUDA(cudaEventCreateWithFlags(&c.stage_free[k], cudaEventDisableTiming));
+  for (int k = 0; k < Context::kTickets; ++k)
+    if (!c.ticket_done[k]) QOB_CUDA(cudaEventCreateWithFlags(&c.ticket_done[k], cudaEventDisableTiming));
+  cudaStream_t sin = c.copy_stream[0], scomp = c.copy_stream[1], sout = c.copy_stream[2];
+  const uint64_t ticket = c.host_calls + 1;
+  if (!sh.empty) {
+    if (!x || !y) fail(QOB_ERR_ARG, "null data pointer");
+    const int st = (int)(c.host_calls & 1);
+    const size_t esz = dtype == QOB_C128 ? 16 : 8;
+    const size_t xb = (size_t)x_rows * x_cols * esz, yb = (size_t)y_rows * y_cols * esz;
+    if (c.stage_x[st].bytes < xb || c.stage_y[st].bytes < yb) {
+      // a larger set: the calls in flight finish before the old one is freed
+      for (int k = 0; k < 3; ++k) QOB_CUDA(cudaStreamSynchronize(c.copy_stream[k]));
+      if (c.stage_x[st].bytes < xb) c.stage_x[st].alloc(xb);
+      if (c.stage_y[st].bytes < yb) c.stage_y[st].alloc(yb);
+    }
+    Plan& P = get_plan(c, op, side, dtype);
+    if (c.stage_used[st]) QOB_CUDA(cudaStreamWaitEvent(sin, c.stage_free[st], 0));
+    const bool chunked = side == QOB_LEFT && x_cols >= 8;
+    const int64_t nchunk = chunked ? std::min<int64_t>(4, x_cols / 4) : 1;
+    const int64_t per = chunked ? (x_cols + nchunk - 1) / nchunk : x_cols;
+    int64_t k = 0;
+    for (int64_t c0 = 0; c0 < x_cols; c0 += per, ++k) {
+      const int64_t nc = std::min(per, x_cols - c0);
+      char* dx = static_cast<char*>(c.stage_x[st].p) + (size_t)c0 * x_rows * esz;
+      char* dy = static_cast<char*>(c.stage_y[st].p) + (size_t)c0 * y_rows * esz;
+      const char* hx = static_cast<const char*>(x) + (size_t)c0 * x_rows * esz;
+      char* hy = static_cast<char*>(y) + (size_t)c0 * y_rows * esz;
+      QOB_CUDA(cudaMemcpyAsync(dx, hx, (size_t)nc * x_rows * esz, cudaMemcpyHostToDevice, sin));
+      if (has_beta) QOB_CUDA(cudaMemcpyAsync(dy, hy, (size_t)nc * y_rows * esz, cudaMemcpyHostToDevice, sin));
+      QOB_CUDA(cudaEventRecord(c.pipe_in[k], sin));
+      QOB_CUDA(cudaStreamWaitEvent(scomp, c.pipe_in[k], 0));
+      if (chunked)
+        apply_plan(c, P, alpha, dx, 1, x_rows, beta, dy, 1, y_rows, nc, scomp, 24);
+      else
+        apply_plan(c, P, alpha, dx, sh.xes, sh.xcs, beta, dy, sh.yes, sh.ycs, sh.ncols, scomp, 24);
+      QOB_CUDA(cudaEventRecord(c.pipe_done[k], scomp));
+      QOB_CUDA(cudaStreamWaitEvent(sout, c.pipe_done[k], 0));
+      QOB_CUDA(cudaMemcpyAsync(hy, dy, (size_t)nc * y_rows * esz, cudaMemcpyDeviceToHost, sout));
+    }
+    QOB_CUDA(cudaEventRecord(c.stage_free[st], sout));
+    c.stage_used[st] = true;
+  }
+  QOB_CUDA(cudaEventRecord(c.ticket_done[(ticket - 1) % Context::kTickets], sout));
+  c.host_calls = ticket;
+  return ticket;
+}
+
+}  // namespace
+
 int qob_mul(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, double alpha_re, double alpha_im,
             const void* x, int64_t x_rows, int64_t x_cols, int64_t x_ld, double beta_re, double beta_im, void* y,
             int64_t y_rows, int64_t y_cols, int64_t y_ld, void* stream) {
   return guard(ctx, [&] {
-    if (!ctx || !op) fail(QOB_ERR_ARG, "null context or operator");
-    if (side != QOB_LEFT && side != QOB_RIGHT) fail(QOB_ERR_ARG, "side must be QOB_LEFT or QOB_RIGHT");
+    if (!ctx) fail(QOB_ERR_ARG, "null context or operator");
     check_dtype(dtype);
-    const int64_t m = op->node->m, n = op->node->n;
-    int64_t ncols, xes, xcs, yes, ycs;
-    if (side == QOB_LEFT) {
-      if (x_rows != n) fail(QOB_ERR_DIM, "A and B dimensions do not match. Can't do `A*B`");
-      if (y_rows != m || y_cols != x_cols) fail(QOB_ERR_DIM, "Output dimensions do not match A*B. Can't do `R.=A*B`");
-      if (is_vector && x_cols != 1) fail(QOB_ERR_ARG, "a Ket has one column");
-      if (x_ld < std::max<int64_t>(x_rows, 1) || y_ld < std::max<int64_t>(y_rows, 1))
-        fail(QOB_ERR_ARG, "leading dimension smaller than the number of rows");
-      ncols = x_cols;
-      xes = 1;
-      xcs = x_ld;
-      yes = 1;
-      ycs = y_ld;
-    } else {
-      if (x_cols != m) fail(QOB_ERR_DIM, "A and B dimensions do not match. Can't do `A*B`");
-      if (y_cols != n || y_rows != x_rows) fail(QOB_ERR_DIM, "Output dimensions do not match A*B. Can't do `R.=A*B`");
-      if (is_vector && x_rows != 1) fail(QOB_ERR_ARG, "a Bra has one row");
-      if (x_ld < std::max<int64_t>(x_rows, 1) || y_ld < std::max<int64_t>(y_rows, 1))
-        fail(QOB_ERR_ARG, "leading dimension smaller than the number of rows");
-      ncols = x_rows;
-      xes = x_ld;
-      xcs = 1;
-      yes = y_ld;
-      ycs = 1;
-    }
-    if (ncols == 0 || (side == QOB_LEFT ? m : n) == 0) return;
+    const MulShape sh = mul_shape(op, side, is_vector, x_rows, x_cols, x_ld, y_rows, y_cols, y_ld);
+    if (sh.empty) return;
     if (!x || !y) fail(QOB_ERR_ARG, "null data pointer");
     const size_t esz = dtype == QOB_C128 ? 16 : 8;
     const size_t xbytes = (size_t)(x_ld * (x_cols - 1) + x_rows) * esz;
     const size_t ybytes = (size_t)(y_ld * (y_cols - 1) + y_rows) * esz;
     if (overlaps(x, xbytes, y, ybytes)) fail(QOB_ERR_ALIAS, "output matrix must not be aliased with input matrix");
-    if (ncols > 65535 && side == QOB_RIGHT) fail(QOB_ERR_UNSUPPORTED, "more than 65535 rows");
     Plan& P = get_plan(ctx->c, op, side, dtype);
-    apply_plan(ctx->c, P, {alpha_re, alpha_im}, x, xes, xcs, {beta_re, beta_im}, y, yes, ycs, ncols,
+    apply_plan(ctx->c, P, {alpha_re, alpha_im}, x, sh.xes, sh.xcs, {beta_re, beta_im}, y, sh.yes, sh.ycs, sh.ncols,
                (cudaStream_t)stream, 0);
   });
 }
@@ -613,73 +727,31 @@ int qob_mul(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, double
 int qob_mul_host(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, double alpha_re, double alpha_im,
                  const void* x, int64_t x_rows, int64_t x_cols, double beta_re, double beta_im, void* y,
                  int64_t y_rows, int64_t y_cols) {
-  const bool has_beta = beta_re != 0.0 || beta_im != 0.0;
-  // Several kets from the left: chunks of columns through a three-stream
-  // pipeline -- host-to-device copies back to back on one stream (the link is
-  // the bottleneck), each chunk's kernels on a second stream once its copy is
-  // in, its result copied back on a third -- so the copy engine for inputs
-  // never waits behind an output copy.
-  if (side == QOB_LEFT && x_cols >= 8 && x_cols == y_cols) {
-    return guard(ctx, [&] {
-      if (!ctx || !op || !x || !y) fail(QOB_ERR_ARG, "null argument");
-      check_dtype(dtype);
-      if (x_rows != op->node->n || y_rows != op->node->m)
-        fail(QOB_ERR_DIM, "A and B dimensions do not match. Can't do `A*B`");
-      Context& c = ctx->c;
-      const size_t esz = dtype == QOB_C128 ? 16 : 8;
-      const size_t xb = (size_t)x_rows * x_cols * esz, yb = (size_t)y_rows * y_cols * esz;
-      if (c.host_x.bytes < xb) c.host_x.alloc(xb);
-      if (c.host_y.bytes < yb) c.host_y.alloc(yb);
-      for (int k = 0; k < 3; ++k)
-        if (!c.copy_stream[k]) QOB_CUDA(cudaStreamCreateWithFlags(&c.copy_stream[k], cudaStreamNonBlocking));
-      for (int k = 0; k < Context::kPipeChunks; ++k) {
-        if (!c.pipe_in[k]) QOB_CUDA(cudaEventCreateWithFlags(&c.pipe_in[k], cudaEventDisableTiming));
-        if (!c.pipe_done[k]) QOB_CUDA(cudaEventCreateWithFlags(&c.pipe_done[k], cudaEventDisableTiming));
-      }
-      Plan& P = get_plan(c, op, QOB_LEFT, dtype);
-      cudaStream_t sin = c.copy_stream[0], scomp = c.copy_stream[1], sout = c.copy_stream[2];
-      const int64_t nchunk = std::min<int64_t>(4, x_cols / 4);
-      const int64_t per = (x_cols + nchunk - 1) / nchunk;
-      int64_t k = 0;
-      for (int64_t c0 = 0; c0 < x_cols; c0 += per, ++k) {
-        const int64_t nc = std::min(per, x_cols - c0);
-        char* dx = static_cast<char*>(c.host_x.p) + (size_t)c0 * x_rows * esz;
-        char* dy = static_cast<char*>(c.host_y.p) + (size_t)c0 * y_rows * esz;
-        const char* hx = static_cast<const char*>(x) + (size_t)c0 * x_rows * esz;
-        char* hy = static_cast<char*>(y) + (size_t)c0 * y_rows * esz;
-        QOB_CUDA(cudaMemcpyAsync(dx, hx, (size_t)nc * x_rows * esz, cudaMemcpyHostToDevice, sin));
-        if (has_beta) QOB_CUDA(cudaMemcpyAsync(dy, hy, (size_t)nc * y_rows * esz, cudaMemcpyHostToDevice, sin));
-        QOB_CUDA(cudaEventRecord(c.pipe_in[k], sin));
-        QOB_CUDA(cudaStreamWaitEvent(scomp, c.pipe_in[k], 0));
-        apply_plan(c, P, {alpha_re, alpha_im}, dx, 1, x_rows, {beta_re, beta_im}, dy, 1, y_rows, nc, scomp, 24);
-        QOB_CUDA(cudaEventRecord(c.pipe_done[k], scomp));
-        QOB_CUDA(cudaStreamWaitEvent(sout, c.pipe_done[k], 0));
-        QOB_CUDA(cudaMemcpyAsync(hy, dy, (size_t)nc * y_rows * esz, cudaMemcpyDeviceToHost, sout));
-      }
-      QOB_CUDA(cudaStreamSynchronize(sout));
-      QOB_CUDA(cudaStreamSynchronize(scomp));
-      QOB_CUDA(cudaStreamSynchronize(sin));
-    });
-  }
-  int rc = guard(ctx, [&] {
-    if (!ctx || !op || !x || !y) fail(QOB_ERR_ARG, "null argument");
-    check_dtype(dtype);
-    const size_t esz = dtype == QOB_C128 ? 16 : 8;
-    const size_t xb = (size_t)x_rows * x_cols * esz, yb = (size_t)y_rows * y_cols * esz;
-    if (ctx->c.host_x.bytes < xb) ctx->c.host_x.alloc(xb);
-    if (ctx->c.host_y.bytes < yb) ctx->c.host_y.alloc(yb);
-    QOB_CUDA(cudaMemcpyAsync(ctx->c.host_x.p, x, xb, cudaMemcpyHostToDevice, 0));
-    if (has_beta) QOB_CUDA(cudaMemcpyAsync(ctx->c.host_y.p, y, yb, cudaMemcpyHostToDevice, 0));
-  });
-  if (rc) return rc;
-  rc = qob_mul(ctx, side, is_vector, op, dtype, alpha_re, alpha_im, ctx->c.host_x.p, x_rows, x_cols,
-               std::max<int64_t>(x_rows, 1), beta_re, beta_im, ctx->c.host_y.p, y_rows, y_cols,
-               std::max<int64_t>(y_rows, 1), nullptr);
-  if (rc) return rc;
   return guard(ctx, [&] {
-    const size_t esz = dtype == QOB_C128 ? 16 : 8;
-    QOB_CUDA(cudaMemcpyAsync(y, ctx->c.host_y.p, (size_t)y_rows * y_cols * esz, cudaMemcpyDeviceToHost, 0));
-    QOB_CUDA(cudaStreamSynchronize(0));
+    if (!ctx) fail(QOB_ERR_ARG, "null context or operator");
+    const uint64_t t = enqueue_host(ctx->c, side, is_vector, op, dtype, {alpha_re, alpha_im}, x, x_rows, x_cols,
+                                    {beta_re, beta_im}, y, y_rows, y_cols);
+    QOB_CUDA(cudaEventSynchronize(ctx->c.ticket_done[(t - 1) % Context::kTickets]));
+  });
+}
+
+int qob_mul_host_async(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, double alpha_re,
+                       double alpha_im, const void* x, int64_t x_rows, int64_t x_cols, double beta_re,
+                       double beta_im, void* y, int64_t y_rows, int64_t y_cols, uint64_t* ticket) {
+  return guard(ctx, [&] {
+    if (!ctx || !ticket) fail(QOB_ERR_ARG, "null context or ticket");
+    *ticket = enqueue_host(ctx->c, side, is_vector, op, dtype, {alpha_re, alpha_im}, x, x_rows, x_cols,
+                           {beta_re, beta_im}, y, y_rows, y_cols);
+  });
+}
+
+int qob_host_wait(qob_ctx* ctx, uint64_t ticket) {
+  return guard(ctx, [&] {
+    if (!ctx) fail(QOB_ERR_ARG, "null context");
+    if (ticket > ctx->c.host_calls) fail(QOB_ERR_ARG, "qob_host_wait: ticket not handed out");
+    if (ticket == 0) return;
+    // a slot recorded again by a later call ends later: waiting on it is safe
+    QOB_CUDA(cudaEventSynchronize(ctx->c.ticket_done[(ticket - 1) % Context::kTickets]));
   });
 }
 

@@ -337,12 +337,20 @@ struct Context {
   Workspace ws;
   DeviceBuf reduce_buf;
   void* reduce_host = nullptr;  // pinned
-  DeviceBuf host_x, host_y;     // staging for qob_mul_host
   // qob_mul_host's pipeline: copies in, kernels, copies out on three streams,
   // linked per chunk by events
   cudaStream_t copy_stream[3] = {nullptr, nullptr, nullptr};
   static constexpr int kPipeChunks = 8;
   cudaEvent_t pipe_in[kPipeChunks] = {}, pipe_done[kPipeChunks] = {};
+  // two device staging sets for host calls, used in turn; stage_free[s] marks
+  // the last copy out of the call that used set s
+  DeviceBuf stage_x[2], stage_y[2];
+  cudaEvent_t stage_free[2] = {};
+  bool stage_used[2] = {false, false};
+  // tickets of qob_mul_host_async: call t's last copy out is ticket_done[(t-1) % kTickets]
+  static constexpr int kTickets = 16;
+  cudaEvent_t ticket_done[kTickets] = {};
+  uint64_t host_calls = 0;
   ~Context();
 };
 

@@ -53,6 +53,8 @@ SIGNATURES = {
     "qob_op_set_launch": (I, [VP, VP, I, I, I, I, I]),
     "qob_mul": (I, [VP, I, I, VP, I, D, D, VP, I64, I64, I64, D, D, VP, I64, I64, I64, VP]),
     "qob_mul_host": (I, [VP, I, I, VP, I, D, D, VP, I64, I64, D, D, VP, I64, I64]),
+    "qob_mul_host_async": (I, [VP, I, I, VP, I, D, D, VP, I64, I64, D, D, VP, I64, I64, VP]),
+    "qob_host_wait": (I, [VP, C.c_uint64]),
     "qob_norm": (I, [VP, I, VP, I64, DP, VP]),
     "qob_dot": (I, [VP, I, VP, VP, I64, DP, VP]),
     "qob_expect": (I, [VP, VP, I, VP, I64, DP, VP]),
