@@ -350,12 +350,13 @@ def run_own(args, rank, world, local_rank):
                 "persistent": block < 0, "fixed": spec}
 
     prepare(H, L.QOB_LEFT, np.complex64, dev)
+    prepare(H, L.QOB_LEFT, "ff", dev)
     if args.shape:
         spec = dict(kv.split("=") for kv in args.shape.split(","))
         tuning = {k: fix(dt, spec[k]) if k in spec else tune(dt)
-                  for k, dt in (("c128", np.complex128), ("c64", np.complex64))}
+                  for k, dt in (("c128", np.complex128), ("c64", np.complex64), ("c128x", "ff"))}
     else:
-        tuning = {"c128": tune(np.complex128), "c64": tune(np.complex64)}
+        tuning = {"c128": tune(np.complex128), "c64": tune(np.complex64), "c128x": tune("ff")}
     K, W = args.steps, max(3, args.warmup)
     ms64, launches64, win64, _ = timed(torch.complex128, dtype_code(np.complex128), K, W)
     stats64 = step_stats(torch.complex128, dtype_code(np.complex128))
@@ -364,7 +365,10 @@ def run_own(args, rank, world, local_rank):
     # ComplexF32 mode on the same workload, error against the oracle on one ket
     ms32, _, _, _ = timed(torch.complex64, dtype_code(np.complex64), K, W)
     value32 = whole_job_rate(BATCH * K, world, ms32 / 1e3)
-    err32 = fp32_error(H, dev) if rank == 0 else None
+    # ComplexF64 data in double-float arithmetic on the FP32 pipes (QOB_C128X)
+    msff, launchesff, _, _ = timed(torch.complex128, L.QOB_C128X, K, W)
+    valueff = whole_job_rate(BATCH * K, world, msff / 1e3)
+    err32, errff = mode_errors(H, dev) if rank == 0 else (None, None)
 
     # end to end through the host-buffer C call with pinned host memory
     e2e = None
@@ -407,7 +411,11 @@ def run_own(args, rank, world, local_rank):
         "tuning": tuning,
         "gpu_launches": launches64,
         "fp32_mode": {"value": value32, "unit": UNIT, "ms_per_step": ms32 / K, "vs_fp64": value32 / value,
-                      "rel_l2_err_vs_oracle": err32},
+                      "rel_l2_err_vs_c128": err32},
+        "ff_mode": {"value": valueff, "unit": UNIT, "ms_per_step": msff / K, "vs_fp64": valueff / value,
+                    "rel_l2_err_vs_c128": errff, "gpu_launches": launchesff,
+                    "note": "ComplexF64 data, fused gather in double-float (FP32-pair) arithmetic, "
+                            "one split launch + one gather launch per step (QOB_C128X)"},
         "e2e": e2e,
         "clocks": sampler.summary(*win64) if sampler else None,
     }
@@ -416,21 +424,26 @@ def run_own(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
-def fp32_error(H, dev):
+def mode_errors(H, dev):
+    """Relative l2 error of the ComplexF32 and the double-float form against the
+    ComplexF64 form (itself held to the oracle at 1e-12 by the tests) on one ket."""
     import numpy as np
 
-    import oracle as OR
     import qobgpu as Q
     from qobgpu.mul import mul_, to_device
 
     rng = Q.Rng(97)
     psi = Q.Ket(H.basis_r, rng.ket_data(len(H.basis_r)))
     out = Q.Ket(H.basis_l, rng.ket_data(len(H.basis_l)))
-    ref = OR.mul(out, H, psi, ALPHA, BETA)
-    d_out = to_device(out, dev, np.complex64)
-    mul_(d_out, H, to_device(psi, dev, np.complex64), ALPHA, BETA)
-    got = d_out.data.cpu().numpy().astype(np.complex128)
-    return float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+
+    def run(dtype, arith=None):
+        d_out = to_device(out, dev, dtype)
+        mul_(d_out, H, to_device(psi, dev, dtype), ALPHA, BETA, arith=arith)
+        return d_out.data.cpu().numpy().astype(np.complex128)
+
+    ref = run(np.complex128)
+    rel = lambda got: float(np.linalg.norm(got - ref) / np.linalg.norm(ref))  # noqa: E731
+    return rel(run(np.complex64)), rel(run(np.complex128, "ff"))
 
 
 def end_to_end(lib, ctx, hd, dim, K, dev, world):

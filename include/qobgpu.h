@@ -47,6 +47,17 @@ extern "C" {
 /* element types */
 #define QOB_C128 0 /* ComplexF64 */
 #define QOB_C64 1  /* ComplexF32 */
+/* ComplexF64 data with the fused LazySum part applied in double-float
+ * arithmetic (each number the unevaluated sum of two FP32 numbers, about 48
+ * significant bits) on the FP32 pipes, which on GB300 issue far faster than
+ * its FP64 pipe; other parts (dense, mode-k, FFT passes) run in FP64.  Results
+ * agree with QOB_C128 to about 1e-14 relative (l2).  Magnitudes of vector
+ * elements, operator entries, alpha and beta in [2^-74, 2^128) keep full
+ * precision; smaller ones keep 24 bits and below 2^-126 flush to zero; larger
+ * ones become infinite.  Accepted by qob_mul, qob_mul_host, qob_mul_host_async,
+ * qob_op_prepare, qob_op_tune and qob_op_set_launch; the other entry points
+ * take QOB_C128 or QOB_C64. */
+#define QOB_C128X 2
 
 /* sides of qob_mul */
 #define QOB_LEFT 0  /* y = alpha * op * x + beta * y   (Ket, or Operator from the left)  */

@@ -83,7 +83,7 @@ const void* batch_kernel(int prec, bool real) {
 
 bool plan_fusable(const Plan& P) {
   return P.kind == Plan::Kind::Sum && P.gather && P.dense.empty() && P.modek.empty() && P.subs.empty() &&
-         P.gather->square && !P.gather->phased && P.gather->ngroups <= 256 && P.nterms_total > 0;
+         P.gather->square && !P.gather->phased && !P.gather->ff && P.gather->ngroups <= 256 && P.nterms_total > 0;
 }
 
 void build_tables(Context& ctx, BatchTables& T, const std::vector<BatchSpec>& specs, int prec, int tile) {

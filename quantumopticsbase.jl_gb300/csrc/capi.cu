@@ -93,7 +93,12 @@ void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, i
     }
     c128 b = beta;  // the first pass applies beta, the rest accumulate (:194-197)
     if (P.gather) {
-      launch_gather(*P.gather, P.precision, x, xes, xcs, y, yes, ycs, ncols, alpha, b, s);
+      // a double-float gather splits x into slot ws first (free here: x and y
+      // of a nested call live in the caller's slots)
+      void* ffx = P.gather->ff
+                      ? ctx.ws.get(ws, (size_t)((P.n - 1) * xes + (ncols - 1) * xcs + 1) * 16)
+                      : nullptr;
+      launch_gather(*P.gather, P.precision, x, xes, xcs, y, yes, ycs, ncols, alpha, b, s, P.n, ffx);
       b = one;
     }
     for (auto& d : P.dense) {
@@ -224,6 +229,12 @@ c128 read_c(const void* p, int dtype, int64_t i) {
 void check_dtype(int dtype) {
   if (dtype != QOB_C128 && dtype != QOB_C64) fail(QOB_ERR_ARG, "dtype must be QOB_C128 or QOB_C64");
 }
+// qob_mul and its relatives also take the double-float form of ComplexF64
+void check_mul_dtype(int dtype) {
+  if (dtype != QOB_C128 && dtype != QOB_C64 && dtype != QOB_C128X)
+    fail(QOB_ERR_ARG, "dtype must be QOB_C128, QOB_C64 or QOB_C128X");
+}
+size_t elem_size(int dtype) { return dtype == QOB_C64 ? 8 : 16; }
 
 qob_op* wrap(NodeP n) {
   auto* h = new qob_op;
@@ -461,7 +472,7 @@ int qob_op_shape(qob_ctx* ctx, const qob_op* op, int64_t* rows, int64_t* cols) {
 int qob_op_prepare(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t* info) {
   return guard(ctx, [&] {
     if (!ctx || !op || (side != QOB_LEFT && side != QOB_RIGHT)) fail(QOB_ERR_ARG, "qob_op_prepare: bad arguments");
-    check_dtype(dtype);
+    check_mul_dtype(dtype);
     Plan& P = get_plan(ctx->c, op, side, dtype);
     if (info) {
       info[0] = P.gather ? P.gather->ngroups : 0;
@@ -476,7 +487,7 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
   return guard(ctx, [&] {
     if (!ctx || !op || ncols < 1 || (side != QOB_LEFT && side != QOB_RIGHT))
       fail(QOB_ERR_ARG, "qob_op_tune: bad arguments");
-    check_dtype(dtype);
+    check_mul_dtype(dtype);
     Plan& P = get_plan(ctx->c, op, side, dtype);
     const int tiles[4] = {1, 2, 4, 8};
     // launch shapes: 128 / 256 threads, the persistent grid of 256-thread
@@ -489,7 +500,7 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
     int best = 0, best_block = 256, best_split = 1;
     if (P.gather && P.kind == Plan::Kind::Sum) {
       GatherPlan& g = *P.gather;
-      const size_t esz = dtype == QOB_C128 ? 16 : 8;
+      const size_t esz = elem_size(dtype);
       // Vector sets of 16 MB or more are tuned as a stream of such sets would
       // run -- inputs not in L2: up to 16 copies, at least 256 MB in all, used
       // in turn; smaller sets are tuned L2-resident, as they would be used.
@@ -575,7 +586,7 @@ int qob_op_set_launch(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors
                       int lane_split) {
   return guard(ctx, [&] {
     if (!ctx || !op || (side != QOB_LEFT && side != QOB_RIGHT)) fail(QOB_ERR_ARG, "qob_op_set_launch: bad arguments");
-    check_dtype(dtype);
+    check_mul_dtype(dtype);
     if (vectors_per_thread != 1 && vectors_per_thread != 2 && vectors_per_thread != 4 && vectors_per_thread != 8)
       fail(QOB_ERR_ARG, "vectors per thread must be 1, 2, 4 or 8");
     if (block != 128 && block != 256 && block != -256) fail(QOB_ERR_ARG, "block must be 128, 256 or -256");
@@ -639,12 +650,12 @@ MulShape mul_shape(const qob_op* op, int side, int is_vector, int64_t x_rows, in
 // call's ticket.
 uint64_t enqueue_host(Context& c, int side, int is_vector, qob_op* op, int dtype, c128 alpha, const void* x,
                       int64_t x_rows, int64_t x_cols, c128 beta, void* y, int64_t y_rows, int64_t y_cols) {
-  check_dtype(dtype);
+  check_mul_dtype(dtype);
   const MulShape sh = mul_shape(op, side, is_vector, x_rows, x_cols, std::max<int64_t>(x_rows, 1), y_rows, y_cols,
                                 std::max<int64_t>(y_rows, 1));
   const bool has_beta = beta.re != 0.0 || beta.im != 0.0;
   {
-    const size_t esz = dtype == QOB_C128 ? 16 : 8;
+    const size_t esz = elem_size(dtype);
     if (!sh.empty && overlaps(x, (size_t)x_rows * x_cols * esz, y, (size_t)y_rows * y_cols * esz))
       fail(QOB_ERR_ALIAS, "output matrix must not be aliased with input matrix");
   }
@@ -663,7 +674,7 @@ uint64_t enqueue_host(Context& c, int side, int is_vector, qob_op* op, int dtype
   if (!sh.empty) {
     if (!x || !y) fail(QOB_ERR_ARG, "null data pointer");
     const int st = (int)(c.host_calls & 1);
-    const size_t esz = dtype == QOB_C128 ? 16 : 8;
+    const size_t esz = elem_size(dtype);
     const size_t xb = (size_t)x_rows * x_cols * esz, yb = (size_t)y_rows * y_cols * esz;
     if (c.stage_x[st].bytes < xb || c.stage_y[st].bytes < yb) {
       // a larger set: the calls in flight finish before the old one is freed
@@ -710,11 +721,11 @@ int qob_mul(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, double
             int64_t y_rows, int64_t y_cols, int64_t y_ld, void* stream) {
   return guard(ctx, [&] {
     if (!ctx) fail(QOB_ERR_ARG, "null context or operator");
-    check_dtype(dtype);
+    check_mul_dtype(dtype);
     const MulShape sh = mul_shape(op, side, is_vector, x_rows, x_cols, x_ld, y_rows, y_cols, y_ld);
     if (sh.empty) return;
     if (!x || !y) fail(QOB_ERR_ARG, "null data pointer");
-    const size_t esz = dtype == QOB_C128 ? 16 : 8;
+    const size_t esz = elem_size(dtype);
     const size_t xbytes = (size_t)(x_ld * (x_cols - 1) + x_rows) * esz;
     const size_t ybytes = (size_t)(y_ld * (y_cols - 1) + y_rows) * esz;
     if (overlaps(x, xbytes, y, ybytes)) fail(QOB_ERR_ALIAS, "output matrix must not be aliased with input matrix");

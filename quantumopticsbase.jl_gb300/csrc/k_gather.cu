@@ -3,6 +3,8 @@
 // and the merged-diagonal builder.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "k_gather.cuh"
 
 namespace qob {
@@ -13,11 +15,19 @@ extern template void dispatch<double>(const GatherView&, const SiteTable&, int, 
                                       void*, int64_t, int64_t, int64_t, c128, c128, cudaStream_t);
 extern template void dispatch<float>(const GatherView&, const SiteTable&, int, const void*, int64_t, int64_t,
                                      void*, int64_t, int64_t, int64_t, c128, c128, cudaStream_t);
+extern template void dispatch<DF>(const GatherView&, const SiteTable&, int, const void*, int64_t, int64_t,
+                                  void*, int64_t, int64_t, int64_t, c128, c128, cudaStream_t);
 }  // namespace gather
 
 namespace {
 
 constexpr int kGroupsPerLaunch = 256;  // 256 * sizeof(GGroup) = 44 KB of shared memory
+
+// (hi, lo) float pair of a double: hi rounded to nearest, lo = the rest (not hot)
+__device__ __forceinline__ float2 split_rn(double v) {
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
 
 // Merged diagonal: diag[J] = sum over groups of their local diagonal table.
 template <typename R, bool REALV>
@@ -35,7 +45,14 @@ __global__ void k_build_diag(int64_t m, int ndg, const GGroup* __restrict__ dg,
   }
   using VT = typename gather::Val<R, REALV>::T;
   VT* out = static_cast<VT*>(diag);
-  if constexpr (REALV) {
+  if constexpr (std::is_same<R, gather::DF>::value) {
+    if constexpr (REALV) {
+      out[J] = split_rn(re);
+    } else {
+      const float2 a = split_rn(re), b = split_rn(im);
+      out[J] = make_float4(a.x, a.y, b.x, b.y);
+    }
+  } else if constexpr (REALV) {
     out[J] = (R)re;
   } else {
     typename gather::Cx<R>::T o;
@@ -43,6 +60,34 @@ __global__ void k_build_diag(int64_t m, int ndg, const GGroup* __restrict__ dg,
     o.y = (R)im;
     out[J] = o;
   }
+}
+
+// Split of the input vectors into double-float quadruples (re hi, re lo, im
+// hi, im lo), element e of vector c at e * es + c * cs in both arrays.  Each
+// thread moves kSplitPer elements a block apart, their loads issued together.
+constexpr int kSplitPer = 4;
+__global__ void __launch_bounds__(256) k_ff_split(const double2* __restrict__ x, int64_t n, int64_t ncols,
+                                                  int64_t es, int64_t cs, float4* __restrict__ out) {
+  const int64_t total = n * ncols;
+  const int64_t i0 = blockIdx.x * (int64_t)blockDim.x * kSplitPer + threadIdx.x;
+  int64_t o[kSplitPer];
+  double2 v[kSplitPer];
+#pragma unroll
+  for (int k = 0; k < kSplitPer; ++k) {
+    const int64_t i = i0 + (int64_t)k * blockDim.x;
+    o[k] = -1;
+    if (i < total) {
+      const int64_t c = i / n, e = i - c * n;
+      o[k] = e * es + c * cs;
+      v[k] = __ldg(x + o[k]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kSplitPer; ++k)
+    if (o[k] >= 0) {
+      const float2 a = gather::ff_split(v[k].x), b = gather::ff_split(v[k].y);
+      out[o[k]] = make_float4(a.x, a.y, b.x, b.y);
+    }
 }
 
 // Stored values re-evaluated from the root LazySum's factors: one thread per
@@ -80,29 +125,52 @@ __global__ void __launch_bounds__(256) k_td_values(int nslots, const TdSlot* __r
   }
   if (sl.dst_diag >= 0) dtab[sl.dst_diag] = make_double2(re, im);
   const double sv = sl.part ? im : re;  // the stored number of a real-storage plan
-  if (sl.dst_val >= 0) {
-    if constexpr (REALV) {
-      static_cast<R*>(vals)[sl.dst_val] = (R)sv;
-    } else {
-      typename gather::Cx<R>::T o;
-      o.x = (R)re;
-      o.y = (R)im;
-      static_cast<typename gather::Cx<R>::T*>(vals)[sl.dst_val] = o;
+  if constexpr (std::is_same<R, gather::DF>::value) {
+    const float2 a = split_rn(REALV ? sv : re), b = split_rn(im);
+    if (sl.dst_val >= 0) {
+      if constexpr (REALV)
+        static_cast<float2*>(vals)[sl.dst_val] = a;
+      else
+        static_cast<float4*>(vals)[sl.dst_val] = make_float4(a.x, a.y, b.x, b.y);
     }
-  }
-  if (sl.dst_ell >= 0) {
-    if constexpr (sizeof(R) == 8 && REALV) {
-      static_cast<EllD*>(ell)[sl.dst_ell].v = sv;
-    } else if constexpr (sizeof(R) == 8) {
-      EllZ& e = static_cast<EllZ*>(ell)[sl.dst_ell];
-      e.v[0] = re;
-      e.v[1] = im;
-    } else if constexpr (REALV) {
-      static_cast<EllF*>(ell)[sl.dst_ell].v = (float)sv;
-    } else {
-      EllC& e = static_cast<EllC*>(ell)[sl.dst_ell];
-      e.v[0] = (float)re;
-      e.v[1] = (float)im;
+    if (sl.dst_ell >= 0) {
+      if constexpr (REALV) {
+        EllDF& e = static_cast<EllDF*>(ell)[sl.dst_ell];
+        e.v[0] = a.x;
+        e.v[1] = a.y;
+      } else {
+        EllZF& e = static_cast<EllZF*>(ell)[sl.dst_ell];
+        e.v[0] = a.x;
+        e.v[1] = a.y;
+        e.v[2] = b.x;
+        e.v[3] = b.y;
+      }
+    }
+  } else {
+    if (sl.dst_val >= 0) {
+      if constexpr (REALV) {
+        static_cast<R*>(vals)[sl.dst_val] = (R)sv;
+      } else {
+        typename gather::Cx<R>::T o;
+        o.x = (R)re;
+        o.y = (R)im;
+        static_cast<typename gather::Cx<R>::T*>(vals)[sl.dst_val] = o;
+      }
+    }
+    if (sl.dst_ell >= 0) {
+      if constexpr (sizeof(R) == 8 && REALV) {
+        static_cast<EllD*>(ell)[sl.dst_ell].v = sv;
+      } else if constexpr (sizeof(R) == 8) {
+        EllZ& e = static_cast<EllZ*>(ell)[sl.dst_ell];
+        e.v[0] = re;
+        e.v[1] = im;
+      } else if constexpr (REALV) {
+        static_cast<EllF*>(ell)[sl.dst_ell].v = (float)sv;
+      } else {
+        EllC& e = static_cast<EllC*>(ell)[sl.dst_ell];
+        e.v[0] = (float)re;
+        e.v[1] = (float)im;
+      }
     }
   }
 }
@@ -127,7 +195,12 @@ void launch_td_values(const GatherPlan& g, const double2* factors_dev, cudaStrea
   const TdTerm* te = (const TdTerm*)g.td_terms.p;
   double2* dt = (double2*)g.dvals.p;
   const bool store_real = g.real_vals || g.phased;
-  if (g.precision == QOB_C128) {
+  if (g.ff) {
+    if (store_real)
+      k_td_values<gather::DF, true><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, step, off, nf, g.vals.p, g.ell.p, dt);
+    else
+      k_td_values<gather::DF, false><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, step, off, nf, g.vals.p, g.ell.p, dt);
+  } else if (g.precision == QOB_C128) {
     if (store_real)
       k_td_values<double, true><<<blocks, threads, 0, s>>>(g.td_nslots, sl, co, te, factors_dev, step, off, nf, g.vals.p, g.ell.p, dt);
     else
@@ -152,9 +225,18 @@ int gather_tile(const GatherPlan& g, int64_t ncols) {
 
 void launch_gather(const GatherPlan& g, int precision, const void* x, int64_t xes, int64_t xcs,
                    void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta,
-                   cudaStream_t s) {
+                   cudaStream_t s, int64_t n, void* ff_x) {
   GatherView v = g.view();
   const int tc = gather_tile(g, ncols);
+  if (g.ff) {
+    // split x once; the gather then reads the quadruples with x's strides
+    if (!ff_x || n <= 0) fail(QOB_ERR_ARG, "double-float gather without split buffer");
+    const int64_t total = n * ncols;
+    const unsigned blocks = (unsigned)((total + 256 * kSplitPer - 1) / (256 * kSplitPer));
+    k_ff_split<<<blocks, 256, 0, s>>>(static_cast<const double2*>(x), n, ncols, xes, xcs, static_cast<float4*>(ff_x));
+    QOB_LAUNCHED();
+    x = ff_x;
+  }
   // groups beyond one launch's shared-memory budget go in further launches
   // that accumulate into y (beta = 1, no diagonal)
   int g0 = 0;
@@ -167,7 +249,9 @@ void launch_gather(const GatherPlan& g, int precision, const void* x, int64_t xe
     c.has_diag = first ? v.has_diag : 0;
     if (v.ngroups > kGroupsPerLaunch) c.ell_slots = 0;  // chunks read their slots from global memory
     const c128 b = first ? beta : c128{1.0, 0.0};
-    if (precision == QOB_C128)
+    if (g.ff)
+      gather::dispatch<gather::DF>(c, g.sites, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, b, s);
+    else if (precision == QOB_C128)
       gather::dispatch<double>(c, g.sites, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, b, s);
     else
       gather::dispatch<float>(c, g.sites, tc, x, xes, xcs, y, yes, ycs, ncols, alpha, b, s);
@@ -181,7 +265,12 @@ void launch_build_diag(const GatherPlan& g, cudaStream_t s) {
   const unsigned blocks = (unsigned)((g.m + threads - 1) / threads);
   const GGroup* dg = (const GGroup*)g.dgroups.p;
   const double2* dt = (const double2*)g.dvals.p;
-  if (g.precision == QOB_C128) {
+  if (g.ff) {
+    if (g.real_vals)
+      k_build_diag<gather::DF, true><<<blocks, threads, 0, s>>>(g.m, g.ndgroups, dg, dt, g.diag.p);
+    else
+      k_build_diag<gather::DF, false><<<blocks, threads, 0, s>>>(g.m, g.ndgroups, dg, dt, g.diag.p);
+  } else if (g.precision == QOB_C128) {
     if (g.real_vals)
       k_build_diag<double, true><<<blocks, threads, 0, s>>>(g.m, g.ndgroups, dg, dt, g.diag.p);
     else

@@ -26,7 +26,12 @@
 // FP64 keeps the reference's arithmetic type; with real merged values (all
 // the Hamiltonians built from number/ladder/Pauli factors with real
 // coefficients) each stored entry costs two DFMA per vector.  FP32 mode adds
-// Kahan compensation across the accumulated contributions.
+// Kahan compensation across the accumulated contributions.  The double-float
+// mode (R = DF) reads and writes ComplexF64 data but does the arithmetic as
+// pairs of FP32 numbers on the FP32 pipes, which on GB300 issue 64x the FP64
+// rate: x is split once into (hi, lo) float pairs by k_ff_split, the stored
+// values are (hi, lo) pairs, and y is joined back to double by integer
+// instructions.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -46,6 +51,9 @@ __device__ __forceinline__ uint32_t fmodu(uint32_t n, uint32_t d, uint64_t M) {
   return (uint32_t)__umul64hi(low, (uint64_t)d);
 }
 
+// Precision tag of the double-float mode: ComplexF64 data, FP32-pair arithmetic.
+struct DF {};
+
 template <typename R>
 struct Cx;
 template <>
@@ -55,6 +63,21 @@ struct Cx<double> {
 template <>
 struct Cx<float> {
   using T = float2;
+};
+template <>
+struct Cx<DF> {
+  using T = double2;  // y and alpha / beta: ComplexF64
+};
+
+// element type of the input vectors as the kernels read them: the data type,
+// or for DF the (re hi, re lo, im hi, im lo) quadruple written by k_ff_split
+template <typename R>
+struct In {
+  using T = typename Cx<R>::T;
+};
+template <>
+struct In<DF> {
+  using T = float4;
 };
 
 template <typename R, int VM>
@@ -68,6 +91,14 @@ struct Val<double, true> {
 template <>
 struct Val<float, true> {
   using T = float;
+};
+template <>
+struct Val<DF, true> {
+  using T = float2;  // (hi, lo)
+};
+template <>
+struct Val<DF, false> {
+  using T = float4;  // (re hi, re lo, im hi, im lo)
 };
 
 // fixed-width slot type per precision / realness, and its value
@@ -93,6 +124,16 @@ struct Ell<float, false> {
   using T = EllC;
   static __device__ __forceinline__ float2 v(const EllC& e) { return make_float2(e.v[0], e.v[1]); }
 };
+template <>
+struct Ell<DF, true> {
+  using T = EllDF;
+  static __device__ __forceinline__ float2 v(const EllDF& e) { return make_float2(e.v[0], e.v[1]); }
+};
+template <>
+struct Ell<DF, false> {
+  using T = EllZF;
+  static __device__ __forceinline__ float4 v(const EllZF& e) { return make_float4(e.v[0], e.v[1], e.v[2], e.v[3]); }
+};
 
 // Value modes of a plan: complex entries; real entries (and a real diagonal);
 // real entries of groups that are either real or purely imaginary, with a
@@ -109,6 +150,9 @@ __device__ __forceinline__ bool nz(double2 v) {
   return ((unsigned long long)(__double_as_longlong(v.x) | __double_as_longlong(v.y)) << 1) != 0ull;
 }
 __device__ __forceinline__ bool nz(float2 v) { return ((__float_as_uint(v.x) | __float_as_uint(v.y)) << 1) != 0u; }
+__device__ __forceinline__ bool nz(float4 v) {
+  return ((__float_as_uint(v.x) | __float_as_uint(v.y) | __float_as_uint(v.z) | __float_as_uint(v.w)) << 1) != 0u;
+}
 
 // FP64 accumulator: plain fused multiply-adds.
 struct AccD {
@@ -175,6 +219,121 @@ struct AccF {
   __device__ float2 total() const { return make_float2(re - cre, im - cim); }
 };
 
+// ---- double-float arithmetic (Dekker 1971; Knuth, TAOCP vol. 2, 4.2.2) ----
+// A value is the unevaluated sum hi + lo of two floats.
+
+// double -> (hi, lo) with integer instructions only: hi = the double truncated
+// to 24 significant bits (exact), lo = the remaining 29 bits rounded to 24, so
+// hi + lo is within 2^-48 relative of d.  Magnitudes in [2^-74, 2^128) keep
+// both parts; in [2^-126, 2^-74) lo is dropped; below 2^-126 the value
+// flushes to zero; above, hi is infinite (NaN stays NaN).
+__device__ __forceinline__ float2 ff_split(double d) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+  const uint32_t H = (uint32_t)(u >> 32), L = (uint32_t)u;
+  const uint32_t sgn = H & 0x80000000u, ma = H & 0x7fffffffu;
+  const uint32_t e = ma >> 20;  // biased binary exponent of the double
+  float hi, lo;
+  if (e >= 897u && e <= 1150u) {
+    hi = __uint_as_float(sgn | ((ma - 0x38000000u) << 3) | (L >> 29));
+  } else if (e > 1150u) {
+    const bool nan = e == 2047u && ((ma & 0xfffffu) | L) != 0u;
+    hi = __uint_as_float(sgn | 0x7f800000u | (nan ? 0x400000u : 0u));
+  } else {
+    hi = __uint_as_float(sgn);
+  }
+  if (e >= 949u && e <= 1150u) {
+    // (L mod 2^29) * 2^(e - 1075); the power of two is a float with exponent field e - 948
+    lo = __uint2float_rn(L & 0x1fffffffu) * __uint_as_float((e - 948u) << 23);
+    lo = __uint_as_float(__float_as_uint(lo) | sgn);
+  } else {
+    lo = 0.f;
+  }
+  return make_float2(hi, lo);
+}
+
+// (hi, lo) -> double with integer instructions: renormalise with a two-sum,
+// write hi's bits as a double and add lo in units of the double's last place.
+__device__ __forceinline__ double ff_join(float h, float l) {
+  const float s = h + l;
+  const float bb = s - h;
+  const float e = (h - (s - bb)) + (l - bb);  // s + e == h + l, |e| <= ulp(s) / 2
+  const uint32_t S = __float_as_uint(s);
+  const uint32_t E = (S >> 23) & 0xffu, M = S & 0x7fffffu;
+  const unsigned long long sgn = (unsigned long long)(S & 0x80000000u) << 32;
+  if (E == 0u) return __longlong_as_double((long long)sgn);  // zero (subnormal floats flush)
+  if (E == 255u)
+    return __longlong_as_double((long long)(sgn | 0x7ff0000000000000ull | (M ? 0x8000000000000ull : 0ull)));
+  unsigned long long mag = ((unsigned long long)(E + 896u) << 52) | ((unsigned long long)M << 29);
+  if (E >= 53u) {
+    // e in units of the double's last place at s (2^(E - 179)); half that when
+    // s is a power of two and e points below it (the next lower binade); the
+    // scale 2^(179 - E) or 2^(180 - E) is a normal float for E >= 53, and
+    // below that (|s| < 2^-74) e is dropped
+    const bool toward = (__float_as_uint(e) ^ S) & 0x80000000u;
+    const uint32_t sc = (M == 0u && toward) ? (307u - E) : (306u - E);
+    const int n = __float2int_rn(fabsf(e) * __uint_as_float(sc << 23));
+    mag = toward ? mag - (unsigned long long)n : mag + (unsigned long long)n;
+  }
+  return __longlong_as_double((long long)(sgn | mag));
+}
+
+// product of two double-float numbers (the lo * lo term is below 2^-48)
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
+  const float p = a.x * b.x;
+  float pe = __fmaf_rn(a.x, b.x, -p);
+  pe = __fmaf_rn(a.x, b.y, pe);
+  pe = __fmaf_rn(a.y, b.x, pe);
+  return make_float2(p, pe);
+}
+__device__ __forceinline__ float2 ff_neg(float2 a) { return make_float2(-a.x, -a.y); }
+
+// Double-float accumulator of one complex value: acc += v * x with the
+// product error (FMA) and the addition error (two-sum) carried in the low parts.
+struct AccFF {
+  float rh, rl, ih, il;
+  static __device__ __forceinline__ void madd(float& h, float& l, float2 v, float xh, float xl) {
+    const float p = v.x * xh;
+    float pe = __fmaf_rn(v.x, xh, -p);
+    pe = __fmaf_rn(v.x, xl, pe);
+    pe = __fmaf_rn(v.y, xh, pe);
+    const float s = h + p;
+    const float bb = s - h;
+    const float err = (h - (s - bb)) + (p - bb);
+    l = l + (err + pe);
+    h = s;
+  }
+  __device__ void zero() { rh = rl = ih = il = 0.f; }
+  __device__ void mac(float2 v, float4 x) {
+    madd(rh, rl, v, x.x, x.y);
+    madd(ih, il, v, x.z, x.w);
+  }
+  // (i v) x for real v
+  __device__ void mac_i(float2 v, float4 x) {
+    madd(rh, rl, ff_neg(v), x.z, x.w);
+    madd(ih, il, v, x.x, x.y);
+  }
+  __device__ void mac(float4 v, float4 x) {
+    const float2 vr = make_float2(v.x, v.y), vi = make_float2(v.z, v.w);
+    madd(rh, rl, vr, x.x, x.y);
+    madd(rh, rl, ff_neg(vi), x.z, x.w);
+    madd(ih, il, vr, x.z, x.w);
+    madd(ih, il, vi, x.x, x.y);
+  }
+  __device__ void mac_i(float4 v, float4 x) { mac(make_float4(-v.z, -v.w, v.x, v.y), x); }
+  __device__ void set(float2 v, float4 x) {
+    const float2 r = ff_mul(v, make_float2(x.x, x.y)), i = ff_mul(v, make_float2(x.z, x.w));
+    rh = r.x;
+    rl = r.y;
+    ih = i.x;
+    il = i.y;
+  }
+  __device__ void set(float4 v, float4 x) {
+    zero();
+    mac(v, x);
+  }
+  __device__ float4 total() const { return make_float4(rh, rl, ih, il); }
+};
+
 template <typename R>
 struct AccOf;
 template <>
@@ -185,9 +344,14 @@ template <>
 struct AccOf<float> {
   using T = AccF;
 };
+template <>
+struct AccOf<DF> {
+  using T = AccFF;
+};
 
 __device__ __forceinline__ double2 ld(const double2* p) { return __ldg(p); }
 __device__ __forceinline__ float2 ld(const float2* p) { return __ldg(p); }
+__device__ __forceinline__ float4 ld(const float4* p) { return __ldg(p); }
 
 // y = alpha * acc + beta * y with the reference's beta semantics:
 // BMODE 0: beta == 0 (y is not read), 2: general complex beta, 3: real beta.
@@ -220,6 +384,15 @@ __device__ __forceinline__ void combine(float2* yp, float2 a, float2 alpha, floa
     im = __fmaf_rn(beta.x, o.y, im);
   }
   *yp = make_float2(re, im);
+}
+
+// double-float: acc = (re hi, re lo, im hi, im lo), joined to double by
+// integer instructions; alpha * acc + beta * y then in FP64 like the ComplexF64
+// kernels (six FP64 operations per element, on the pipe the FP32-pair gather
+// leaves idle)
+template <int BMODE>
+__device__ __forceinline__ void combine(double2* yp, float4 a, double2 alpha, double2 beta) {
+  combine<BMODE>(yp, make_double2(ff_join(a.x, a.y), ff_join(a.z, a.w)), alpha, beta);
 }
 
 // Copy the group descriptors (then, for plans with the compact form, one int4
@@ -324,12 +497,12 @@ __device__ __forceinline__ bool group_row(const GGroup& G, const SiteTable& st, 
 template <typename R, int VM, bool SQUARE, bool W1, int TC>
 __device__ __forceinline__ void accumulate(const GatherView& g, const SiteTable& st, const GGroup* sg,
                                            const typename Ell<R, VM != kComplex>::T* ell, uint32_t J,
-                                           const typename Cx<R>::T* xb, int64_t es, int64_t xcs, int nt,
+                                           const typename In<R>::T* xb, int64_t es, int64_t xcs, int nt,
                                            typename AccOf<R>::T (&acc)[TC]) {
   using VT = typename Val<R, VM != kComplex>::T;  // stored entries
   using DT = typename Val<R, VM == kReal>::T;     // merged diagonal
   using ET = typename Ell<R, VM != kComplex>::T;
-  using CT = typename Cx<R>::T;
+  using CT = typename In<R>::T;
   if (g.has_diag) {
     const DT d = static_cast<const DT*>(g.diag)[J];
     const CT* xp = xb + (int64_t)J * es;
@@ -438,10 +611,11 @@ __device__ __forceinline__ void accumulate(const GatherView& g, const SiteTable&
 // the vectors are contiguous (element stride 1).
 template <typename R, int VM, bool SQUARE, bool W1, int TC, int BMODE>
 __global__ void __launch_bounds__(256) k_gather_j(GatherView g, SiteTable st,
-                                                  const typename Cx<R>::T* __restrict__ x, int64_t xcs,
+                                                  const typename In<R>::T* __restrict__ x, int64_t xcs,
                                                   typename Cx<R>::T* __restrict__ y, int64_t ycs, int ncols,
                                                   typename Cx<R>::T alpha, typename Cx<R>::T beta) {
   using CT = typename Cx<R>::T;
+  using XT = typename In<R>::T;
   using AT = typename AccOf<R>::T;
   using ET = typename Ell<R, VM != kComplex>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -461,7 +635,7 @@ __global__ void __launch_bounds__(256) k_gather_j(GatherView g, SiteTable st,
   const int nt = c0 < ncols ? min(TC, (ncols - c0 + ls - 1) / ls) : 0;
   if (nt <= 0) return;
   const int64_t vs_x = (int64_t)ls * xcs, vs_y = (int64_t)ls * ycs;
-  const CT* xb = x + (int64_t)c0 * xcs;
+  const XT* xb = x + (int64_t)c0 * xcs;
   AT acc[TC];
   accumulate<R, VM, SQUARE, W1, TC>(g, st, sg, ell, (uint32_t)J, xb, 1, vs_x, nt, acc);
   CT* yb = y + J + (int64_t)c0 * ycs;
@@ -479,10 +653,11 @@ __global__ void __launch_bounds__(256) k_gather_j(GatherView g, SiteTable st,
 // block.
 template <typename R, int VM, bool SQUARE, bool W1, int TC, int BMODE>
 __global__ void __launch_bounds__(256) k_gather_p(GatherView g, SiteTable st,
-                                                  const typename Cx<R>::T* __restrict__ x, int64_t xcs,
+                                                  const typename In<R>::T* __restrict__ x, int64_t xcs,
                                                   typename Cx<R>::T* __restrict__ y, int64_t ycs, int ncols,
                                                   typename Cx<R>::T alpha, typename Cx<R>::T beta) {
   using CT = typename Cx<R>::T;
+  using XT = typename In<R>::T;
   using AT = typename AccOf<R>::T;
   using ET = typename Ell<R, VM != kComplex>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -499,7 +674,7 @@ __global__ void __launch_bounds__(256) k_gather_p(GatherView g, SiteTable st,
     if (J >= g.m) continue;
     const int c0 = (int)tile * TC;
     const int nt = min(TC, ncols - c0);
-    const CT* xb = x + (int64_t)c0 * xcs;
+    const XT* xb = x + (int64_t)c0 * xcs;
     AT acc[TC];
     accumulate<R, VM, SQUARE, W1, TC>(g, st, sg, ell, (uint32_t)J, xb, 1, xcs, nt, acc);
     CT* yb = y + J + (int64_t)c0 * ycs;
@@ -514,7 +689,7 @@ __global__ void __launch_bounds__(256) k_gather_p(GatherView g, SiteTable st,
 // all threads of a block share one output index J.
 template <typename R, int VM, bool SQUARE, int BMODE>
 __global__ void __launch_bounds__(256) k_gather_c(GatherView g, SiteTable st,
-                                                  const typename Cx<R>::T* __restrict__ x, int64_t xes,
+                                                  const typename In<R>::T* __restrict__ x, int64_t xes,
                                                   int64_t xcs, typename Cx<R>::T* __restrict__ y,
                                                   int64_t yes, int64_t ycs, int ncols, typename Cx<R>::T alpha,
                                                   typename Cx<R>::T beta) {
@@ -551,6 +726,7 @@ template <typename R, int VM, bool SQUARE, bool W1, int TC, int BMODE>
 void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t xcs, void* y, int64_t ycs,
               int64_t ncols, typename Cx<R>::T a, typename Cx<R>::T b, size_t smem, cudaStream_t s) {
   using CT = typename Cx<R>::T;
+  using XT = typename In<R>::T;
   if (v.block < 0 && ncols <= (int64_t)INT32_MAX) {
     // persistent grid: SMs x resident blocks of -v.block threads
     auto pk = k_gather_p<R, VM, SQUARE, W1, TC, BMODE>;
@@ -563,7 +739,7 @@ void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t x
     if (occ > 0) {
       GatherView w = v;
       w.jmul = chunk_multiplier((v.m + 31) / 32);
-      pk<<<(unsigned)(sms * occ), threads, smem, s>>>(w, st, (const CT*)x, xcs, (CT*)y, ycs, (int)ncols, a, b);
+      pk<<<(unsigned)(sms * occ), threads, smem, s>>>(w, st, (const XT*)x, xcs, (CT*)y, ycs, (int)ncols, a, b);
       QOB_LAUNCHED();
       return;
     }
@@ -584,7 +760,7 @@ void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t x
   for (int64_t c0 = 0; c0 < ncols; c0 += (int64_t)65535 * per_y) {  // grid.y limit
     const int64_t nc = std::min<int64_t>(ncols - c0, (int64_t)65535 * per_y);
     kern<<<dim3(gx, (unsigned)((nc + per_y - 1) / per_y)), threads, smem, s>>>(
-        w, st, (const CT*)x + c0 * xcs, xcs, (CT*)y + c0 * ycs, ycs, (int)nc, a, b);
+        w, st, (const XT*)x + c0 * xcs, xcs, (CT*)y + c0 * ycs, ycs, (int)nc, a, b);
     QOB_LAUNCHED();
   }
 }
@@ -612,6 +788,7 @@ void dispatch_layout(const GatherView& v, const SiteTable& st, int tc, const voi
                      int64_t xcs, void* y, int64_t yes, int64_t ycs, int64_t ncols, typename Cx<R>::T a, typename Cx<R>::T b,
                      cudaStream_t s) {
   using CT = typename Cx<R>::T;
+  using XT = typename In<R>::T;
   using ET = typename Ell<R, VM != kComplex>::T;
   GatherView w = v;
   size_t smem = (size_t)v.ngroups * (sizeof(GGroup) + (v.fast ? sizeof(int4) : 0));
@@ -630,7 +807,7 @@ void dispatch_layout(const GatherView& v, const SiteTable& st, int tc, const voi
     for (int64_t c0 = 0; c0 < ncols; c0 += (int64_t)65535 * threads) {  // grid.y limit
       const int64_t nc = std::min<int64_t>(ncols - c0, (int64_t)65535 * threads);
       dim3 grid((unsigned)v.m, (unsigned)((nc + threads - 1) / threads));
-      kern<<<grid, threads, smem, s>>>(w, st, (const CT*)x + c0 * xcs, xes, xcs, (CT*)y + c0 * ycs, yes, ycs,
+      kern<<<grid, threads, smem, s>>>(w, st, (const XT*)x + c0 * xcs, xes, xcs, (CT*)y + c0 * ycs, yes, ycs,
                                        (int)nc, a, b);
       QOB_LAUNCHED();
     }
@@ -641,10 +818,11 @@ template <typename R, int VM, bool SQUARE>
 void dispatch_beta(const GatherView& v, const SiteTable& st, int tc, const void* x, int64_t xes, int64_t xcs,
                    void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta, cudaStream_t s) {
   typename Cx<R>::T a, b;
-  a.x = (R)alpha.re;
-  a.y = (R)alpha.im;
-  b.x = (R)beta.re;
-  b.y = (R)beta.im;
+  using S = decltype(a.x);
+  a.x = (S)alpha.re;
+  a.y = (S)alpha.im;
+  b.x = (S)beta.re;
+  b.y = (S)beta.im;
   if (beta.re == 0.0 && beta.im == 0.0)
     dispatch_layout<R, VM, SQUARE, 0>(v, st, tc, x, xes, xcs, y, yes, ycs, ncols, a, b, s);
   else if (beta.im == 0.0)

@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <tuple>
 
 #include "qob_internal.h"
 
@@ -495,8 +496,26 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
   upload_vec(gp.groups, descs);
   upload_vec(gp.rowptr, rowptr);
   upload_vec(gp.coloff, coloff);
-  // values in the plan precision, real or complex
-  if (precision == QOB_C128) {
+  // values in the plan precision, real or complex; double-float plans store
+  // (hi, lo) float pairs in the same sizes
+  auto split = [](double v) {
+    const float h = (float)v;
+    return std::pair<float, float>(h, (float)(v - (double)h));
+  };
+  if (gp.ff) {
+    if (store_real) {
+      std::vector<float> v(2 * vals.size());
+      for (size_t i = 0; i < vals.size(); ++i) std::tie(v[2 * i], v[2 * i + 1]) = split(vals[i].re);
+      upload_vec(gp.vals, v);
+    } else {
+      std::vector<float> v(4 * vals.size());
+      for (size_t i = 0; i < vals.size(); ++i) {
+        std::tie(v[4 * i], v[4 * i + 1]) = split(vals[i].re);
+        std::tie(v[4 * i + 2], v[4 * i + 3]) = split(vals[i].im);
+      }
+      upload_vec(gp.vals, v);
+    }
+  } else if (precision == QOB_C128) {
     if (store_real) {
       std::vector<double> v(vals.size());
       for (size_t i = 0; i < vals.size(); ++i) v[i] = vals[i].re;
@@ -517,7 +536,24 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
   }
   // fixed-width slots in the plan precision
   gp.ell_slots = (int32_t)ell.size();
-  if (precision == QOB_C128) {
+  if (gp.ff) {
+    if (store_real) {
+      std::vector<EllDF> e(ell.size());
+      for (size_t i = 0; i < ell.size(); ++i) {
+        e[i] = {ell[i].col, 0, {0.f, 0.f}};
+        std::tie(e[i].v[0], e[i].v[1]) = split(ell[i].v.re);
+      }
+      upload_vec(gp.ell, e);
+    } else {
+      std::vector<EllZF> e(ell.size());
+      for (size_t i = 0; i < ell.size(); ++i) {
+        e[i] = {ell[i].col, {0, 0, 0}, {0.f, 0.f, 0.f, 0.f}};
+        std::tie(e[i].v[0], e[i].v[1]) = split(ell[i].v.re);
+        std::tie(e[i].v[2], e[i].v[3]) = split(ell[i].v.im);
+      }
+      upload_vec(gp.ell, e);
+    }
+  } else if (precision == QOB_C128) {
     if (store_real) {
       std::vector<EllD> e(ell.size());
       for (size_t i = 0; i < ell.size(); ++i) e[i] = {ell[i].col, 0, ell[i].v.re};
@@ -600,7 +636,7 @@ static std::unique_ptr<Plan> compile_sum(Context& ctx, const NodeP& root, int si
   auto P = std::make_unique<Plan>();
   P->kind = Plan::Kind::Sum;
   P->side = side;
-  P->precision = precision;
+  P->precision = precision == QOB_C128X ? QOB_C128 : precision;
   const bool tr = (side == QOB_RIGHT);
   P->m = tr ? root->n : root->m;  // output vector length
   P->n = tr ? root->m : root->n;  // input vector length
@@ -687,7 +723,7 @@ static std::unique_ptr<Plan> compile_sum(Context& ctx, const NodeP& root, int si
             std::vector<c128> a(st.dout * st.din, c128{0.0, 0.0});
             for (int64_t row = 0; row < r.rows; ++row)
               for (int64_t p = r.ptr[row]; p < r.ptr[row + 1]; ++p) a[row + r.col[p] * st.dout] = r.val[p];
-            if (precision == QOB_C128) {
+            if (P->precision == QOB_C128) {
               upload_vec(st.a, a);
             } else {
               std::vector<c64> a32(a.size());
@@ -739,7 +775,7 @@ static std::unique_ptr<Plan> compile_sum(Context& ctx, const NodeP& root, int si
                 v = nd->vals[r + c * nd->sm];
               a[i + j * dp.m] = v;
             }
-          if (precision == QOB_C128) {
+          if (P->precision == QOB_C128) {
             upload_vec(dp.a, a);
           } else {
             std::vector<c64> a32(a.size());
@@ -789,7 +825,8 @@ static void finalize_gather(GatherPlan& gp, GatherBuilder& B, const OpNode* root
                             int64_t m, int64_t n) {
   gp.m = m;
   gp.n = n;
-  gp.precision = precision;
+  gp.precision = precision == QOB_C128X ? QOB_C128 : precision;
+  gp.ff = precision == QOB_C128X;
   gp.terms = B.terms;
   auto hp = std::make_shared<GatherHost>();
   GatherHost& H = *hp;
@@ -840,17 +877,20 @@ static void finalize_gather(GatherPlan& gp, GatherBuilder& B, const OpNode* root
   }
   for (auto& g : B.groups) H.groups.push_back(g);
   std::vector<c128> val = eval_slots(H, gp.terms, root);
-  upload_structure(gp, H, val, precision);
+  upload_structure(gp, H, val, gp.precision);
   gp.host_rec = hp;
 }
 
+// precision QOB_C128X: a ComplexF64 plan (P->precision QOB_C128) whose fused
+// gathers store and apply their values in double-float arithmetic
 std::unique_ptr<Plan> compile_plan(Context& ctx, const NodeP& op, int side, int precision) {
-  if (op->kind == Kind::Fft) return compile_fft(op, side, precision);
+  const int layout = precision == QOB_C128X ? QOB_C128 : precision;
+  if (op->kind == Kind::Fft) return compile_fft(op, side, layout);
   if (op->kind == Kind::LazyProduct) {
     auto P = std::make_unique<Plan>();
     P->kind = Plan::Kind::Product;
     P->side = side;
-    P->precision = precision;
+    P->precision = layout;
     const bool tr = (side == QOB_RIGHT);
     P->m = tr ? op->n : op->m;
     P->n = tr ? op->m : op->n;

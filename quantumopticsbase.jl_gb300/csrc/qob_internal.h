@@ -129,6 +129,17 @@ struct EllC {  // FP32, complex value
   int32_t pad;
   float v[2];
 };
+struct EllDF {  // double-float, real value (hi, lo): the size of EllD
+  int32_t col;
+  int32_t pad;
+  float v[2];
+};
+struct EllZF {  // double-float, complex value (re hi, re lo, im hi, im lo): the size of EllZ
+  int32_t col;
+  int32_t pad[3];
+  float v[4];
+};
+static_assert(sizeof(EllDF) == sizeof(EllD) && sizeof(EllZF) == sizeof(EllZ), "double-float slots keep the FP64 sizes");
 
 static_assert(sizeof(GGroup) % 16 == 0,
               "GGroup is copied to shared memory in 8-byte words and the 16-byte items staged after the "
@@ -234,6 +245,7 @@ struct GatherPlan {
   bool square = true;
   bool real_vals = true;
   bool phased = false;  // real stored values, per-group imag flags, complex diagonal
+  bool ff = false;      // ComplexF64 plan whose values are stored and applied as double-float pairs
   bool has_diag = false;
   int precision = QOB_C128;
   int ngroups = 0;
@@ -367,9 +379,11 @@ void device_refresh(GatherPlan& g, const double2* factors_dev, cudaStream_t s, c
                     long long off = 0, long long nf = 0);
 
 // kernels (launchers)
+// ff_x: for a double-float plan, room for the split input (the span of x's
+// elements, 16 bytes each); unused otherwise.  n = x's length.
 void launch_gather(const GatherPlan& g, int precision, const void* x, int64_t xes, int64_t xcs,
                    void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta,
-                   cudaStream_t s);
+                   cudaStream_t s, int64_t n = 0, void* ff_x = nullptr);
 void launch_build_diag(const GatherPlan& g, cudaStream_t s);
 // Factors at factors_dev, or, with a device step counter, at row 2 * *step + off
 // of the table factors_dev (nf factors per row).
@@ -433,5 +447,5 @@ struct qob_ctx {
 };
 struct qob_op {
   qob::NodeP node;
-  std::unique_ptr<qob::Plan> plans[2][2];  // [side][precision]
+  std::unique_ptr<qob::Plan> plans[2][3];  // [side][dtype: QOB_C128, QOB_C64, QOB_C128X]
 };

@@ -22,6 +22,7 @@ QOB_ERR_TIMEOUT = 7
 QOB_ERR_STATE = 8
 QOB_C128 = 0
 QOB_C64 = 1
+QOB_C128X = 2  # ComplexF64 data, fused part in double-float arithmetic
 QOB_LEFT = 0
 QOB_RIGHT = 1
 

@@ -67,6 +67,10 @@ class Handle:
 
 
 def dtype_code(dt) -> int:
+    """numpy complex128 / complex64, or "ff" for ComplexF64 data applied in
+    double-float arithmetic (QOB_C128X)."""
+    if isinstance(dt, str) and dt == "ff":
+        return L.QOB_C128X
     return L.QOB_C64 if np.dtype(dt) == np.complex64 else L.QOB_C128
 
 

@@ -84,8 +84,18 @@ def _classify(result, a, b):
     return L.QOB_RIGHT, False, b, a.data, result.data
 
 
-def mul_(result, a, b, alpha=1.0, beta=0.0, device: int | None = None):
-    """In place ``result = alpha * a * b + beta * result``; returns ``result``."""
+def _code(ydt, arith):
+    if arith is None:
+        return dtype_code(ydt)
+    if arith != "ff" or ydt != np.complex128:
+        raise O.ArgumentError('arith="ff" (double-float) applies to ComplexF64 data')
+    return L.QOB_C128X
+
+
+def mul_(result, a, b, alpha=1.0, beta=0.0, device: int | None = None, arith: str | None = None):
+    """In place ``result = alpha * a * b + beta * result``; returns ``result``.
+    ``arith="ff"``: ComplexF64 data, the fused LazySum part in double-float
+    arithmetic on the FP32 pipes (about 1e-14 relative; QOB_C128X)."""
     side, is_vec, op, x, y = _classify(result, a, b)
     alpha, beta = complex(alpha), complex(beta)
     lib = L.lib()
@@ -106,7 +116,7 @@ def mul_(result, a, b, alpha=1.0, beta=0.0, device: int | None = None):
         if side == L.QOB_RIGHT and x.ndim == 1:
             xr, xc, xld = 1, x.shape[0], 1
             yr, yc, yld = 1, y.shape[0], 1
-        rc = lib.qob_mul(ctx.ptr, side, int(is_vec), h.ptr, dtype_code(ydt), alpha.real, alpha.imag,
+        rc = lib.qob_mul(ctx.ptr, side, int(is_vec), h.ptr, _code(ydt, arith), alpha.real, alpha.imag,
                          C.c_void_p(x.data_ptr()), xr, xc, xld, beta.real, beta.imag, C.c_void_p(y.data_ptr()),
                          yr, yc, yld, _stream_ptr(dev))
         raise_for(rc, ctx)
@@ -125,7 +135,7 @@ def mul_(result, a, b, alpha=1.0, beta=0.0, device: int | None = None):
     else:
         xr, xc = (1, xh.shape[0]) if xh.ndim == 1 else xh.shape
         yr, yc = (1, y.shape[0]) if y.ndim == 1 else y.shape
-    rc = lib.qob_mul_host(ctx.ptr, side, int(is_vec), h.ptr, dtype_code(ydt), alpha.real, alpha.imag,
+    rc = lib.qob_mul_host(ctx.ptr, side, int(is_vec), h.ptr, _code(ydt, arith), alpha.real, alpha.imag,
                           xh.ctypes.data_as(C.c_void_p), xr, xc, beta.real, beta.imag, y.ctypes.data_as(C.c_void_p),
                           yr, yc)
     raise_for(rc, ctx)
