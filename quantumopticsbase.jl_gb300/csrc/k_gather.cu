@@ -77,8 +77,12 @@ __global__ void __launch_bounds__(256) k_ff_split(const double2* __restrict__ x,
     const int64_t i = i0 + (int64_t)k * blockDim.x;
     o[k] = -1;
     if (i < total) {
-      const int64_t c = i / n, e = i - c * n;
-      o[k] = e * es + c * cs;
+      if (es == 1 && cs == n) {  // contiguous columns (kets): offset = index, no division
+        o[k] = i;
+      } else {
+        const int64_t c = i / n, e = i - c * n;
+        o[k] = e * es + c * cs;
+      }
       v[k] = __ldg(x + o[k]);
     }
   }

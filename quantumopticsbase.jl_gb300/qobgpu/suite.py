@@ -6,7 +6,8 @@ launch sequence) or, for the served stream, with the host clock around request
 submission and completion:
 
 * ``jc512``       Jaynes-Cummings LazySum, FockBasis(15) x Spin(1/2) x FockBasis(15),
-                  mul!(out, H, psi, 0.7-0.2i, 0.3) on one ket and on 64 kets;
+                  mul!(out, H, psi, 0.7-0.2i, 0.3) on one ket and on 64 kets (ComplexF64,
+                  ComplexF64 in double-float arithmetic, ComplexF32; also for ``lindblad``);
 * ``sparse4096``  sparse(H) of the 32 x 2 x 64 Jaynes-Cummings model: SpMV on a ket
                   and SpMM on 256 columns of a density matrix, FP64 and FP32;
 * ``rho_h8``      mul!(rho', rho, H) and mul!(rho', H, rho) with the 8-spin
@@ -58,6 +59,16 @@ def _timed_graph(ctx, stream, record, reps=20):
     return e0.elapsed_time(e1) / reps
 
 
+def _modes():
+    """(torch dtype, numpy dtype, dtype code, label): ComplexF64, ComplexF64 in
+    double-float arithmetic (QOB_C128X), ComplexF32."""
+    import torch
+
+    return ((torch.complex128, np.complex128, L.QOB_C128, "complex128"),
+            (torch.complex128, np.complex128, L.QOB_C128X, "complex128 double-float"),
+            (torch.complex64, np.complex64, L.QOB_C64, "complex64"))
+
+
 def _cols(n, k, dt, seed):
     import torch
 
@@ -92,14 +103,14 @@ def jc512(ctx, stream):
     H = jaynes_cummings(15, 15, seed=1)
     h = handle(ctx, H)
     out = []
-    for tdt, npdt in ((torch.complex128, np.complex128), (torch.complex64, np.complex64)):
+    for tdt, npdt, code, label in _modes():
         for ncols in (1, 64):
             x = _cols(512, ncols, tdt, 1)
             y = _cols(512, ncols, tdt, 2)
             reps = 50
-            ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, L.QOB_LEFT, 512, 512, ncols, x, y, dtype_code(npdt),
+            ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, L.QOB_LEFT, 512, 512, ncols, x, y, code,
                                                          reps=reps))
-            out.append({"dtype": np.dtype(npdt).name, "kets": ncols, "us_per_apply_call": ms * 1e3 / reps,
+            out.append({"dtype": label, "kets": ncols, "us_per_apply_call": ms * 1e3 / reps,
                         "applies_per_s": ncols * reps / (ms * 1e-3)})
     return {"workload": "jc512", "results": out}
 
@@ -199,21 +210,21 @@ def lindblad(ctx, stream):
         n2 = len(b) ** 2
         for form, L_ in forms:
             h = handle(ctx, L_.vectorised)
-            for tdt, npdt in ((torch.complex128, np.complex128), (torch.complex64, np.complex64)):
+            for tdt, npdt, code, label in _modes():
                 x = _cols(n2, 1, tdt, 30).contiguous()
                 y = _cols(n2, 1, tdt, 31).contiguous()
                 reps = 20
-                ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, L.QOB_LEFT, n2, n2, 1, x, y, dtype_code(npdt),
+                ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, L.QOB_LEFT, n2, n2, 1, x, y, code,
                                                              alpha=1.0 + 0j, beta=0.0, reps=reps))
                 t = ms * 1e-3 / reps
                 s = 16 if npdt == np.complex128 else 8
-                row = {"spins": nspins, "rho_dim": len(b), "form": form, "dtype": np.dtype(npdt).name,
+                row = {"spins": nspins, "rho_dim": len(b), "form": form, "dtype": label,
                        "us_per_apply": t * 1e6, "algorithmic_GBps": 2 * n2 * s / t / 1e9}
                 if form == "materialised":
                     row["nnz"] = int(L_.data.nnz)
                 else:
                     info = (C.c_int64 * 4)()
-                    raise_for(L.lib().qob_op_prepare(ctx.ptr, h.ptr, L.QOB_LEFT, dtype_code(npdt), info), ctx)
+                    raise_for(L.lib().qob_op_prepare(ctx.ptr, h.ptr, L.QOB_LEFT, code, info), ctx)
                     row["terms"] = len(L_.operator.operators)
                     row["groups"] = int(info[0])
                 out.append(row)
