@@ -47,9 +47,9 @@ __device__ __forceinline__ CT cm(CT a, CT b) {
 // lines of one vector); p = lo + stride * hi with lo < stride.
 __device__ __forceinline__ int64_t line_base(int64_t line, int64_t lines_per_vec, int64_t stride, int64_t n,
                                              int64_t es, int64_t cs) {
-  const int64_t c = line / lines_per_vec;
-  const int64_t p = line - c * lines_per_vec;
-  const int64_t lo = p % stride, hi = p / stride;
+  int64_t c, p, lo, hi;
+  udivmod(line, lines_per_vec, c, p);
+  udivmod(p, stride, hi, lo);
   return c * cs + (lo + hi * stride * n) * es;
 }
 
@@ -137,7 +137,8 @@ __global__ void __launch_bounds__(256) k_fft4_a(int64_t n1, int log2n1, int64_t 
   __syncthreads();
   const CT* r = stockham(a, b, n1, log2n1, twn, n2);
   CT* out = scratch + line * n;
-  for (int64_t k1 = threadIdx.x; k1 < n1; k1 += blockDim.x) out[j2 + n2 * k1] = cm(r[k1], twn[(j2 * k1) % n]);
+  // n is a power of two on this path: the twiddle index wraps with a mask
+  for (int64_t k1 = threadIdx.x; k1 < n1; k1 += blockDim.x) out[j2 + n2 * k1] = cm(r[k1], twn[(j2 * k1) & (n - 1)]);
 }
 
 template <typename CT, int BMODE>

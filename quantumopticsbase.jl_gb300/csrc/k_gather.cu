@@ -80,7 +80,8 @@ __global__ void __launch_bounds__(256) k_ff_split(const double2* __restrict__ x,
       if (es == 1 && cs == n) {  // contiguous columns (kets): offset = index, no division
         o[k] = i;
       } else {
-        const int64_t c = i / n, e = i - c * n;
+        int64_t c, e;
+        udivmod(i, n, c, e);
         o[k] = e * es + c * cs;
       }
       v[k] = __ldg(x + o[k]);

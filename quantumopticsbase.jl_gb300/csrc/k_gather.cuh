@@ -625,15 +625,21 @@ __global__ void __launch_bounds__(256) k_gather_j(GatherView g, SiteTable st,
   // interleaved sets of TC vectors (vectors q, q + ls, ...), so operator
   // entries that vary with the low index bits diverge over fewer lanes; each
   // load still reads whole 32-byte sectors (32/ls consecutive elements per vector)
+  // (ls is a power of two: shifts and masks, no integer division, which would
+  // cost more than the work of a thread with one vector and few groups)
   const int ls = g.lane_split;
-  const int jw = 32 / ls;
+  const int lsh = __ffs(ls) - 1;  // log2(ls)
+  const int jsh = 5 - lsh;        // log2(32 / ls)
   const int lane = threadIdx.x & 31;
-  const int64_t blk = (int64_t)(((uint64_t)blockIdx.x * g.jmul) % (uint64_t)gridDim.x);
-  const int64_t J = blk * (blockDim.x / ls) + (threadIdx.x >> 5) * jw + (lane % jw);
+  // block permutation: only grids of at most 4096 blocks use one (jmul < gridDim.x),
+  // so the product fits 32 bits; jmul == 1 keeps the order without a modulo
+  const int64_t blk = g.jmul == 1u ? (int64_t)blockIdx.x : (int64_t)((blockIdx.x * g.jmul) % gridDim.x);
+  const int64_t J = blk * (int64_t)(blockDim.x >> lsh) + ((threadIdx.x >> 5) << jsh) + (lane & ((1 << jsh) - 1));
   if (J >= g.m) return;
-  const int c0 = blockIdx.y * TC * ls + lane / jw;
-  const int nt = c0 < ncols ? min(TC, (ncols - c0 + ls - 1) / ls) : 0;
-  if (nt <= 0) return;
+  const int c0 = blockIdx.y * TC * ls + (lane >> jsh);
+  // nt == 0 (a ket set past the last vector) skips every load and store below;
+  // an early return here instead makes the FP64 single-vector kernels ~45 % slower
+  const int nt = c0 < ncols ? min(TC, (ncols - c0 + ls - 1) >> lsh) : 0;
   const int64_t vs_x = (int64_t)ls * xcs, vs_y = (int64_t)ls * ycs;
   const XT* xb = x + (int64_t)c0 * xcs;
   AT acc[TC];

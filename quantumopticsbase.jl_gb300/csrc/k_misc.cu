@@ -40,7 +40,8 @@ __global__ void k_scale(CT* y, int64_t rows, int64_t cols, int64_t lr, int64_t l
                         double bi) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= rows * cols) return;
-  const int64_t r = i % rows, c = i / rows;
+  int64_t c, r;
+  udivmod(i, rows, c, r);
   CT* p = y + r * lr + c * lc;
   if (br == 0.0 && bi == 0.0) {
     *p = mk<CT>(0.0, 0.0);
@@ -59,7 +60,8 @@ __global__ void k_axpby(const CT* __restrict__ x, int64_t xes, int64_t xcs, CT* 
                         double br, double bi) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= len * ncols) return;
-  const int64_t e = i % len, c = i / len;
+  int64_t c, e;
+  udivmod(i, len, c, e);
   CT xv = x[e * xes + c * xcs];
   R re = (R)ar * xv.x - (R)ai * xv.y;
   R im = (R)ar * xv.y + (R)ai * xv.x;
@@ -114,7 +116,9 @@ __global__ void k_modek(const CT* __restrict__ A, int64_t s1, int64_t dout, int6
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t c = blockIdx.y;
   if (i >= len || c >= ncols) return;
-  const int64_t a = i % s1, t = i / s1, j = t % dout, b = t / dout;
+  int64_t a, t, j, b;
+  udivmod(i, s1, t, a);
+  udivmod(t, dout, b, j);
   const CT* xc = x + c * xcs;
   R sre = 0, sim = 0;
   if (EYE) {

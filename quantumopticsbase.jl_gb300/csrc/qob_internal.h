@@ -418,6 +418,22 @@ void apply_plan(Context& ctx, Plan& plan, c128 alpha, const void* x, int64_t xes
                 c128 beta, void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s,
                 int ws_base);
 
+#ifdef __CUDACC__
+// Quotient and remainder of non-negative 64-bit values, in 32-bit arithmetic
+// when both fit: a 64-bit division is a long instruction sequence, more than an
+// elementwise kernel's own work per element.
+__device__ __forceinline__ void udivmod(int64_t a, int64_t b, int64_t& q, int64_t& r) {
+  if ((((uint64_t)a | (uint64_t)b) >> 32) == 0) {
+    const uint32_t q32 = (uint32_t)a / (uint32_t)b;
+    q = q32;
+    r = (int64_t)((uint32_t)a - q32 * (uint32_t)b);
+  } else {
+    q = a / b;
+    r = a - q * b;
+  }
+}
+#endif
+
 // A multiplier coprime to n near n * (sqrt(5) - 1) / 2: c -> (c * mul) mod n
 // visits 0 .. n-1 in an order where neighbours are far apart (1 for n <= 2).
 inline uint32_t chunk_multiplier(int64_t n) {
