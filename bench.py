@@ -330,14 +330,15 @@ def run_own(args, rank, world, local_rank):
         return out
 
     def tune(dt):
-        times = (C.c_double * 20)()
+        times = (C.c_double * 28)()
         chosen = C.c_int()
         raise_for(lib.qob_op_tune(ctx.ptr, hd.ptr, L.QOB_LEFT, dtype_code(dt), BATCH, times, C.byref(chosen)), ctx)
         v = chosen.value
         return {"kets_per_thread": v & 0xFFFF, "threads_per_block": (v >> 16) & 0x3FF,
                 "ket_sets_per_warp": 1 << ((v >> 26) & 0x7), "persistent": bool(v >> 30),
                 "ms_by_kets_per_thread_and_shape": {
-                    f"{1 << (k // 5)}x{('128', '256', 'P256', '128s4', '256s4')[k % 5]}": times[k] for k in range(20)}}
+                    f"{1 << (k // 7)}x{('128', '256', 'P256', '128s4', '256s4', '128s8', '256s8')[k % 7]}": times[k]
+                    for k in range(28)}}
 
     def fix(dt, spec):
         """A launch shape given as <kets per thread>x<threads>[s<ket sets per warp>], P for persistent."""

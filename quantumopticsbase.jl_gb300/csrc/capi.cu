@@ -491,10 +491,10 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
     Plan& P = get_plan(ctx->c, op, side, dtype);
     const int tiles[4] = {1, 2, 4, 8};
     // launch shapes: 128 / 256 threads, the persistent grid of 256-thread
-    // blocks, and 128 / 256 threads with four vector sets per warp
-    constexpr int kShapes = 5;
-    const int blocks[kShapes] = {128, 256, -256, 128, 256};
-    const int splits[kShapes] = {1, 1, 1, 4, 4};
+    // blocks, and 128 / 256 threads with four or eight vector sets per warp
+    constexpr int kShapes = 7;
+    const int blocks[kShapes] = {128, 256, -256, 128, 256, 128, 256};
+    const int splits[kShapes] = {1, 1, 1, 4, 4, 8, 8};
     double t[4 * kShapes];
     for (double& v : t) v = -1.0;
     int best = 0, best_block = 256, best_split = 1;

@@ -191,7 +191,7 @@ def test_host_buffers_and_tuning():
     n = len(H.basis_l)
     ctx = get_context(0)
     h = handle(ctx, H)
-    times = (C.c_double * 20)()
+    times = (C.c_double * 28)()
     chosen = C.c_int()
     raise_for(L.lib().qob_op_tune(ctx.ptr, h.ptr, L.QOB_LEFT, L.QOB_C128X, 16, times, C.byref(chosen)), ctx)
     assert chosen.value & 0xFFFF in (1, 2, 4, 8) and max(times) > 0
