@@ -37,6 +37,8 @@ METRIC = "LazySum·ket applies/s (14-spin Heisenberg, batch 64)"
 UNIT = "applies/s"
 NSPINS, BATCH, ROTATE = 14, 64, 20
 ALPHA, BETA = 0.7 - 0.2j, 0.3
+# launch shapes of qob_op_tune, in its order (threads per block, P = persistent, sN = N ket sets per warp)
+SHAPES = ("128", "256", "P256", "128s4", "256s4", "128s8", "256s8", "128s16", "256s16")
 SEED_H = 3
 L2_NOTE = "20 distinct 64-ket batches rotate: 640 MiB (c128) / 320 MiB (c64) of in+out per rotation, > 2x the 129 MB L2"
 
@@ -330,15 +332,14 @@ def run_own(args, rank, world, local_rank):
         return out
 
     def tune(dt):
-        times = (C.c_double * 28)()
+        times = (C.c_double * 36)()
         chosen = C.c_int()
         raise_for(lib.qob_op_tune(ctx.ptr, hd.ptr, L.QOB_LEFT, dtype_code(dt), BATCH, times, C.byref(chosen)), ctx)
         v = chosen.value
         return {"kets_per_thread": v & 0xFFFF, "threads_per_block": (v >> 16) & 0x3FF,
                 "ket_sets_per_warp": 1 << ((v >> 26) & 0x7), "persistent": bool(v >> 30),
                 "ms_by_kets_per_thread_and_shape": {
-                    f"{1 << (k // 7)}x{('128', '256', 'P256', '128s4', '256s4', '128s8', '256s8')[k % 7]}": times[k]
-                    for k in range(28)}}
+                    f"{1 << (k // 9)}x{SHAPES[k % 9]}": times[k] for k in range(36)}}
 
     def fix(dt, spec):
         """A launch shape given as <kets per thread>x<threads>[s<ket sets per warp>], P for persistent."""

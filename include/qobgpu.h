@@ -155,15 +155,16 @@ int qob_op_shape(qob_ctx* ctx, const qob_op* op, int64_t* rows, int64_t* cols);
 int qob_op_prepare(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t* info);
 
 /* Autotuner: time the fused kernel with 1, 2, 4 and 8 vectors per thread and
- * seven launch shapes for applications of op to ncols vectors (side, dtype as
+ * nine launch shapes for applications of op to ncols vectors (side, dtype as
  * in qob_mul) and keep the fastest for later calls with this operator, side
  * and dtype.  Shapes b: 0 / 1 = blocks of 128 / 256 threads over the output
  * indices; 2 = a persistent grid of (SMs x resident blocks) 256-thread blocks
  * that split the work evenly; 3 / 4 = blocks of 128 / 256 threads whose warps
  * cover 8 output indices x 4 sets of vectors, 5 / 6 = 4 output indices x 8
- * sets (entries that vary with the low index bits then diverge over fewer
- * lanes).  times_ms[7k + b] = milliseconds per application with 2^k vectors
- * per thread and shape b, -1 when not tried (28 entries); *chosen = vectors per thread | (threads per block << 16) |
+ * sets, 7 / 8 = 2 output indices x 16 sets (entries that vary with the low
+ * index bits then diverge over fewer lanes).  times_ms[9k + b] = milliseconds
+ * per application with 2^k vectors per thread and shape b, -1 when not tried
+ * (36 entries); *chosen = vectors per thread | (threads per block << 16) |
  * (log2 vector sets per warp << 26) | (1 << 30 when persistent), 0 when the
  * operator has no fused part.  Either pointer may be NULL.  Vector sets (x
  * and y) of 16 MB or more are timed with inputs not in L2 (up to 16 scratch
@@ -177,7 +178,8 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
 
 /* Fix the launch shape instead of tuning: vectors_per_thread 1, 2, 4 or 8;
  * block 128 or 256 threads, or -256 for the persistent grid; lane_split 1, 2,
- * 4 or 8 vector sets per warp (not used by the persistent grid).  Kept until
+ * 4, 8, 16 or 32 vector sets per warp (32 / lane_split output indices per
+ * warp; not used by the persistent grid).  Kept until
  * the next tune or recompilation. */
 int qob_op_set_launch(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_per_thread, int block,
                       int lane_split);

@@ -491,10 +491,10 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
     Plan& P = get_plan(ctx->c, op, side, dtype);
     const int tiles[4] = {1, 2, 4, 8};
     // launch shapes: 128 / 256 threads, the persistent grid of 256-thread
-    // blocks, and 128 / 256 threads with four or eight vector sets per warp
-    constexpr int kShapes = 7;
-    const int blocks[kShapes] = {128, 256, -256, 128, 256, 128, 256};
-    const int splits[kShapes] = {1, 1, 1, 4, 4, 8, 8};
+    // blocks, and 128 / 256 threads with 4, 8 or 16 vector sets per warp
+    constexpr int kShapes = 9;
+    const int blocks[kShapes] = {128, 256, -256, 128, 256, 128, 256, 128, 256};
+    const int splits[kShapes] = {1, 1, 1, 4, 4, 8, 8, 16, 16};
     double t[4 * kShapes];
     for (double& v : t) v = -1.0;
     int best = 0, best_block = 256, best_split = 1;
@@ -590,8 +590,8 @@ int qob_op_set_launch(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors
     if (vectors_per_thread != 1 && vectors_per_thread != 2 && vectors_per_thread != 4 && vectors_per_thread != 8)
       fail(QOB_ERR_ARG, "vectors per thread must be 1, 2, 4 or 8");
     if (block != 128 && block != 256 && block != -256) fail(QOB_ERR_ARG, "block must be 128, 256 or -256");
-    if (lane_split != 1 && lane_split != 2 && lane_split != 4 && lane_split != 8)
-      fail(QOB_ERR_ARG, "lane_split must be 1, 2, 4 or 8");
+    if (lane_split < 1 || lane_split > 32 || (lane_split & (lane_split - 1)) != 0)
+      fail(QOB_ERR_ARG, "lane_split must be 1, 2, 4, 8, 16 or 32");
     Plan& P = get_plan(ctx->c, op, side, dtype);
     if (P.gather) {
       P.gather->tc = vectors_per_thread;

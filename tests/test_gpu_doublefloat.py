@@ -60,7 +60,7 @@ def test_benchmark_hamiltonians_kets_and_batches():
     assert max(errs) < 1e-13, errs
 
 
-@pytest.mark.parametrize("block,split", [(128, 1), (256, 1), (-256, 1), (256, 4), (128, 8)])
+@pytest.mark.parametrize("block,split", [(128, 1), (256, 1), (-256, 1), (256, 4), (128, 8), (128, 16), (256, 32)])
 @pytest.mark.parametrize("tc", [1, 2, 4, 8])
 def test_every_launch_shape(tc, block, split):
     from qobgpu import _lib as L
@@ -191,7 +191,7 @@ def test_host_buffers_and_tuning():
     n = len(H.basis_l)
     ctx = get_context(0)
     h = handle(ctx, H)
-    times = (C.c_double * 28)()
+    times = (C.c_double * 36)()
     chosen = C.c_int()
     raise_for(L.lib().qob_op_tune(ctx.ptr, h.ptr, L.QOB_LEFT, L.QOB_C128X, 16, times, C.byref(chosen)), ctx)
     assert chosen.value & 0xFFFF in (1, 2, 4, 8) and max(times) > 0
