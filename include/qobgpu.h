@@ -220,7 +220,9 @@ int qob_mul_host(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, d
  * and y may be reused; until then the caller leaves both untouched.  Calls run
  * in the order made, and each call's copies in overlap the previous call's
  * kernels and copy out (two device staging sets are used in turn), so a stream
- * of batches moves at the host link's rate.  With page-locked host memory the
+ * of batches moves at the host link's rate; a call's own copies and kernels
+ * run one after another (no chunks: fewer copies), so a single call waited on
+ * alone is slower than qob_mul_host.  With page-locked host memory the
  * copies are asynchronous; with pageable memory the driver stages them and the
  * call returns once they are done.  Errors of the argument checks return at
  * once; errors of the device work return from qob_host_wait. */

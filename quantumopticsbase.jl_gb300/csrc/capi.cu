@@ -643,13 +643,15 @@ MulShape mul_shape(const qob_op* op, int side, int is_vector, int64_t x_rows, in
 
 // Enqueues one host call: copies in on copy_stream[0], the application on
 // copy_stream[1], the copy of y back on copy_stream[2], linked per chunk by
-// events.  Several kets from the left go through in up to four chunks of
-// columns, so that the copies of one chunk overlap the kernels of another;
-// other shapes in one chunk.  The call uses staging set (host_calls % 2) once
-// the copy out of the call before the previous one has left it.  Returns the
-// call's ticket.
+// events.  With `chunks` (a call waited on alone), several kets from the left
+// go through in up to four chunks of columns, so that the copies of one chunk
+// overlap the kernels of another; otherwise (a stream of calls, which overlap
+// one another) and for other shapes in one piece, with the fewest copies.  The
+// call uses staging set (host_calls % 2) once the copy out of the call before
+// the previous one has left it.  Returns the call's ticket.
 uint64_t enqueue_host(Context& c, int side, int is_vector, qob_op* op, int dtype, c128 alpha, const void* x,
-                      int64_t x_rows, int64_t x_cols, c128 beta, void* y, int64_t y_rows, int64_t y_cols) {
+                      int64_t x_rows, int64_t x_cols, c128 beta, void* y, int64_t y_rows, int64_t y_cols,
+                      bool chunks) {
   check_mul_dtype(dtype);
   const MulShape sh = mul_shape(op, side, is_vector, x_rows, x_cols, std::max<int64_t>(x_rows, 1), y_rows, y_cols,
                                 std::max<int64_t>(y_rows, 1));
@@ -684,7 +686,7 @@ uint64_t enqueue_host(Context& c, int side, int is_vector, qob_op* op, int dtype
     }
     Plan& P = get_plan(c, op, side, dtype);
     if (c.stage_used[st]) QOB_CUDA(cudaStreamWaitEvent(sin, c.stage_free[st], 0));
-    const bool chunked = side == QOB_LEFT && x_cols >= 8;
+    const bool chunked = chunks && side == QOB_LEFT && x_cols >= 8;
     const int64_t nchunk = chunked ? std::min<int64_t>(4, x_cols / 4) : 1;
     const int64_t per = chunked ? (x_cols + nchunk - 1) / nchunk : x_cols;
     int64_t k = 0;
@@ -741,7 +743,7 @@ int qob_mul_host(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dtype, d
   return guard(ctx, [&] {
     if (!ctx) fail(QOB_ERR_ARG, "null context or operator");
     const uint64_t t = enqueue_host(ctx->c, side, is_vector, op, dtype, {alpha_re, alpha_im}, x, x_rows, x_cols,
-                                    {beta_re, beta_im}, y, y_rows, y_cols);
+                                    {beta_re, beta_im}, y, y_rows, y_cols, true);
     QOB_CUDA(cudaEventSynchronize(ctx->c.ticket_done[(t - 1) % Context::kTickets]));
   });
 }
@@ -752,7 +754,7 @@ int qob_mul_host_async(qob_ctx* ctx, int side, int is_vector, qob_op* op, int dt
   return guard(ctx, [&] {
     if (!ctx || !ticket) fail(QOB_ERR_ARG, "null context or ticket");
     *ticket = enqueue_host(ctx->c, side, is_vector, op, dtype, {alpha_re, alpha_im}, x, x_rows, x_cols,
-                           {beta_re, beta_im}, y, y_rows, y_cols);
+                           {beta_re, beta_im}, y, y_rows, y_cols, false);
   });
 }
 

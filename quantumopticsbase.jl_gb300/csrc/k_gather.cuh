@@ -753,7 +753,10 @@ void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t x
   auto kern = k_gather_j<R, VM, SQUARE, W1, TC, BMODE>;
   allow_smem(kern, smem);
   const int threads = v.block > 0 ? v.block : kThreads;
-  const int ls = v.lane_split > 0 ? v.lane_split : 1;
+  // a tuned lane split wider than this call's vectors fill (fewer vectors than
+  // the tuning, e.g. the chunks of a host call) is narrowed
+  int ls = v.lane_split > 0 ? v.lane_split : 1;
+  while (ls > 1 && (int64_t)TC * ls > ncols) ls >>= 1;
   const int64_t jpb = threads / ls;  // output indices per block
   const unsigned gx = (unsigned)((v.m + jpb - 1) / jpb);
   GatherView w = v;
