@@ -413,7 +413,7 @@ void launch_axpby(int precision, const void* x, int64_t xes, int64_t xcs, c128 a
 void reduce_dot(Context& ctx, int precision, const void* x, const void* y, int64_t n, bool norm,
                 double* out, cudaStream_t s);
 
-// execution (apply.cu)
+// execution (capi.cu)
 void apply_plan(Context& ctx, Plan& plan, c128 alpha, const void* x, int64_t xes, int64_t xcs,
                 c128 beta, void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s,
                 int ws_base);

@@ -231,7 +231,7 @@ def test_large_dense_factor_mode_products():
 @pytest.mark.parametrize("ncols", [1, 3, 16, 37])
 def test_host_buffers_through_qob_mul_host(ncols):
     """numpy (host) data goes through qob_mul_host: copies in, kernels, copy out
-    (pipelined over two streams for 8 or more columns)."""
+    (in four chunks over three streams for 8 or more columns)."""
     from qobgpu.mul import mul_
 
     H = heisenberg_chain(9, seed=5)
