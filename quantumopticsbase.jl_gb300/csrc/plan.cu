@@ -620,14 +620,23 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
 // plan compilation
 // ---------------------------------------------------------------------------
 
+// Merge a LazyTensor's factors into one local operator (fused gather) or keep
+// the mode-product chain.  A merged row holds the product of the factors' row
+// widths, the chain costs their sum per element plus one pass over the state
+// per factor: merge while the product stays within max(16, 2 x sum) -- every
+// Pauli / ladder / number product, single dense factors of any size -- and
+// chain for several wide (dense) factors, e.g. 64 x 64 and 16 x 16 dense
+// factors: 1024 entries per merged row against 80 multiply-adds per element.
 static bool gatherable_factor_sizes(const std::vector<const RowList*>& rl, int64_t nrows) {
-  double entries = (double)nrows;
+  double entries = (double)nrows, prod = 1.0, sum = 0.0;
   for (auto* r : rl) {
     int64_t mx = 0;
     for (int64_t i = 0; i < r->rows; ++i) mx = std::max(mx, r->ptr[i + 1] - r->ptr[i]);
     entries *= (double)std::max<int64_t>(mx, 1);
+    prod *= (double)std::max<int64_t>(mx, 1);
+    sum += (double)std::max<int64_t>(mx, 1);
   }
-  return nrows <= (int64_t(1) << 24) && entries <= double(int64_t(1) << 25);
+  return nrows <= (int64_t(1) << 24) && entries <= double(int64_t(1) << 25) && prod <= std::max(16.0, 2.0 * sum);
 }
 
 std::unique_ptr<Plan> compile_plan(Context& ctx, const NodeP& op, int side, int precision);

@@ -15,6 +15,8 @@ submission and completion:
 * ``lindblad``    Lindblad right-hand side S rho, lazy Liouvillian of 8 / 10 / 12-spin
                   chains with sigma_- decay (and the materialised one at 8 spins);
 * ``particle``    split-operator particle Hamiltonian (FFT operators) on 4096 and 512 x 512 grids;
+* ``modek``       LazyTensor mode products with dense factors too large to merge (120,000 and
+                  65,536 states, 1 and 16 kets);
 * ``cavities256`` 256 two-mode cavity models (dims 81 ... 4225) in one launch;
 * ``served``      Poisson arrivals of 100-step RK4 requests (Heisenberg chains of
                   8 ... 16 spins, Jaynes-Cummings models of dim 512 ... 8192).
@@ -345,7 +347,47 @@ def host_link(ctx, stream):
     return {"workload": "host_link", "bytes_per_copy": n * 16, "results": out}
 
 
-WORKLOADS = ("jc512", "sparse4096", "rho_h8", "lindblad", "particle", "cavities256", "served", "host_link")
+def modek(ctx, stream):
+    """Mode products of a LazyTensor whose dense factors are too large to merge
+    (_tp_sum_matmul!'s path): two 200 x 200 dense factors on the outer sites of
+    FockBasis(199) x Spin(1) x FockBasis(199) (120,000 states), one ket and 16
+    kets; and one 64 x 64 dense factor with a 16 x 16 one on a 64 x 16 x 64 space."""
+    import torch
+
+    from . import operators as O
+    from .bases import GenericBasis
+    from .bases import tensor as tensor_basis
+
+    rng = Rng(60)
+
+    def dense(d):
+        a = rng.complex_normal(d * d).reshape(d, d, order="F")
+        return O.Operator(GenericBasis(d), GenericBasis(d), np.asfortranarray(a))
+
+    out = []
+    for dims, sites in (((200, 3, 200), (1, 3)), ((64, 16, 64), (1, 2))):
+        bs = [GenericBasis(d) for d in dims]
+        b = tensor_basis(*bs)
+        facs = tuple(dense(dims[s - 1]) for s in sites)
+        op = O.LazyTensor(b, b, sites, facs, 0.3)
+        h = handle(ctx, op)
+        n = len(b)
+        for tdt, npdt, code, label in _modes():
+            for ncols in (1, 16):
+                x = _cols(n, ncols, tdt, 61)
+                y = _cols(n, ncols, tdt, 62)
+                reps = 5
+                ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, L.QOB_LEFT, n, n, ncols, x, y, code,
+                                                             reps=reps))
+                t = ms * 1e-3 / reps
+                flops = 8.0 * n * ncols * sum(dims[s - 1] for s in sites)  # complex FMA = 8 flop per term
+                out.append({"dims": list(dims), "dense_sites": list(sites), "dtype": label, "kets": ncols,
+                            "us_per_call": t * 1e6, "tflops": flops / t / 1e12})
+        del h
+    return {"workload": "modek", "results": out}
+
+
+WORKLOADS = ("jc512", "sparse4096", "rho_h8", "lindblad", "particle", "modek", "cavities256", "served", "host_link")
 
 
 def run_suite(device: int = 0, only=None):
