@@ -102,8 +102,9 @@ void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, i
       b = one;
     }
     for (auto& d : P.dense) {
+      // partial sums of a split product in slot ws (free here, as for the split input above)
       launch_dense(P.precision, d.a.p, d.m, d.n, cmul(alpha, coefval(d.coef, P.root)), x, xes, xcs, b, y,
-                   yes, ycs, ncols, s);
+                   yes, ycs, ncols, s, &ctx.ws, ws);
       b = one;
     }
     for (auto& mk : P.modek) {

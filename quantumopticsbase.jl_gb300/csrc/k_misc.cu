@@ -74,30 +74,81 @@ __global__ void k_axpby(const CT* __restrict__ x, int64_t xes, int64_t xcs, CT* 
   *yp = mk<CT>(re, im);
 }
 
-// Dense operator (m x n, column-major) times ncols vectors: one thread per
-// output (i, c); the operator column reads are coalesced across i.
+// Dense operator (m x n, column-major) times ncols vectors.  A thread owns one
+// row i and a tile of TC vectors (each A element it loads serves all of them);
+// blocks split the columns k into kchunks ranges so that a tall-skinny product
+// (one ket, m ~ 1000) still fills the GPU.  With one range the thread writes
+// alpha * acc + beta * y; otherwise it writes its partial sum to part[z][c][i]
+// and k_dense_reduce adds the ranges in order (deterministic) and combines.
+template <typename CT, typename R, int TC>
+__global__ void __launch_bounds__(128) k_dense(const CT* __restrict__ a, int64_t m, int64_t n,
+                                               const CT* __restrict__ x, int64_t xes, int64_t xcs,
+                                               CT* __restrict__ y, int64_t yes, int64_t ycs, int64_t ncols,
+                                               int64_t kc, CT* __restrict__ part, double ar, double ai,
+                                               double br, double bi) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t c0 = (int64_t)blockIdx.y * TC;
+  if (i >= m) return;
+  const int nt = (int)(ncols - c0 < TC ? ncols - c0 : TC);
+  const int64_t k0 = (int64_t)blockIdx.z * kc, k1 = k0 + kc < n ? k0 + kc : n;
+  R sre[TC], sim[TC];
+#pragma unroll
+  for (int t = 0; t < TC; ++t) sre[t] = sim[t] = 0;
+  const CT* xc = x + c0 * xcs;
+  for (int64_t k = k0; k < k1; ++k) {
+    const CT av = a[i + k * m];
+#pragma unroll
+    for (int t = 0; t < TC; ++t) {
+      if (t < nt) {
+        const CT xv = xc[t * xcs + k * xes];
+        sre[t] = fma(av.x, xv.x, sre[t]);
+        sre[t] = fma(-av.y, xv.y, sre[t]);
+        sim[t] = fma(av.x, xv.y, sim[t]);
+        sim[t] = fma(av.y, xv.x, sim[t]);
+      }
+    }
+  }
+  if (part) {
+#pragma unroll
+    for (int t = 0; t < TC; ++t)
+      if (t < nt) part[((int64_t)blockIdx.z * ncols + c0 + t) * m + i] = mk<CT>(sre[t], sim[t]);
+    return;
+  }
+#pragma unroll
+  for (int t = 0; t < TC; ++t) {
+    if (t < nt) {
+      R re = (R)ar * sre[t] - (R)ai * sim[t];
+      R im = (R)ar * sim[t] + (R)ai * sre[t];
+      CT* yp = y + i * yes + (c0 + t) * ycs;
+      if (br != 0.0 || bi != 0.0) {
+        const CT o = *yp;
+        re += (R)br * o.x - (R)bi * o.y;
+        im += (R)br * o.y + (R)bi * o.x;
+      }
+      *yp = mk<CT>(re, im);
+    }
+  }
+}
+
+// The k ranges' partial sums of k_dense added in order, then alpha / beta.
 template <typename CT, typename R>
-__global__ void k_dense(const CT* __restrict__ a, int64_t m, int64_t n, const CT* __restrict__ x,
-                        int64_t xes, int64_t xcs, CT* __restrict__ y, int64_t yes, int64_t ycs,
-                        int64_t ncols, double ar, double ai, double br, double bi) {
+__global__ void k_dense_reduce(const CT* __restrict__ part, int kchunks, int64_t m, int64_t ncols,
+                               CT* __restrict__ y, int64_t yes, int64_t ycs, double ar, double ai, double br,
+                               double bi) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t c = blockIdx.y;
-  if (i >= m || c >= ncols) return;
+  if (i >= m) return;
   R sre = 0, sim = 0;
-  const CT* xc = x + c * xcs;
-  for (int64_t k = 0; k < n; ++k) {
-    CT av = a[i + k * m];
-    CT xv = xc[k * xes];
-    sre = fma(av.x, xv.x, sre);
-    sre = fma(-av.y, xv.y, sre);
-    sim = fma(av.x, xv.y, sim);
-    sim = fma(av.y, xv.x, sim);
+  for (int z = 0; z < kchunks; ++z) {
+    const CT p = part[((int64_t)z * ncols + c) * m + i];
+    sre += p.x;
+    sim += p.y;
   }
   R re = (R)ar * sre - (R)ai * sim;
   R im = (R)ar * sim + (R)ai * sre;
   CT* yp = y + i * yes + c * ycs;
   if (br != 0.0 || bi != 0.0) {
-    CT o = *yp;
+    const CT o = *yp;
     re += (R)br * o.x - (R)bi * o.y;
     im += (R)br * o.y + (R)bi * o.x;
   }
@@ -231,27 +282,71 @@ void launch_axpby(int precision, const void* x, int64_t xes, int64_t xcs, c128 a
   QOB_LAUNCHED();
 }
 
+namespace {
+// k ranges per dense product: enough blocks for about four per SM, each range
+// at least 64 columns long
+int dense_kchunks(int64_t m, int64_t n, int64_t ncols, int tc) {
+  const int64_t blocks = ((m + 127) / 128) * ((ncols + tc - 1) / tc);
+  int64_t kch = (608 + blocks - 1) / blocks;
+  kch = std::min<int64_t>(kch, std::max<int64_t>(1, n / 64));
+  return (int)std::max<int64_t>(1, std::min<int64_t>(kch, 65535));
+}
+
+template <typename CT, typename R>
+void dense_typed(const void* a, int64_t m, int64_t n, c128 alpha, const void* x, int64_t xes, int64_t xcs,
+                 c128 beta, void* y, int64_t yes, int64_t ycs, int64_t ncols, Workspace* ws, int slot,
+                 cudaStream_t s) {
+  const int tc = ncols >= 8 ? 8 : ncols >= 4 ? 4 : ncols >= 2 ? 2 : 1;
+  int kch = ws ? dense_kchunks(m, n, ncols, tc) : 1;
+  CT* part = nullptr;
+  if (kch > 1) part = static_cast<CT*>(ws->get(slot, (size_t)kch * ncols * m * sizeof(CT)));
+  const int64_t kc = (n + kch - 1) / kch;
+  kch = (int)((n + kc - 1) / kc);
+  const dim3 grid(blocks_for(m, 128), (unsigned)((ncols + tc - 1) / tc), (unsigned)kch);
+  const CT* A = (const CT*)a;
+  const CT* X = (const CT*)x;
+  CT* Y = (CT*)y;
+  switch (tc) {
+    case 8:
+      k_dense<CT, R, 8><<<grid, 128, 0, s>>>(A, m, n, X, xes, xcs, Y, yes, ycs, ncols, kc, part, alpha.re,
+                                             alpha.im, beta.re, beta.im);
+      break;
+    case 4:
+      k_dense<CT, R, 4><<<grid, 128, 0, s>>>(A, m, n, X, xes, xcs, Y, yes, ycs, ncols, kc, part, alpha.re,
+                                             alpha.im, beta.re, beta.im);
+      break;
+    case 2:
+      k_dense<CT, R, 2><<<grid, 128, 0, s>>>(A, m, n, X, xes, xcs, Y, yes, ycs, ncols, kc, part, alpha.re,
+                                             alpha.im, beta.re, beta.im);
+      break;
+    default:
+      k_dense<CT, R, 1><<<grid, 128, 0, s>>>(A, m, n, X, xes, xcs, Y, yes, ycs, ncols, kc, part, alpha.re,
+                                             alpha.im, beta.re, beta.im);
+  }
+  QOB_LAUNCHED();
+  if (part) {
+    k_dense_reduce<CT, R><<<dim3(blocks_for(m, 128), (unsigned)ncols), 128, 0, s>>>(
+        part, kch, m, ncols, Y, yes, ycs, alpha.re, alpha.im, beta.re, beta.im);
+    QOB_LAUNCHED();
+  }
+}
+}  // namespace
+
 void launch_dense(int precision, const void* a, int64_t m, int64_t n, c128 alpha, const void* x,
                   int64_t xes, int64_t xcs, c128 beta, void* y, int64_t yes, int64_t ycs,
-                  int64_t ncols, cudaStream_t s) {
+                  int64_t ncols, cudaStream_t s, Workspace* ws, int slot) {
   if (m == 0 || ncols == 0) return;
   const size_t esz = precision == QOB_C128 ? 16 : 8;
-  if (ncols > 65535) {  // grid.y limit: split the vectors
-    for (int64_t c0 = 0; c0 < ncols; c0 += 65535)
+  if (ncols > 65535 * 8) {  // grid.y limit: split the vectors
+    for (int64_t c0 = 0; c0 < ncols; c0 += 65535 * 8)
       launch_dense(precision, a, m, n, alpha, (const char*)x + c0 * xcs * esz, xes, xcs, beta,
-                   (char*)y + c0 * ycs * esz, yes, ycs, std::min<int64_t>(65535, ncols - c0), s);
+                   (char*)y + c0 * ycs * esz, yes, ycs, std::min<int64_t>(65535 * 8, ncols - c0), s, ws, slot);
     return;
   }
-  dim3 grid(blocks_for(m, 128), (unsigned)ncols);
   if (precision == QOB_C128)
-    k_dense<double2, double><<<grid, 128, 0, s>>>((const double2*)a, m, n, (const double2*)x, xes, xcs,
-                                                  (double2*)y, yes, ycs, ncols, alpha.re, alpha.im,
-                                                  beta.re, beta.im);
+    dense_typed<double2, double>(a, m, n, alpha, x, xes, xcs, beta, y, yes, ycs, ncols, ws, slot, s);
   else
-    k_dense<float2, float><<<grid, 128, 0, s>>>((const float2*)a, m, n, (const float2*)x, xes, xcs,
-                                                (float2*)y, yes, ycs, ncols, alpha.re, alpha.im,
-                                                beta.re, beta.im);
-  QOB_LAUNCHED();
+    dense_typed<float2, float>(a, m, n, alpha, x, xes, xcs, beta, y, yes, ycs, ncols, ws, slot, s);
 }
 
 void launch_modek(int precision, const void* a, bool eye, int64_t s1, int64_t dout, int64_t din,

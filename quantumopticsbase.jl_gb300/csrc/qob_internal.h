@@ -401,9 +401,11 @@ std::unique_ptr<Plan> compile_fft(const NodeP& op, int side, int precision);
 int gather_tile(const GatherPlan& g, int64_t ncols);
 void launch_scale(int precision, void* y, int64_t rows, int64_t cols, int64_t ld_row,
                   int64_t ld_col, c128 beta, cudaStream_t s);
+// ws / slot: room for the partial sums of a product split over column ranges
+// (no split without it)
 void launch_dense(int precision, const void* a, int64_t m, int64_t n, c128 alpha, const void* x,
                   int64_t xes, int64_t xcs, c128 beta, void* y, int64_t yes, int64_t ycs,
-                  int64_t ncols, cudaStream_t s);
+                  int64_t ncols, cudaStream_t s, Workspace* ws = nullptr, int slot = 0);
 void launch_modek(int precision, const void* a, bool eye, int64_t s1, int64_t dout, int64_t din,
                   int64_t s3, c128 alpha, const void* x, int64_t xes, int64_t xcs, c128 beta,
                   void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s);

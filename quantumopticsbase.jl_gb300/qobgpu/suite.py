@@ -17,6 +17,7 @@ submission and completion:
 * ``particle``    split-operator particle Hamiltonian (FFT operators) on 4096 and 512 x 512 grids;
 * ``modek``       LazyTensor mode products with dense factors too large to merge (120,000 and
                   65,536 states, 1 and 16 kets);
+* ``dense``       DenseOperator mul! with n = 1024 and 4096 on one and several kets;
 * ``cavities256`` 256 two-mode cavity models (dims 81 ... 4225) in one launch;
 * ``served``      Poisson arrivals of 100-step RK4 requests (Heisenberg chains of
                   8 ... 16 spins, Jaynes-Cummings models of dim 512 ... 8192).
@@ -387,7 +388,36 @@ def modek(ctx, stream):
     return {"workload": "modek", "results": out}
 
 
-WORKLOADS = ("jc512", "sparse4096", "rho_h8", "lindblad", "particle", "modek", "cavities256", "served", "host_link")
+def dense(ctx, stream):
+    """DenseOperator mul! (gemv / gemm): n x n dense operators, n = 1024 and 4096,
+    on 1 and 64 / 16 kets."""
+    from . import operators as O
+    from .bases import GenericBasis
+
+    rng = Rng(70)
+    out = []
+    for nd, kets in ((1024, (1, 64)), (4096, (1, 16))):
+        b = GenericBasis(nd)
+        op = O.Operator(b, b, np.asfortranarray(rng.complex_normal(nd * nd).reshape(nd, nd, order="F")))
+        h = handle(ctx, op)
+        for tdt, npdt, code, label in (m for m in _modes() if m[2] != L.QOB_C128X):
+            for ncols in kets:
+                x = _cols(nd, ncols, tdt, 71)
+                y = _cols(nd, ncols, tdt, 72)
+                reps = 5
+                ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, L.QOB_LEFT, nd, nd, ncols, x, y, code,
+                                                             reps=reps))
+                t = ms * 1e-3 / reps
+                s_ = 16 if npdt == np.complex128 else 8
+                out.append({"n": nd, "dtype": label, "kets": ncols, "us_per_call": t * 1e6,
+                            "tflops": 8.0 * nd * nd * ncols / t / 1e12,
+                            "matrix_GBps": nd * nd * s_ / t / 1e9})
+        del h
+    return {"workload": "dense", "results": out}
+
+
+WORKLOADS = ("jc512", "sparse4096", "rho_h8", "lindblad", "particle", "modek", "dense", "cavities256", "served",
+             "host_link")
 
 
 def run_suite(device: int = 0, only=None):

@@ -284,3 +284,20 @@ def test_norm_dot_expect_fp64():
     assert abs(expect(H, da) - np.vdot(a.data, D @ a.data)) < 1e-12 * abs(np.vdot(a.data, D @ a.data))
     f = to_device(a, dtype=np.complex64)
     assert abs(norm(f) - np.linalg.norm(a.data.astype(np.complex64).astype(np.complex128))) < 1e-12
+
+
+@pytest.mark.parametrize("ncols", [1, 3, 13])
+def test_dense_operator_split_columns(ncols):
+    """A 700 x 500 DenseOperator (split over column ranges with an ordered
+    reduction of the partial sums) on kets from the left and on rows of an
+    operator from the right, complex beta."""
+    rng = Q.Rng(130 + ncols)
+    bl, br = Q.GenericBasis(700), Q.GenericBasis(500)
+    D = rand_op(rng, bl, br)
+    X = O.Operator(br, Q.GenericBasis(ncols), rng.kets_data(500, ncols))
+    Y = O.Operator(bl, Q.GenericBasis(ncols), rng.kets_data(700, ncols))
+    check(Y, D, X, AL, 0.4 - 0.9j, TOL64)
+    check(Y, D, X, AL, 0.4 - 0.9j, TOL32, np.complex64)
+    R = O.Operator(Q.GenericBasis(ncols), bl, np.asfortranarray(rng.complex_normal(ncols * 700).reshape(ncols, 700, order="F")))
+    Z = O.Operator(Q.GenericBasis(ncols), br, np.asfortranarray(rng.complex_normal(ncols * 500).reshape(ncols, 500, order="F")))
+    check(Z, R, D, AL, 0.4 - 0.9j, TOL64)
