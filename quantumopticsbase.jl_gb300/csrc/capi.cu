@@ -102,9 +102,16 @@ void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, i
       b = one;
     }
     for (auto& d : P.dense) {
-      // partial sums of a split product in slot ws (free here, as for the split input above)
-      launch_dense(P.precision, d.a.p, d.m, d.n, cmul(alpha, coefval(d.coef, P.root)), x, xes, xcs, b, y,
-                   yes, ycs, ncols, s, &ctx.ws, ws);
+      // partial sums of a split product in slot ws (free here, as for the split input above);
+      // a double-float plan splits x into slot ws + 1 first
+      const void* xin = x;
+      if (P.ff) {
+        void* xs = ctx.ws.get(ws + 1, (size_t)((P.n - 1) * xes + (ncols - 1) * xcs + 1) * 16);
+        launch_ff_split(x, P.n, ncols, xes, xcs, xs, s);
+        xin = xs;
+      }
+      launch_dense(P.precision, d.a.p, d.m, d.n, cmul(alpha, coefval(d.coef, P.root)), xin, xes, xcs, b, y,
+                   yes, ycs, ncols, s, &ctx.ws, ws, P.ff);
       b = one;
     }
     for (auto& mk : P.modek) {
@@ -124,14 +131,24 @@ void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, i
         next[st.site] = st.dout;
         const int64_t s1 = prod_range(cur, 0, st.site), s3 = prod_range(cur, st.site + 1, cur.size());
         const c128 ak = (k == 0) ? a : one;
+        // a double-float plan splits each step's input into slot ws + 2 (the
+        // step's temporaries use ws and ws + 1; sub-plans, which use ws + 2, run after)
+        const bool ffs = P.ff && !st.eye;
+        const void* sin = src;
+        if (ffs) {
+          const int64_t len_in = prod_range(cur, 0, cur.size());
+          void* xs = ctx.ws.get(ws + 2, (size_t)((len_in - 1) * ses + (ncols - 1) * scs + 1) * 16);
+          launch_ff_split(src, len_in, ncols, ses, scs, xs, s);
+          sin = xs;
+        }
         if (k + 1 == nst) {
-          launch_modek(P.precision, st.a.p, st.eye, s1, st.dout, st.din, s3, ak, src, ses, scs, b, y, yes,
-                       ycs, ncols, s);
+          launch_modek(P.precision, st.a.p, st.eye, s1, st.dout, st.din, s3, ak, sin, ses, scs, b, y, yes,
+                       ycs, ncols, s, ffs);
         } else {
           const int64_t len = prod_range(next, 0, next.size());
           void* t = ctx.ws.get(ws + (k % 2), (size_t)len * ncols * esz);
-          launch_modek(P.precision, st.a.p, st.eye, s1, st.dout, st.din, s3, ak, src, ses, scs, zero, t, 1,
-                       len, ncols, s);
+          launch_modek(P.precision, st.a.p, st.eye, s1, st.dout, st.din, s3, ak, sin, ses, scs, zero, t, 1,
+                       len, ncols, s, ffs);
           src = t;
           ses = 1;
           scs = len;

@@ -228,6 +228,14 @@ int gather_tile(const GatherPlan& g, int64_t ncols) {
   return tc;
 }
 
+void launch_ff_split(const void* x, int64_t n, int64_t ncols, int64_t es, int64_t cs, void* out, cudaStream_t s) {
+  const int64_t total = n * ncols;
+  if (total == 0) return;
+  const unsigned blocks = (unsigned)((total + 256 * kSplitPer - 1) / (256 * kSplitPer));
+  k_ff_split<<<blocks, 256, 0, s>>>(static_cast<const double2*>(x), n, ncols, es, cs, static_cast<float4*>(out));
+  QOB_LAUNCHED();
+}
+
 void launch_gather(const GatherPlan& g, int precision, const void* x, int64_t xes, int64_t xcs,
                    void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta,
                    cudaStream_t s, int64_t n, void* ff_x) {
@@ -236,10 +244,7 @@ void launch_gather(const GatherPlan& g, int precision, const void* x, int64_t xe
   if (g.ff) {
     // split x once; the gather then reads the quadruples with x's strides
     if (!ff_x || n <= 0) fail(QOB_ERR_ARG, "double-float gather without split buffer");
-    const int64_t total = n * ncols;
-    const unsigned blocks = (unsigned)((total + 256 * kSplitPer - 1) / (256 * kSplitPer));
-    k_ff_split<<<blocks, 256, 0, s>>>(static_cast<const double2*>(x), n, ncols, xes, xcs, static_cast<float4*>(ff_x));
-    QOB_LAUNCHED();
+    launch_ff_split(x, n, ncols, xes, xcs, ff_x, s);
     x = ff_x;
   }
   // groups beyond one launch's shared-memory budget go in further launches

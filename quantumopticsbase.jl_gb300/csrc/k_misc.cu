@@ -9,6 +9,7 @@
 
 #include <algorithm>
 
+#include "k_gather.cuh"  // double-float helpers (ff_join, AccFF)
 #include "qob_internal.h"
 
 namespace qob {
@@ -128,6 +129,74 @@ __global__ void __launch_bounds__(128) k_dense(const CT* __restrict__ a, int64_t
       *yp = mk<CT>(re, im);
     }
   }
+}
+
+// Double-float forms (ComplexF64 data, QOB_C128X): the operator factor is
+// stored as (re hi, re lo, im hi, im lo) quadruples, x arrives split the same
+// way (k_ff_split), the sums are FP32 pairs, joined to double for the FP64
+// alpha / beta epilogue (or for the partial sums of a split product).
+__device__ __forceinline__ double2 ff_total(const gather::AccFF& acc) {
+  return make_double2(gather::ff_join(acc.rh, acc.rl), gather::ff_join(acc.ih, acc.il));
+}
+__device__ __forceinline__ void combine64(double2* yp, double2 v, double ar, double ai, double br, double bi) {
+  double re = ar * v.x - ai * v.y;
+  double im = ar * v.y + ai * v.x;
+  if (br != 0.0 || bi != 0.0) {
+    const double2 o = *yp;
+    re += br * o.x - bi * o.y;
+    im += br * o.y + bi * o.x;
+  }
+  *yp = make_double2(re, im);
+}
+
+template <int TC>
+__global__ void __launch_bounds__(128) k_dense_ff(const float4* __restrict__ a, int64_t m, int64_t n,
+                                                  const float4* __restrict__ x, int64_t xes, int64_t xcs,
+                                                  double2* __restrict__ y, int64_t yes, int64_t ycs, int64_t ncols,
+                                                  int64_t kc, double2* __restrict__ part, double ar, double ai,
+                                                  double br, double bi) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t c0 = (int64_t)blockIdx.y * TC;
+  if (i >= m) return;
+  const int nt = (int)(ncols - c0 < TC ? ncols - c0 : TC);
+  const int64_t k0 = (int64_t)blockIdx.z * kc, k1 = k0 + kc < n ? k0 + kc : n;
+  gather::AccFF acc[TC];
+#pragma unroll
+  for (int t = 0; t < TC; ++t) acc[t].zero();
+  const float4* xc = x + c0 * xcs;
+  for (int64_t k = k0; k < k1; ++k) {
+    const float4 av = a[i + k * m];
+#pragma unroll
+    for (int t = 0; t < TC; ++t)
+      if (t < nt) acc[t].mac(av, xc[t * xcs + k * xes]);
+  }
+#pragma unroll
+  for (int t = 0; t < TC; ++t) {
+    if (t < nt) {
+      const double2 v = ff_total(acc[t]);
+      if (part)
+        part[((int64_t)blockIdx.z * ncols + c0 + t) * m + i] = v;
+      else
+        combine64(y + i * yes + (c0 + t) * ycs, v, ar, ai, br, bi);
+    }
+  }
+}
+
+__global__ void k_modek_ff(const float4* __restrict__ A, int64_t s1, int64_t dout, int64_t din, int64_t s3,
+                           const float4* __restrict__ x, int64_t xes, int64_t xcs, double2* __restrict__ y,
+                           int64_t yes, int64_t ycs, int64_t ncols, double ar, double ai, double br, double bi) {
+  const int64_t len = s1 * dout * s3;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t c = blockIdx.y;
+  if (i >= len || c >= ncols) return;
+  int64_t a, t, j, b;
+  udivmod(i, s1, t, a);
+  udivmod(t, dout, b, j);
+  const float4* xc = x + c * xcs;
+  gather::AccFF acc;
+  acc.zero();
+  for (int64_t k = 0; k < din; ++k) acc.mac(A[j + k * dout], xc[(a + s1 * (k + din * b)) * xes]);
+  combine64(y + i * yes + c * ycs, ff_total(acc), ar, ai, br, bi);
 }
 
 // The k ranges' partial sums of k_dense added in order, then alpha / beta.
@@ -330,20 +399,56 @@ void dense_typed(const void* a, int64_t m, int64_t n, c128 alpha, const void* x,
     QOB_LAUNCHED();
   }
 }
+void dense_ff(const void* a, int64_t m, int64_t n, c128 alpha, const void* x, int64_t xes, int64_t xcs,
+              c128 beta, void* y, int64_t yes, int64_t ycs, int64_t ncols, Workspace* ws, int slot,
+              cudaStream_t s) {
+  const int tc = ncols >= 4 ? 4 : ncols >= 2 ? 2 : 1;
+  int kch = ws ? dense_kchunks(m, n, ncols, tc) : 1;
+  double2* part = nullptr;
+  if (kch > 1) part = static_cast<double2*>(ws->get(slot, (size_t)kch * ncols * m * sizeof(double2)));
+  const int64_t kc = (n + kch - 1) / kch;
+  kch = (int)((n + kc - 1) / kc);
+  const dim3 grid(blocks_for(m, 128), (unsigned)((ncols + tc - 1) / tc), (unsigned)kch);
+  const float4* A = (const float4*)a;
+  const float4* X = (const float4*)x;
+  double2* Y = (double2*)y;
+  switch (tc) {
+    case 4:
+      k_dense_ff<4><<<grid, 128, 0, s>>>(A, m, n, X, xes, xcs, Y, yes, ycs, ncols, kc, part, alpha.re, alpha.im,
+                                         beta.re, beta.im);
+      break;
+    case 2:
+      k_dense_ff<2><<<grid, 128, 0, s>>>(A, m, n, X, xes, xcs, Y, yes, ycs, ncols, kc, part, alpha.re, alpha.im,
+                                         beta.re, beta.im);
+      break;
+    default:
+      k_dense_ff<1><<<grid, 128, 0, s>>>(A, m, n, X, xes, xcs, Y, yes, ycs, ncols, kc, part, alpha.re, alpha.im,
+                                         beta.re, beta.im);
+  }
+  QOB_LAUNCHED();
+  if (part) {
+    k_dense_reduce<double2, double><<<dim3(blocks_for(m, 128), (unsigned)ncols), 128, 0, s>>>(
+        part, kch, m, ncols, Y, yes, ycs, alpha.re, alpha.im, beta.re, beta.im);
+    QOB_LAUNCHED();
+  }
+}
 }  // namespace
 
 void launch_dense(int precision, const void* a, int64_t m, int64_t n, c128 alpha, const void* x,
                   int64_t xes, int64_t xcs, c128 beta, void* y, int64_t yes, int64_t ycs,
-                  int64_t ncols, cudaStream_t s, Workspace* ws, int slot) {
+                  int64_t ncols, cudaStream_t s, Workspace* ws, int slot, bool ff) {
   if (m == 0 || ncols == 0) return;
   const size_t esz = precision == QOB_C128 ? 16 : 8;
   if (ncols > 65535 * 8) {  // grid.y limit: split the vectors
     for (int64_t c0 = 0; c0 < ncols; c0 += 65535 * 8)
       launch_dense(precision, a, m, n, alpha, (const char*)x + c0 * xcs * esz, xes, xcs, beta,
-                   (char*)y + c0 * ycs * esz, yes, ycs, std::min<int64_t>(65535 * 8, ncols - c0), s, ws, slot);
+                   (char*)y + c0 * ycs * esz, yes, ycs, std::min<int64_t>(65535 * 8, ncols - c0), s, ws, slot,
+                   ff);
     return;
   }
-  if (precision == QOB_C128)
+  if (ff)
+    dense_ff(a, m, n, alpha, x, xes, xcs, beta, y, yes, ycs, ncols, ws, slot, s);
+  else if (precision == QOB_C128)
     dense_typed<double2, double>(a, m, n, alpha, x, xes, xcs, beta, y, yes, ycs, ncols, ws, slot, s);
   else
     dense_typed<float2, float>(a, m, n, alpha, x, xes, xcs, beta, y, yes, ycs, ncols, ws, slot, s);
@@ -351,18 +456,21 @@ void launch_dense(int precision, const void* a, int64_t m, int64_t n, c128 alpha
 
 void launch_modek(int precision, const void* a, bool eye, int64_t s1, int64_t dout, int64_t din,
                   int64_t s3, c128 alpha, const void* x, int64_t xes, int64_t xcs, c128 beta,
-                  void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s) {
+                  void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s, bool ff) {
   const int64_t len = s1 * dout * s3;
   if (len == 0 || ncols == 0) return;
   const size_t esz = precision == QOB_C128 ? 16 : 8;
   if (ncols > 65535) {  // grid.y limit: split the vectors
     for (int64_t c0 = 0; c0 < ncols; c0 += 65535)
       launch_modek(precision, a, eye, s1, dout, din, s3, alpha, (const char*)x + c0 * xcs * esz, xes, xcs,
-                   beta, (char*)y + c0 * ycs * esz, yes, ycs, std::min<int64_t>(65535, ncols - c0), s);
+                   beta, (char*)y + c0 * ycs * esz, yes, ycs, std::min<int64_t>(65535, ncols - c0), s, ff);
     return;
   }
   dim3 grid(blocks_for(len, 256), (unsigned)ncols);
-  if (precision == QOB_C128) {
+  if (ff && !eye) {
+    k_modek_ff<<<grid, 256, 0, s>>>((const float4*)a, s1, dout, din, s3, (const float4*)x, xes, xcs, (double2*)y,
+                                    yes, ycs, ncols, alpha.re, alpha.im, beta.re, beta.im);
+  } else if (precision == QOB_C128) {
     if (eye)
       k_modek<double2, double, true><<<grid, 256, 0, s>>>(nullptr, s1, dout, din, s3, (const double2*)x, xes,
                                                           xcs, (double2*)y, yes, ycs, ncols, alpha.re,

@@ -627,6 +627,28 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
 // Pauli / ladder / number product, single dense factors of any size -- and
 // chain for several wide (dense) factors, e.g. 64 x 64 and 16 x 16 dense
 // factors: 1024 entries per merged row against 80 multiply-adds per element.
+// A complex matrix in the plan's storage: ComplexF64, ComplexF32, or for a
+// double-float plan (hi, lo) float pairs of the real and imaginary parts.
+static void upload_matrix(DeviceBuf& d, const std::vector<c128>& a, const Plan& P) {
+  if (P.ff) {
+    std::vector<float> q(4 * a.size());
+    for (size_t k = 0; k < a.size(); ++k) {
+      const float rh = (float)a[k].re, ih = (float)a[k].im;
+      q[4 * k] = rh;
+      q[4 * k + 1] = (float)(a[k].re - (double)rh);
+      q[4 * k + 2] = ih;
+      q[4 * k + 3] = (float)(a[k].im - (double)ih);
+    }
+    upload_vec(d, q);
+  } else if (P.precision == QOB_C128) {
+    upload_vec(d, a);
+  } else {
+    std::vector<c64> a32(a.size());
+    for (size_t k = 0; k < a.size(); ++k) a32[k] = {(float)a[k].re, (float)a[k].im};
+    upload_vec(d, a32);
+  }
+}
+
 static bool gatherable_factor_sizes(const std::vector<const RowList*>& rl, int64_t nrows) {
   double entries = (double)nrows, prod = 1.0, sum = 0.0;
   for (auto* r : rl) {
@@ -646,6 +668,7 @@ static std::unique_ptr<Plan> compile_sum(Context& ctx, const NodeP& root, int si
   P->kind = Plan::Kind::Sum;
   P->side = side;
   P->precision = precision == QOB_C128X ? QOB_C128 : precision;
+  P->ff = precision == QOB_C128X;
   const bool tr = (side == QOB_RIGHT);
   P->m = tr ? root->n : root->m;  // output vector length
   P->n = tr ? root->m : root->n;  // input vector length
@@ -732,13 +755,7 @@ static std::unique_ptr<Plan> compile_sum(Context& ctx, const NodeP& root, int si
             std::vector<c128> a(st.dout * st.din, c128{0.0, 0.0});
             for (int64_t row = 0; row < r.rows; ++row)
               for (int64_t p = r.ptr[row]; p < r.ptr[row + 1]; ++p) a[row + r.col[p] * st.dout] = r.val[p];
-            if (P->precision == QOB_C128) {
-              upload_vec(st.a, a);
-            } else {
-              std::vector<c64> a32(a.size());
-              for (size_t k = 0; k < a.size(); ++k) a32[k] = {(float)a[k].re, (float)a[k].im};
-              upload_vec(st.a, a32);
-            }
+            upload_matrix(st.a, a, *P);
             mp.steps.push_back(std::move(st));
           }
           // non-square subsystems without factors: explicit isometries (:491-514)
@@ -784,13 +801,7 @@ static std::unique_ptr<Plan> compile_sum(Context& ctx, const NodeP& root, int si
                 v = nd->vals[r + c * nd->sm];
               a[i + j * dp.m] = v;
             }
-          if (P->precision == QOB_C128) {
-            upload_vec(dp.a, a);
-          } else {
-            std::vector<c64> a32(a.size());
-            for (size_t k = 0; k < a.size(); ++k) a32[k] = {(float)a[k].re, (float)a[k].im};
-            upload_vec(dp.a, a32);
-          }
+          upload_matrix(dp.a, a, *P);
           P->dense.push_back(std::move(dp));
           break;
         }
@@ -900,6 +911,7 @@ std::unique_ptr<Plan> compile_plan(Context& ctx, const NodeP& op, int side, int 
     P->kind = Plan::Kind::Product;
     P->side = side;
     P->precision = layout;
+    P->ff = precision == QOB_C128X;
     const bool tr = (side == QOB_RIGHT);
     P->m = tr ? op->n : op->m;
     P->n = tr ? op->m : op->n;

@@ -317,6 +317,7 @@ struct Plan {
   enum class Kind { Sum, Product, Fft } kind = Kind::Sum;
   int side = QOB_LEFT;
   int precision = QOB_C128;
+  bool ff = false;  // QOB_C128X: gather, dense and mode-product passes in double-float arithmetic
   int64_t m = 0, n = 0;  // rows of the output vectors / of the input vectors
   // Sum
   std::unique_ptr<GatherPlan> gather;
@@ -403,12 +404,16 @@ void launch_scale(int precision, void* y, int64_t rows, int64_t cols, int64_t ld
                   int64_t ld_col, c128 beta, cudaStream_t s);
 // ws / slot: room for the partial sums of a product split over column ranges
 // (no split without it)
+// ff: double-float form (a: (hi, lo) quadruples, x split by launch_ff_split)
 void launch_dense(int precision, const void* a, int64_t m, int64_t n, c128 alpha, const void* x,
                   int64_t xes, int64_t xcs, c128 beta, void* y, int64_t yes, int64_t ycs,
-                  int64_t ncols, cudaStream_t s, Workspace* ws = nullptr, int slot = 0);
+                  int64_t ncols, cudaStream_t s, Workspace* ws = nullptr, int slot = 0, bool ff = false);
+// Split of ncols vectors of n ComplexF64 elements (element stride es, vector
+// stride cs) into double-float quadruples at the same offsets of out.
+void launch_ff_split(const void* x, int64_t n, int64_t ncols, int64_t es, int64_t cs, void* out, cudaStream_t s);
 void launch_modek(int precision, const void* a, bool eye, int64_t s1, int64_t dout, int64_t din,
                   int64_t s3, c128 alpha, const void* x, int64_t xes, int64_t xcs, c128 beta,
-                  void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s);
+                  void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s, bool ff = false);
 void launch_axpby(int precision, const void* x, int64_t xes, int64_t xcs, c128 alpha, void* y,
                   int64_t yes, int64_t ycs, c128 beta, int64_t len, int64_t ncols,
                   cudaStream_t s);

@@ -400,7 +400,7 @@ def dense(ctx, stream):
         b = GenericBasis(nd)
         op = O.Operator(b, b, np.asfortranarray(rng.complex_normal(nd * nd).reshape(nd, nd, order="F")))
         h = handle(ctx, op)
-        for tdt, npdt, code, label in (m for m in _modes() if m[2] != L.QOB_C128X):
+        for tdt, npdt, code, label in _modes():
             for ncols in kets:
                 x = _cols(nd, ncols, tdt, 71)
                 y = _cols(nd, ncols, tdt, 72)

@@ -238,3 +238,21 @@ def test_fp32_data_rejects_double_float():
     out = to_device(rand_state(rng, H.basis_l), dtype=np.complex64)
     with pytest.raises(O.ArgumentError):
         mul_(out, H, psi, 1.0, 0.0, arith="ff")
+
+
+@pytest.mark.parametrize("ncols", [1, 5])
+def test_dense_operator_double_float(ncols):
+    """A 700 x 500 DenseOperator (dense pass, split over column ranges) and its
+    product with a 2-factor dense LazyTensor (mode products), both in
+    double-float arithmetic."""
+    rng = Q.Rng(913 + ncols)
+    bl, br = Q.GenericBasis(700), Q.GenericBasis(500)
+    D = rand_op(rng, bl, br)
+    X = O.Operator(br, Q.GenericBasis(ncols), rng.kets_data(500, ncols))
+    Y = O.Operator(bl, Q.GenericBasis(ncols), rng.kets_data(700, ncols))
+    assert check(Y, D, X, AL, 0.4 - 0.9j) < 1e-13
+    b1, b2 = Q.GenericBasis(40), Q.GenericBasis(30)
+    b = Q.tensor_basis(b1, b2)
+    lt = O.LazyTensor(b, b, (1, 2), (rand_op(rng, b1, b1), rand_op(rng, b2, b2)), 0.6)
+    psi, out = rand_state(rng, b), rand_state(rng, b)
+    assert check(out, lt, psi) < 1e-13
