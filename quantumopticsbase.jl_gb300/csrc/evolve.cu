@@ -175,6 +175,8 @@ struct EvolveState {
 };
 
 void ensemble_build(Context& ctx, Ensemble& E, const std::vector<EvolveState>& states, int prec) {
+  // QOB_C128X: ComplexF64 states (FP64 stage kernels), operators in double-float
+  prec = prec == QOB_C128X ? QOB_C128 : prec;
   E.prec = prec;
   E.from_psi.clear();
   E.from_tmp.clear();
@@ -305,7 +307,7 @@ struct qob_server {
 
 namespace {
 
-size_t elem_bytes(int dtype) { return dtype == QOB_C128 ? 16 : 8; }
+size_t elem_bytes(int dtype) { return dtype == QOB_C64 ? 8 : 16; }
 
 // Admit queued requests while a slot and memory are free (lock held).
 void admit(qob_server* S) {
@@ -538,7 +540,8 @@ extern "C" {
 
 int qob_server_create(qob_ctx* ctx, int dtype, size_t mem_budget, int max_active, int renormalise,
                       qob_server** out) {
-  if (!ctx || !out || (dtype != QOB_C128 && dtype != QOB_C64) || max_active < 1) return QOB_ERR_ARG;
+  if (!ctx || !out || (dtype != QOB_C128 && dtype != QOB_C64 && dtype != QOB_C128X) || max_active < 1)
+    return QOB_ERR_ARG;
   auto* S = new qob_server;
   S->ctx = ctx;
   S->dtype = dtype;
@@ -710,9 +713,10 @@ int qob_rk4(qob_ctx* ctx, qob_op* H, int dtype, void* psi, int64_t n, double dt,
   if (!ctx) return QOB_ERR_ARG;
   try {
     QOB_CUDA(cudaSetDevice(ctx->c.device));
-    if (!H || !psi || n < 1 || (dtype != QOB_C128 && dtype != QOB_C64)) qob::fail(QOB_ERR_ARG, "qob_rk4: bad arguments");
+    if (!H || !psi || n < 1 || (dtype != QOB_C128 && dtype != QOB_C64 && dtype != QOB_C128X))
+      qob::fail(QOB_ERR_ARG, "qob_rk4: bad arguments");
     if (H->node->m != n || H->node->n != n) qob::fail(QOB_ERR_DIM, "Hamiltonian and state dimensions differ");
-    const size_t sz = (size_t)n * (dtype == QOB_C128 ? 16 : 8);
+    const size_t sz = (size_t)n * (dtype == QOB_C64 ? 8 : 16);
     char* w = static_cast<char*>(ctx->c.ws.get(20, 3 * sz));
     qob::Plan& P = qob::batch_plan(ctx->c, H, dtype);
     qob::Ensemble E;
@@ -778,7 +782,7 @@ int qob_rk4_td(qob_ctx* ctx, qob_op* H, int dtype, void* psi, int64_t n, double 
   if (!ctx) return QOB_ERR_ARG;
   try {
     QOB_CUDA(cudaSetDevice(ctx->c.device));
-    if (!H || !psi || n < 1 || nsteps < 0 || (dtype != QOB_C128 && dtype != QOB_C64))
+    if (!H || !psi || n < 1 || nsteps < 0 || (dtype != QOB_C128 && dtype != QOB_C64 && dtype != QOB_C128X))
       qob::fail(QOB_ERR_ARG, "qob_rk4_td: bad arguments");
     if (H->node->kind != qob::Kind::LazySum) qob::fail(QOB_ERR_ARG, "qob_rk4_td needs a LazySum");
     if (nrows != 2 * (int64_t)nsteps + 1) qob::fail(QOB_ERR_ARG, "qob_rk4_td: nrows must be 2*nsteps+1");
@@ -786,7 +790,7 @@ int qob_rk4_td(qob_ctx* ctx, qob_op* H, int dtype, void* psi, int64_t n, double 
     if (nf > 0 && !factors) qob::fail(QOB_ERR_ARG, "qob_rk4_td: null factor table");
     if (H->node->m != n || H->node->n != n) qob::fail(QOB_ERR_DIM, "Hamiltonian and state dimensions differ");
     cudaStream_t st = (cudaStream_t)stream;
-    const size_t sz = (size_t)n * (dtype == QOB_C128 ? 16 : 8);
+    const size_t sz = (size_t)n * (dtype == QOB_C64 ? 8 : 16);
     char* w = static_cast<char*>(ctx->c.ws.get(20, 3 * sz));
     qob::Plan& P = qob::batch_plan(ctx->c, H, dtype);
     if (P.kind != qob::Plan::Kind::Sum || !P.dense.empty() || !P.modek.empty() || !P.subs.empty())

@@ -74,18 +74,23 @@ def factor_rows(H: O.TimeDependentSum, t0: float, dt: float, nsteps: int) -> np.
     return rows
 
 
-def rk4(H, psi, dt: float, nsteps: int, renormalise: bool = False, t0: float = 0.0):
+def rk4(H, psi, dt: float, nsteps: int, renormalise: bool = False, t0: float = 0.0, arith: str | None = None):
     """In-place RK4 on a device Ket (or a contiguous CUDA tensor).
 
     A ``TimeDependentSum`` is evolved with its coefficients evaluated on the host
     at every stage time (as ``set_time!`` would, src/time_dependent_operator.jl:162-171)
     and applied on the device inside the steps; afterwards its current time is
-    t0 + nsteps*dt."""
+    t0 + nsteps*dt.  ``arith="ff"``: ComplexF64 states with the operator applied
+    in double-float arithmetic (QOB_C128X)."""
     data = psi.data if hasattr(psi, "data") and not hasattr(psi, "data_ptr") else psi
     ctx = get_context(data.device.index)
     import torch
 
     dt_code = L.QOB_C64 if data.dtype == torch.complex64 else L.QOB_C128
+    if arith == "ff":
+        if data.dtype != torch.complex128:
+            raise O.ArgumentError('arith="ff" (double-float) applies to ComplexF64 states')
+        dt_code = L.QOB_C128X
     s = C.c_void_p(torch.cuda.current_stream(data.device.index).cuda_stream)
     if isinstance(H, O.TimeDependentSum):
         h = handle(ctx, H)
@@ -104,11 +109,18 @@ class Server:
     """Continuous-batching server of RK4 time-evolution requests."""
 
     def __init__(self, dtype=np.complex128, mem_budget: int = 8 << 30, max_active: int = 256,
-                 renormalise: bool = False, device: int = 0):
+                 renormalise: bool = False, device: int = 0, arith: str | None = None):
+        """``arith="ff"``: ComplexF64 requests with the operators applied in
+        double-float arithmetic (QOB_C128X)."""
         self.ctx: Context = get_context(device)
         self.dtype = np.dtype(dtype)
+        code = dtype_code(self.dtype)
+        if arith == "ff":
+            if self.dtype != np.complex128:
+                raise O.ArgumentError('arith="ff" (double-float) applies to ComplexF64 requests')
+            code = L.QOB_C128X
         p = C.c_void_p()
-        raise_for(L.lib().qob_server_create(self.ctx.ptr, dtype_code(self.dtype), int(mem_budget), int(max_active),
+        raise_for(L.lib().qob_server_create(self.ctx.ptr, code, int(mem_budget), int(max_active),
                                             int(renormalise), C.byref(p)), self.ctx)
         self.ptr = p
         self._ops = {}

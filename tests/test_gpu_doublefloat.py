@@ -256,3 +256,41 @@ def test_dense_operator_double_float(ncols):
     lt = O.LazyTensor(b, b, (1, 2), (rand_op(rng, b1, b1), rand_op(rng, b2, b2)), 0.6)
     psi, out = rand_state(rng, b), rand_state(rng, b)
     assert check(out, lt, psi) < 1e-13
+
+
+def test_rk4_and_server_double_float():
+    """RK4 with the operator in double-float arithmetic (ComplexF64 states and
+    stage arithmetic): time-dependent steps against the host RK4, a static chain
+    against the FP64 device RK4, and both served in a mix, each request equal
+    bitwise to the same evolution run alone."""
+    import torch
+
+    from qobgpu.evolution import Server, rk4
+    from test_gpu_timedependent import rk4_host_td, td_heisenberg
+
+    dt, nsteps, t0 = 2e-3, 40, 0.1
+    td = td_heisenberg(8, seed=920)
+    static = heisenberg_chain(8, seed=921)
+    rng = Q.Rng(922)
+    p_td, p_st = rng.ket_data(len(td.basis_l)), rng.ket_data(len(static.basis_l))
+    ref_td = rk4_host_td(td, p_td, dt, nsteps, t0)
+    d = torch.as_tensor(p_td.copy(), device="cuda:0")
+    rk4(td, d, dt, nsteps, t0=t0, arith="ff")
+    alone_td = d.cpu().numpy()
+    assert rel_l2(alone_td, ref_td) < TOL
+    d64 = torch.as_tensor(p_st.copy(), device="cuda:0")
+    rk4(static, d64, dt, nsteps)
+    dff = torch.as_tensor(p_st.copy(), device="cuda:0")
+    rk4(static, dff, dt, nsteps, arith="ff")
+    alone_st = dff.cpu().numpy()
+    assert rel_l2(alone_st, d64.cpu().numpy()) < TOL
+    S = Server(np.complex128, arith="ff")
+    i_st = S.submit(static, p_st, nsteps, dt)
+    i_td = S.submit(td, p_td, nsteps, dt, t0=t0)
+    while S.step():
+        pass
+    for i, a in ((i_st, alone_st), (i_td, alone_td)):
+        st, _, got = S.poll(i)
+        assert st == 2
+        assert np.array_equal(got, a), "served result differs from the same evolution run alone"
+    S.close()
