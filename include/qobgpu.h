@@ -47,10 +47,10 @@ extern "C" {
 /* element types */
 #define QOB_C128 0 /* ComplexF64 */
 #define QOB_C64 1  /* ComplexF32 */
-/* ComplexF64 data with the fused LazySum part, dense operators and mode
- * products applied in double-float arithmetic (each number the unevaluated
+/* ComplexF64 data with the fused LazySum part, dense operators, mode
+ * products and FFT operators applied in double-float arithmetic (each number the unevaluated
  * sum of two FP32 numbers, about 48 significant bits) on the FP32 pipes, which
- * on GB300 issue far faster than its FP64 pipe; FFT passes run in FP64.  Results
+ * on GB300 issue far faster than its FP64 pipe (FFT passes too).  Results
  * agree with QOB_C128 to about 1e-14 relative (l2).  Magnitudes of vector
  * elements, operator entries, alpha and beta in [2^-74, 2^128) keep full
  * precision; smaller ones keep 24 bits and below 2^-126 flush to zero; larger

@@ -174,10 +174,11 @@ void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, i
       if (a + 1 == na) {
         void* scratch = P.fft[a].n1 > 0 ? ctx.ws.get(ws + 2, (size_t)P.m * ncols * esz) : nullptr;
         launch_fft_pass(P.precision, P.fft[a], P.m, src, ses, scs, y, yes, ycs, ncols, alpha, beta, true, scratch,
-                        s);
+                        s, P.ff);
       } else {
         void* t = ctx.ws.get(ws + (a % 2), (size_t)P.m * ncols * esz);
-        launch_fft_pass(P.precision, P.fft[a], P.m, src, ses, scs, t, 1, P.m, ncols, one, zero, false, nullptr, s);
+        launch_fft_pass(P.precision, P.fft[a], P.m, src, ses, scs, t, 1, P.m, ncols, one, zero, false, nullptr, s,
+                        P.ff);
         src = t;
         ses = 1;
         scs = P.m;

@@ -285,6 +285,13 @@ __device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
   pe = __fmaf_rn(a.y, b.x, pe);
   return make_float2(p, pe);
 }
+// sum of two double-float numbers: two-sum of the high parts, the low parts added
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+  const float s = a.x + b.x;
+  const float bb = s - a.x;
+  const float err = (a.x - (s - bb)) + (b.x - bb);
+  return make_float2(s, err + (a.y + b.y));
+}
 __device__ __forceinline__ float2 ff_neg(float2 a) { return make_float2(-a.x, -a.y); }
 
 // Double-float accumulator of one complex value: acc += v * x with the

@@ -905,7 +905,7 @@ static void finalize_gather(GatherPlan& gp, GatherBuilder& B, const OpNode* root
 // gathers store and apply their values in double-float arithmetic
 std::unique_ptr<Plan> compile_plan(Context& ctx, const NodeP& op, int side, int precision) {
   const int layout = precision == QOB_C128X ? QOB_C128 : precision;
-  if (op->kind == Kind::Fft) return compile_fft(op, side, layout);
+  if (op->kind == Kind::Fft) return compile_fft(op, side, precision);
   if (op->kind == Kind::LazyProduct) {
     auto P = std::make_unique<Plan>();
     P->kind = Plan::Kind::Product;

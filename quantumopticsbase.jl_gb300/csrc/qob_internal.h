@@ -397,7 +397,7 @@ void launch_td_advance(long long* step, cudaStream_t s);
 // four-step FFT over many blocks.
 void launch_fft_pass(int precision, const FftAxis& ax, int64_t len, const void* x, int64_t xes, int64_t xcs,
                      void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta, bool final,
-                     void* scratch, cudaStream_t s);
+                     void* scratch, cudaStream_t s, bool ff = false);
 std::unique_ptr<Plan> compile_fft(const NodeP& op, int side, int precision);
 int gather_tile(const GatherPlan& g, int64_t ncols);
 void launch_scale(int precision, void* y, int64_t rows, int64_t cols, int64_t ld_row,

@@ -267,15 +267,15 @@ def particle(ctx, stream):
         H = O.LazySum(bX, bX, [1.0, 1.0], (O.LazyProduct((Txp, K, Tpx)), V))
         for op_name, op in (("H", H), ("Tpx", Tpx)):
             h = handle(ctx, op)
-            for tdt, npdt in ((torch.complex128, np.complex128), (torch.complex64, np.complex64)):
+            for tdt, npdt, code, label in _modes():
                 for ncols in ((1, 64) if len(bxs) == 1 else (1,)):
                     x = _cols(n, ncols, tdt, 50).contiguous() if ncols == 1 else _cols(n, ncols, tdt, 50)
                     y = _cols(n, ncols, tdt, 51).contiguous() if ncols == 1 else _cols(n, ncols, tdt, 51)
                     reps = 20
                     ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, L.QOB_LEFT, n, n, ncols, x, y,
-                                                                 dtype_code(npdt), reps=reps))
+                                                                 code, reps=reps))
                     t = ms * 1e-3 / reps
-                    out.append({"grid": name, "operator": op_name, "dtype": np.dtype(npdt).name, "kets": ncols,
+                    out.append({"grid": name, "operator": op_name, "dtype": label, "kets": ncols,
                                 "us_per_call": t * 1e6, "applies_per_s": ncols / t})
     return {"workload": "particle", "results": out}
 

@@ -294,3 +294,35 @@ def test_rk4_and_server_double_float():
         assert st == 2
         assert np.array_equal(got, a), "served result differs from the same evolution run alone"
     S.close()
+
+
+@pytest.mark.parametrize("n", [200, 256, 4096])
+def test_fft_transforms_double_float(n):
+    """FFTOperator passes in double-float arithmetic: direct DFT (200 points),
+    radix-2 Stockham (256), the four-step form (4096 points, one ket), kets and
+    bras, and a 2-D composite transform; plus the particle Hamiltonian
+    Txp (p^2/2) Tpx + V (a LazySum holding a LazyProduct of FFT operators)."""
+    from qobgpu.bases import MomentumBasis, PositionBasis
+    from qobgpu.particle import momentum, potentialoperator, transform
+
+    bx = PositionBasis(-32.5, 20.1, n)
+    bp = MomentumBasis(bx)
+    rng = Q.Rng(930 + n)
+    al, be = 0.7 - 0.2j, 0.3 + 0.1j
+    for T in (transform(bp, bx), transform(bx, bp)):
+        x, y = rng.complex_normal(n), rng.complex_normal(n)
+        assert check(Q.Ket(T.basis_l, y), T, Q.Ket(T.basis_r, x), al, be) < 1e-13
+        assert check(Q.Bra(T.basis_r, y), Q.Bra(T.basis_l, x), T, al, be) < 1e-13
+    Tpx, Txp = transform(bp, bx), transform(bx, bp)
+    pd = np.asarray(momentum(bp).data.diagonal())
+    K = O.Operator(bp, bp, O.spdiagm(n, n, {0: pd * pd / 2}))
+    V = potentialoperator(bx, lambda q: 0.5 * q * q)
+    H = O.LazySum(bx, bx, [1.0, 1.0], (O.LazyProduct((Txp, K, Tpx)), V))
+    psi, out = rand_state(rng, bx), rand_state(rng, bx)
+    check(out, H, psi)
+    bxs = [PositionBasis(-3.0, 4.0, 32), PositionBasis(-4.0, 5.0, 21)]
+    bX, bP = Q.tensor_basis(*bxs), Q.tensor_basis(*[MomentumBasis(b) for b in bxs])
+    T2 = transform(bP, bX)
+    m = len(bX)
+    x, y = rng.complex_normal(m), rng.complex_normal(m)
+    check(Q.Ket(T2.basis_l, y), T2, Q.Ket(T2.basis_r, x), al, be)
