@@ -19,6 +19,7 @@
 // The same tables drive the serving engine's batched RK4 stages (evolve.cu).
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 
 #include "batch.h"
 #include "k_gather.cuh"
@@ -50,7 +51,7 @@ __global__ void __launch_bounds__(256) k_gather_batch(const BatchItemDev* __rest
       CT* yp = (CT*)it.y + J;
       // beta == 0 overwrites y without reading it (NaN in y is ignored)
       const bool bz = it.beta.x == 0.0 && it.beta.y == 0.0;
-      if constexpr (sizeof(R) == 8) {
+      if constexpr (std::is_same<R, gather::DFX>::value || sizeof(R) == 8) {
         if (bz)
           gather::combine<0>(yp, acc[0].total(), it.alpha, it.beta);
         else
@@ -74,7 +75,8 @@ size_t ell_size(int prec, bool real) {
   return real ? sizeof(EllF) : sizeof(EllC);
 }
 
-const void* batch_kernel(int prec, bool real) {
+const void* batch_kernel(int prec, bool real, bool ff) {
+  if (ff) return real ? (const void*)k_gather_batch<gather::DFX, true> : (const void*)k_gather_batch<gather::DFX, false>;
   return prec == QOB_C128 ? (real ? (const void*)k_gather_batch<double, true> : (const void*)k_gather_batch<double, false>)
                           : (real ? (const void*)k_gather_batch<float, true> : (const void*)k_gather_batch<float, false>);
 }
@@ -83,7 +85,7 @@ const void* batch_kernel(int prec, bool real) {
 
 bool plan_fusable(const Plan& P) {
   return P.kind == Plan::Kind::Sum && P.gather && P.dense.empty() && P.modek.empty() && P.subs.empty() &&
-         P.gather->square && !P.gather->phased && !P.gather->ff && P.gather->ngroups <= 256 && P.nterms_total > 0;
+         P.gather->square && !P.gather->phased && P.gather->ngroups <= 256 && P.nterms_total > 0;
 }
 
 void build_tables(Context& ctx, BatchTables& T, const std::vector<BatchSpec>& specs, int prec, int tile) {
@@ -91,16 +93,20 @@ void build_tables(Context& ctx, BatchTables& T, const std::vector<BatchSpec>& sp
   std::vector<int2> tiles;
   T.prec = prec;
   T.real = true;
+  T.ff = false;
   T.smem = 0;
   T.fused.assign(specs.size(), false);
   for (size_t i = 0; i < specs.size(); ++i) {
     T.fused[i] = plan_fusable(*specs[i].plan);
     if (T.fused[i]) T.real &= specs[i].plan->gather->real_vals;
+    if (T.fused[i]) T.ff |= specs[i].plan->gather->ff;
   }
   for (size_t i = 0; i < specs.size(); ++i) {
     if (!T.fused[i]) continue;
     const GatherPlan& g = *specs[i].plan->gather;
-    if (g.real_vals != T.real) {  // real items in a batch with complex ones run apart
+    // real items in a batch with complex ones, and FP64 items beside
+    // double-float ones, run apart
+    if (g.real_vals != T.real || g.ff != T.ff) {
       T.fused[i] = false;
       continue;
     }
@@ -129,7 +135,7 @@ void build_tables(Context& ctx, BatchTables& T, const std::vector<BatchSpec>& sp
   // persistent grid: as many 256-thread blocks as are resident at once
   int per_sm = 1;
   if (T.ntiles > 0) {
-    const void* kern = batch_kernel(prec, T.real);
+    const void* kern = batch_kernel(prec, T.real, T.ff);
     if (T.smem > 48 * 1024)
       QOB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T.smem));
     QOB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, T.smem));
@@ -142,7 +148,12 @@ void launch_tables(Context& ctx, const BatchTables& T, const std::vector<BatchSp
   if (T.ntiles > 0) {
     const BatchItemDev* it = (const BatchItemDev*)T.items.p;
     const int2* tl = (const int2*)T.tiles.p;
-    if (T.prec == QOB_C128) {
+    if (T.ff) {
+      if (T.real)
+        k_gather_batch<gather::DFX, true><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile);
+      else
+        k_gather_batch<gather::DFX, false><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile);
+    } else if (T.prec == QOB_C128) {
       if (T.real)
         k_gather_batch<double, true><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile);
       else

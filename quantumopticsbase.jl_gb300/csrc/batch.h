@@ -32,6 +32,7 @@ struct BatchTables {
   int nfused = 0;
   int tile = 256;
   bool real = true;
+  bool ff = false;  // double-float items (ComplexF64 data): the kernel splits x as it loads
   size_t smem = 0;
   int grid = 1;
 };

@@ -53,6 +53,10 @@ __device__ __forceinline__ uint32_t fmodu(uint32_t n, uint32_t d, uint64_t M) {
 
 // Precision tag of the double-float mode: ComplexF64 data, FP32-pair arithmetic.
 struct DF {};
+// The same arithmetic reading ComplexF64 vectors directly and splitting each
+// element as it is loaded (the persistent batch kernel, whose items' vectors
+// are read in place).
+struct DFX {};
 
 template <typename R>
 struct Cx;
@@ -67,6 +71,10 @@ struct Cx<float> {
 template <>
 struct Cx<DF> {
   using T = double2;  // y and alpha / beta: ComplexF64
+};
+template <>
+struct Cx<DFX> {
+  using T = double2;
 };
 
 // element type of the input vectors as the kernels read them: the data type,
@@ -99,6 +107,14 @@ struct Val<DF, true> {
 template <>
 struct Val<DF, false> {
   using T = float4;  // (re hi, re lo, im hi, im lo)
+};
+template <>
+struct Val<DFX, true> {
+  using T = float2;
+};
+template <>
+struct Val<DFX, false> {
+  using T = float4;
 };
 
 // fixed-width slot type per precision / realness, and its value
@@ -134,6 +150,8 @@ struct Ell<DF, false> {
   using T = EllZF;
   static __device__ __forceinline__ float4 v(const EllZF& e) { return make_float4(e.v[0], e.v[1], e.v[2], e.v[3]); }
 };
+template <int RV>
+struct Ell<DFX, RV> : Ell<DF, RV> {};
 
 // Value modes of a plan: complex entries; real entries (and a real diagonal);
 // real entries of groups that are either real or purely imaginary, with a
@@ -354,6 +372,24 @@ struct AccOf<float> {
 template <>
 struct AccOf<DF> {
   using T = AccFF;
+};
+
+// AccFF fed with ComplexF64 elements, split as they arrive (DFX)
+__device__ __forceinline__ float4 ff_split4(double2 x) {
+  const float2 a = ff_split(x.x), b = ff_split(x.y);
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+struct AccFFX : AccFF {
+  __device__ void mac(float2 v, double2 x) { AccFF::mac(v, ff_split4(x)); }
+  __device__ void mac_i(float2 v, double2 x) { AccFF::mac_i(v, ff_split4(x)); }
+  __device__ void mac(float4 v, double2 x) { AccFF::mac(v, ff_split4(x)); }
+  __device__ void mac_i(float4 v, double2 x) { AccFF::mac_i(v, ff_split4(x)); }
+  __device__ void set(float2 v, double2 x) { AccFF::set(v, ff_split4(x)); }
+  __device__ void set(float4 v, double2 x) { AccFF::set(v, ff_split4(x)); }
+};
+template <>
+struct AccOf<DFX> {
+  using T = AccFFX;
 };
 
 __device__ __forceinline__ double2 ld(const double2* p) { return __ldg(p); }
