@@ -55,9 +55,10 @@ extern "C" {
  * elements, operator entries, alpha and beta in [2^-74, 2^128) keep full
  * precision; smaller ones keep 24 bits and below 2^-126 flush to zero; larger
  * ones become infinite.  Accepted by qob_mul, qob_mul_host, qob_mul_host_async,
- * qob_op_prepare, qob_op_tune, qob_op_set_launch, qob_rk4, qob_rk4_td and
- * qob_server_create (ComplexF64 states, stage arithmetic and norms in FP64);
- * the other entry points take QOB_C128 or QOB_C64. */
+ * qob_op_prepare, qob_op_tune, qob_op_set_launch, qob_batch_create,
+ * qob_apply_batched, qob_rk4, qob_rk4_td and qob_server_create (ComplexF64
+ * states, stage arithmetic and norms in FP64); the other entry points take
+ * QOB_C128 or QOB_C64. */
 #define QOB_C128X 2
 
 /* sides of qob_mul */

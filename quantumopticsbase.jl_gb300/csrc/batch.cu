@@ -89,6 +89,7 @@ bool plan_fusable(const Plan& P) {
 }
 
 void build_tables(Context& ctx, BatchTables& T, const std::vector<BatchSpec>& specs, int prec, int tile) {
+  prec = prec == QOB_C128X ? QOB_C128 : prec;  // ComplexF64 data; the items' plans say double-float
   std::vector<BatchItemDev> dev;
   std::vector<int2> tiles;
   T.prec = prec;
@@ -224,7 +225,8 @@ extern "C" {
 
 int qob_batch_create(qob_ctx* ctx, int dtype, qob_batch** out) {
   return bguard(ctx, [&] {
-    if (!out || (dtype != QOB_C128 && dtype != QOB_C64)) qob::fail(QOB_ERR_ARG, "qob_batch_create: bad arguments");
+    if (!out || (dtype != QOB_C128 && dtype != QOB_C64 && dtype != QOB_C128X))
+      qob::fail(QOB_ERR_ARG, "qob_batch_create: bad arguments");
     auto* b = new qob_batch;
     b->dtype = dtype;
     *out = b;
@@ -235,7 +237,7 @@ int qob_batch_add(qob_ctx* ctx, qob_batch* b, qob_op* op, double alpha_re, doubl
                   double beta_re, double beta_im) {
   return bguard(ctx, [&] {
     if (!b || !op || !x || !y) qob::fail(QOB_ERR_ARG, "qob_batch_add: bad arguments");
-    const size_t esz = b->dtype == QOB_C128 ? 16 : 8;
+    const size_t esz = b->dtype == QOB_C64 ? 8 : 16;
     const char* px = static_cast<const char*>(x);
     const char* py = static_cast<const char*>(y);
     if (px < py + op->node->m * esz && py < px + op->node->n * esz)

@@ -26,11 +26,18 @@ def _ptr(t):
 class Batch:
     """y_i = alpha_i * op_i * x_i + beta_i * y_i for many kets in one launch."""
 
-    def __init__(self, dtype=np.complex128, device: int = 0):
+    def __init__(self, dtype=np.complex128, device: int = 0, arith: str | None = None):
+        """``arith="ff"``: ComplexF64 kets, operators applied in double-float
+        arithmetic (QOB_C128X)."""
         self.ctx = get_context(device)
         self.dtype = np.dtype(dtype)
+        code = dtype_code(self.dtype)
+        if arith == "ff":
+            if self.dtype != np.complex128:
+                raise O.ArgumentError('arith="ff" (double-float) applies to ComplexF64 kets')
+            code = L.QOB_C128X
         p = C.c_void_p()
-        raise_for(L.lib().qob_batch_create(self.ctx.ptr, dtype_code(self.dtype), C.byref(p)), self.ctx)
+        raise_for(L.lib().qob_batch_create(self.ctx.ptr, code, C.byref(p)), self.ctx)
         self.ptr = p
         self._keep = []
 

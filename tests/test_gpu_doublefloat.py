@@ -326,3 +326,29 @@ def test_fft_transforms_double_float(n):
     m = len(bX)
     x, y = rng.complex_normal(m), rng.complex_normal(m)
     check(Q.Ket(T2.basis_l, y), T2, Q.Ket(T2.basis_r, x), al, be)
+
+
+def test_uneven_batch_double_float():
+    """Uneven two-mode cavities in one persistent launch (the fused batch kernel
+    splitting each element as it loads), against the oracle."""
+    import torch
+
+    from qobgpu.evolution import Batch
+
+    rng = Q.Rng(940)
+    b = Batch(np.complex128, arith="ff")
+    refs, ys = [], []
+    for k in range(12):
+        n1, n2 = rng.integers(2, 3, 20)
+        H = two_mode_cavity(int(n1), int(n2), seed=941 + k)
+        n = len(H.basis_l)
+        x, y = rng.ket_data(n), rng.ket_data(n)
+        refs.append(OR.mul(Q.Ket(H.basis_l, y), H, Q.Ket(H.basis_r, x), AL, BE))
+        xt, yt = torch.as_tensor(x, device="cuda:0"), torch.as_tensor(y, device="cuda:0")
+        b.add(H, xt, yt, AL, BE)
+        ys.append(yt)
+    assert b.info()["fused"] == 12
+    b.run()
+    torch.cuda.synchronize()
+    for yt, r in zip(ys, refs):
+        assert rel_l2(yt.cpu().numpy(), r) < 1e-13
