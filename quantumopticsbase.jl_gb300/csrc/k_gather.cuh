@@ -712,24 +712,36 @@ __global__ void __launch_bounds__(256) k_gather_p(GatherView g, SiteTable st,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const ET* ell = stage<ET>(smem_raw, g);
   const GGroup* sg = reinterpret_cast<const GGroup*>(smem_raw);
-  const int64_t nj = (g.m + 31) / 32;
-  const int64_t nchunks = nj * (int64_t)((ncols + TC - 1) / TC);
+  // chunks of (32/ls output indices x ls sets of TC vectors), one per warp at a
+  // time, as in k_gather_j's lane split
+  const int ls = g.lane_split;
+  const int lsh = __ffs(ls) - 1, jsh = 5 - lsh;
+  const int lane = threadIdx.x & 31;
+  const int64_t nj = (g.m + (1 << jsh) - 1) >> jsh;
+  const int64_t per_tile = (int64_t)TC * ls;
+  const int64_t nchunks = nj * ((ncols + per_tile - 1) / per_tile);
   const int64_t lo = (int64_t)blockIdx.x * nchunks / gridDim.x;
   const int64_t hi = ((int64_t)blockIdx.x + 1) * nchunks / gridDim.x;
-  const int lane = threadIdx.x & 31;
+  const int64_t vs_x = (int64_t)ls * xcs, vs_y = (int64_t)ls * ycs;
   for (int64_t c = lo + (threadIdx.x >> 5); c < hi; c += blockDim.x >> 5) {
-    const int64_t tile = c / nj;
-    const int64_t J = (int64_t)(((uint64_t)(c - tile * nj) * g.jmul) % (uint64_t)nj) * 32 + lane;
-    if (J >= g.m) continue;
-    const int c0 = (int)tile * TC;
-    const int nt = min(TC, ncols - c0);
-    const XT* xb = x + (int64_t)c0 * xcs;
-    AT acc[TC];
-    accumulate<R, VM, SQUARE, W1, TC>(g, st, sg, ell, (uint32_t)J, xb, 1, xcs, nt, acc);
-    CT* yb = y + J + (int64_t)c0 * ycs;
+    int64_t tile, jc;
+    udivmod(c, nj, tile, jc);
+    if (g.jmul != 1u) {  // permuted order of the index chunks (jmul < nj, coprime)
+      int64_t q;
+      udivmod((int64_t)((uint64_t)jc * g.jmul), nj, q, jc);
+    }
+    const int64_t J = (jc << jsh) + (lane & ((1 << jsh) - 1));
+    const int c0 = (int)(tile * per_tile) + (lane >> jsh);
+    const int nt = c0 < ncols ? min(TC, (ncols - c0 + ls - 1) >> lsh) : 0;
+    if (J < g.m) {
+      const XT* xb = x + (int64_t)c0 * xcs;
+      AT acc[TC];
+      accumulate<R, VM, SQUARE, W1, TC>(g, st, sg, ell, (uint32_t)J, xb, 1, vs_x, nt, acc);
+      CT* yb = y + J + (int64_t)c0 * ycs;
 #pragma unroll
-    for (int t = 0; t < TC; ++t)
-      if (t < nt) combine<BMODE>(yb + t * ycs, acc[t].total(), alpha, beta);
+      for (int t = 0; t < TC; ++t)
+        if (t < nt) combine<BMODE>(yb + t * vs_y, acc[t].total(), alpha, beta);
+    }
   }
 }
 
@@ -776,6 +788,10 @@ void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t x
               int64_t ncols, typename Cx<R>::T a, typename Cx<R>::T b, size_t smem, cudaStream_t s) {
   using CT = typename Cx<R>::T;
   using XT = typename In<R>::T;
+  // a tuned lane split wider than this call's vectors fill (fewer vectors than
+  // the tuning, e.g. the chunks of a host call) is narrowed
+  int ls = v.lane_split > 0 ? v.lane_split : 1;
+  while (ls > 1 && (int64_t)TC * ls > ncols) ls >>= 1;
   if (v.block < 0 && ncols <= (int64_t)INT32_MAX) {
     // persistent grid: SMs x resident blocks of -v.block threads
     auto pk = k_gather_p<R, VM, SQUARE, W1, TC, BMODE>;
@@ -787,7 +803,9 @@ void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t x
     QOB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk, threads, smem));
     if (occ > 0) {
       GatherView w = v;
-      w.jmul = chunk_multiplier((v.m + 31) / 32);
+      w.lane_split = ls;
+      const int64_t jw = 32 / ls;
+      w.jmul = chunk_multiplier((v.m + jw - 1) / jw);
       pk<<<(unsigned)(sms * occ), threads, smem, s>>>(w, st, (const XT*)x, xcs, (CT*)y, ycs, (int)ncols, a, b);
       QOB_LAUNCHED();
       return;
@@ -796,10 +814,6 @@ void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t x
   auto kern = k_gather_j<R, VM, SQUARE, W1, TC, BMODE>;
   allow_smem(kern, smem);
   const int threads = v.block > 0 ? v.block : kThreads;
-  // a tuned lane split wider than this call's vectors fill (fewer vectors than
-  // the tuning, e.g. the chunks of a host call) is narrowed
-  int ls = v.lane_split > 0 ? v.lane_split : 1;
-  while (ls > 1 && (int64_t)TC * ls > ncols) ls >>= 1;
   const int64_t jpb = threads / ls;  // output indices per block
   const unsigned gx = (unsigned)((v.m + jpb - 1) / jpb);
   GatherView w = v;

@@ -60,7 +60,7 @@ def test_benchmark_hamiltonians_kets_and_batches():
     assert max(errs) < 1e-13, errs
 
 
-@pytest.mark.parametrize("block,split", [(128, 1), (256, 1), (-256, 1), (256, 4), (128, 8), (128, 16), (256, 32)])
+@pytest.mark.parametrize("block,split", [(128, 1), (256, 1), (-256, 1), (256, 4), (128, 8), (128, 16), (256, 32), (-256, 16)])
 @pytest.mark.parametrize("tc", [1, 2, 4, 8])
 def test_every_launch_shape(tc, block, split):
     from qobgpu import _lib as L

@@ -69,7 +69,7 @@ def test_heisenberg_14_spins_batch():
     check(out, H, psi, AL, BE, TOL64)
 
 
-@pytest.mark.parametrize("block,split", [(128, 1), (256, 1), (-256, 1), (128, 4), (256, 2), (128, 8), (128, 16), (256, 32)])
+@pytest.mark.parametrize("block,split", [(128, 1), (256, 1), (-256, 1), (128, 4), (256, 2), (128, 8), (128, 16), (256, 32), (-256, 4), (-256, 16)])
 @pytest.mark.parametrize("tc", [1, 2, 4, 8])
 def test_every_launch_shape(tc, block, split):
     """Each vectors-per-thread tile and launch shape (-256: the persistent grid of
