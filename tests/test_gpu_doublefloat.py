@@ -352,3 +352,33 @@ def test_uneven_batch_double_float():
     torch.cuda.synchronize()
     for yt, r in zip(ys, refs):
         assert rel_l2(yt.cpu().numpy(), r) < 1e-13
+
+
+def test_batch_double_float_complex_and_mixed_items():
+    """A double-float batch holding complex-valued models (the fused kernel's
+    complex form) and real ones (run apart, as in the other dtypes), against the
+    oracle; the served engine uses the same tables."""
+    import torch
+
+    from qobgpu.evolution import Batch
+
+    rng = Q.Rng(960)
+    b = Batch(np.complex128, arith="ff")
+    refs, ys = [], []
+    for k in range(6):
+        n1, n2 = rng.integers(2, 3, 12)
+        H = two_mode_cavity(int(n1), int(n2), seed=961 + k)
+        if k % 2 == 0:  # complex coefficients: drive with a phase
+            H = O.LazySum(H.basis_l, H.basis_r, [0.7, 1.1, 0.3, 0.4 * np.exp(0.6j)], H.operators)
+        n = len(H.basis_l)
+        x, y = rng.ket_data(n), rng.ket_data(n)
+        refs.append(OR.mul(Q.Ket(H.basis_l, y), H, Q.Ket(H.basis_r, x), AL, BE))
+        xt, yt = torch.as_tensor(x, device="cuda:0"), torch.as_tensor(y, device="cuda:0")
+        b.add(H, xt, yt, AL, BE)
+        ys.append(yt)
+    b.run()
+    torch.cuda.synchronize()
+    info = b.info()
+    assert info["items"] == 6 and info["fused"] >= 3
+    for yt, r in zip(ys, refs):
+        assert rel_l2(yt.cpu().numpy(), r) < 1e-13
