@@ -72,3 +72,26 @@ def test_lemire_division_exact():
             low = (M * n) & (2 ** 64 - 1)
             r = (low * d) >> 64
             assert q == n // d and r == n % d, (n, d)
+
+
+def test_dtype_codes_and_double_float_argument_checks():
+    """The Python side maps numpy dtypes and the "ff" arithmetic to the C ABI's
+    codes and refuses double-float arithmetic on ComplexF32 data before any
+    library call."""
+    import pytest
+
+    from qobgpu import _lib as L
+    from qobgpu import operators as O
+    from qobgpu.device import dtype_code
+    from qobgpu.mul import _code
+
+    assert dtype_code(np.complex128) == L.QOB_C128 == 0
+    assert dtype_code(np.complex64) == L.QOB_C64 == 1
+    assert dtype_code("ff") == L.QOB_C128X == 2
+    assert _code(np.complex128, None) == L.QOB_C128
+    assert _code(np.complex128, "ff") == L.QOB_C128X
+    assert _code(np.complex64, None) == L.QOB_C64
+    with pytest.raises(O.ArgumentError):
+        _code(np.complex64, "ff")
+    with pytest.raises(O.ArgumentError):
+        _code(np.complex128, "fp16")
