@@ -95,3 +95,18 @@ def test_dtype_codes_and_double_float_argument_checks():
         _code(np.complex64, "ff")
     with pytest.raises(O.ArgumentError):
         _code(np.complex128, "fp16")
+
+
+def test_reference_flop_count_of_the_heisenberg_chain():
+    """bench.py's count of the reference's term-by-term arithmetic: 53 Pauli
+    product terms, each touching every one of the 2^14 rows once, 8 flops per
+    complex multiply-add, plus the beta scaling: 8 * 54 * 16384."""
+    import sys
+
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    from qobgpu.hamiltonians import heisenberg_chain
+
+    H = heisenberg_chain(14, seed=3)
+    assert len(H.operators) == 53
+    assert bench.reference_flops(H) == 8 * 54 * 16384
