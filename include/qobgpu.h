@@ -250,6 +250,11 @@ int qob_dot(qob_ctx* ctx, int dtype, const void* x, const void* y, int64_t n, do
 /* expect(op, psi) = <psi|op|psi> (src/operators.jl:119) */
 int qob_expect(qob_ctx* ctx, qob_op* op, int dtype, const void* psi, int64_t n, double* result,
                void* stream);
+/* variance(op, psi) = <psi|op (op psi)> - <psi|op psi>^2 (src/operators.jl:139-142):
+ * two applications of op, two FP64 inner products; result interleaved complex
+ * (real for a Hermitian op up to rounding). */
+int qob_variance(qob_ctx* ctx, qob_op* op, int dtype, const void* psi, int64_t n, double* result,
+                 void* stream);
 
 /* qob_dot_noalloc: the inner product of qob_dot for callers that cannot
  * allocate device memory while they run (their memory pool owns the device, or

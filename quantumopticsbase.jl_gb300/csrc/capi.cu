@@ -863,6 +863,29 @@ int qob_expect(qob_ctx* ctx, qob_op* op, int dtype, const void* psi, int64_t n, 
   });
 }
 
+int qob_variance(qob_ctx* ctx, qob_op* op, int dtype, const void* psi, int64_t n, double* result, void* stream) {
+  return guard(ctx, [&] {
+    if (!ctx || !op || !psi || !result) fail(QOB_ERR_ARG, "qob_variance: bad arguments");
+    check_dtype(dtype);
+    if (op->node->m != n || op->node->n != n) fail(QOB_ERR_DIM, "variance needs a square operator matching the state");
+    const size_t esz = dtype == QOB_C128 ? 16 : 8;
+    const cudaStream_t s = (cudaStream_t)stream;
+    void* x = ctx->c.ws.get(14, (size_t)n * esz);
+    void* z = ctx->c.ws.get(15, (size_t)n * esz);
+    Plan& P = get_plan(ctx->c, op, QOB_LEFT, dtype);
+    // x = op psi, z = op x (the reference's op*state, op*x)
+    apply_plan(ctx->c, P, {1.0, 0.0}, psi, 1, n, {0.0, 0.0}, x, 1, n, 1, s, 16);
+    apply_plan(ctx->c, P, {1.0, 0.0}, x, 1, n, {0.0, 0.0}, z, 1, n, 1, s, 16);
+    double e2[2], e1[2];
+    reduce_dot(ctx->c, dtype, psi, z, n, false, e2, s);
+    reduce_dot(ctx->c, dtype, psi, x, n, false, e1, s);
+    // <psi|op^2|psi> - <psi|op|psi>^2 in complex arithmetic, as the reference's
+    // state.data' * (op*x).data - (state.data' * x.data)^2
+    result[0] = e2[0] - (e1[0] * e1[0] - e1[1] * e1[1]);
+    result[1] = e2[1] - 2.0 * e1[0] * e1[1];
+  });
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

@@ -16,7 +16,7 @@ from .rng import Rng
 
 def __getattr__(name):
     # device layer is imported lazily so host-only use does not need CUDA
-    if name in ("mul_", "apply_alloc", "apply_alloc_bra", "expect", "norm", "dot", "to_device"):
+    if name in ("mul_", "apply_alloc", "apply_alloc_bra", "expect", "variance", "norm", "dot", "to_device"):
         from . import mul as _m
 
         return getattr(_m, name)

@@ -19,6 +19,7 @@ import numpy as np
 
 from . import _lib as L
 from . import operators as O
+from .bases import CompositeBasis
 from .device import dtype_code, get_context, handle, raise_for
 from .states import Bra, Ket, StateVector
 
@@ -209,12 +210,45 @@ def dot(x: StateVector, y: StateVector) -> complex:
     return complex(out[0], out[1])
 
 
-def expect(op, psi: Ket) -> complex:
-    """``expect(op, psi) = <psi|op|psi>`` (src/operators.jl:119) in FP64."""
+def _site_operator(index, op, psi):
+    """LazyTensor(psi.basis, index, op) for the subsystem forms of expect, with
+    the reference's checks (src/operators_sparse.jl:49-55)."""
+    b = psi.basis
+    if not isinstance(b, CompositeBasis):
+        raise O.ArgumentError("a subsystem expectation value needs a state on a composite basis")
+    if not 1 <= int(index) <= len(b.bases):  # check_indices, as LazyTensor's constructor
+        raise AssertionError("index out of range")
+    site = b.bases[int(index) - 1]
+    if op.basis_l != site or op.basis_r != site:
+        raise O.IncompatibleBases("the operator's bases differ from the subsystem's")
+    return O.LazyTensor(b, b, (int(index),), (op,))
+
+
+def _reduce_op(fn, op, psi) -> complex:
     p, dev = _vec_ptr(psi.data)
     ctx = get_context(dev)
     h = handle(ctx, op)
     out = (C.c_double * 2)()
-    raise_for(L.lib().qob_expect(ctx.ptr, h.ptr, dtype_code(_np_dtype(psi.data)), p, psi.data.shape[0], out,
-                                 _stream_ptr(dev)), ctx)
+    raise_for(fn(ctx.ptr, h.ptr, dtype_code(_np_dtype(psi.data)), p, psi.data.shape[0], out, _stream_ptr(dev)), ctx)
     return complex(out[0], out[1])
+
+
+def expect(*args) -> complex:
+    """``expect(op, psi) = <psi|op|psi>`` (src/operators.jl:119) in FP64, and
+    ``expect(index, op, psi)``: op on subsystem ``index`` of a composite state,
+    applied as ``LazyTensor(psi.basis, index, op)`` (src/operators_sparse.jl:49-61)."""
+    if len(args) == 3:
+        index, op, psi = args
+        op = _site_operator(index, op, psi)
+    elif len(args) == 2:
+        op, psi = args
+    else:
+        raise TypeError("expect(op, psi) or expect(index, op, psi)")
+    return _reduce_op(L.lib().qob_expect, op, psi)
+
+
+def variance(op, psi: Ket) -> complex:
+    """``variance(op, psi) = <psi|op (op psi)> - <psi|op psi>^2``
+    (src/operators.jl:139-142): two applications of op on the device and two
+    FP64 inner products."""
+    return _reduce_op(L.lib().qob_variance, op, psi)

@@ -286,6 +286,44 @@ def test_norm_dot_expect_fp64():
     assert abs(norm(f) - np.linalg.norm(a.data.astype(np.complex64).astype(np.complex128))) < 1e-12
 
 
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, TOL64), (np.complex64, TOL32)])
+def test_variance_and_subsystem_expect(dtype, tol):
+    """variance(op, psi) (src/operators.jl:139-142) of a Hermitian LazySum (real
+    result) and of a non-Hermitian one (complex result), and expect(index, op,
+    psi) (src/operators_sparse.jl:49-61), against the oracle's mul! followed by
+    FP64 inner products on the host."""
+    from qobgpu.mul import expect, to_device, variance
+
+    H = jaynes_cummings(15, 15)
+    b = H.basis_r
+    rng = Q.Rng(141)
+    psi = rand_state(rng, b)
+    psi.data[:] /= np.linalg.norm(psi.data)
+    A = O.LazySum(b, b, (1.0, 0.4j - 0.2), (H, O.LazyTensor(b, b, (1,), (O.destroy(b.bases[0]),))))
+    dpsi = to_device(psi, dtype=dtype)
+    v = psi.data.astype(dtype).astype(np.complex128)  # the state the device holds
+
+    def ref_apply(op, u):
+        return OR.mul(Q.Ket(b, np.zeros(len(b), np.complex128)), op, Q.Ket(b, u), 1.0, 0.0)
+
+    for op in (H, A):
+        x = ref_apply(op, v)
+        z = ref_apply(op, x)
+        ref = np.vdot(v, z) - np.vdot(v, x) ** 2
+        got = variance(op, dpsi)
+        # relative to the two terms of the difference (<op^2>, <op>^2)
+        scale = abs(np.vdot(v, z)) + abs(np.vdot(v, x)) ** 2
+        assert abs(got - ref) <= tol * scale, (op, got, ref)
+    var_h = variance(H, dpsi)
+    assert abs(var_h.imag) <= tol * abs(var_h.real)
+
+    # errors relative to |op psi| (the state is normalised)
+    for index, f in ((2, O.sigmaz(b.bases[1])), (3, O.number(b.bases[2]))):
+        x = ref_apply(O.LazyTensor(b, b, (index,), (f,)), v)
+        ref = np.vdot(v, x)
+        assert abs(expect(index, f, dpsi) - ref) <= tol * np.linalg.norm(x), (index, ref)
+
+
 @pytest.mark.parametrize("ncols", [1, 3, 13])
 def test_dense_operator_split_columns(ncols):
     """A 700 x 500 DenseOperator (split over column ranges with an ordered

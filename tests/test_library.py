@@ -110,3 +110,26 @@ def test_reference_flop_count_of_the_heisenberg_chain():
     H = heisenberg_chain(14, seed=3)
     assert len(H.operators) == 53
     assert bench.reference_flops(H) == 8 * 54 * 16384
+
+
+def test_subsystem_expect_argument_checks():
+    """expect(index, op, psi) refuses an index outside the composite basis, an
+    operator on another subsystem's basis and a state on a simple basis before
+    any device call (src/operators_sparse.jl:49-55)."""
+    import pytest
+
+    import qobgpu as Q
+    from qobgpu import operators as O
+    from qobgpu.mul import expect
+
+    bf, bs = Q.FockBasis(3), Q.SpinBasis("1/2")
+    b = Q.tensor_basis(bf, bs)
+    psi = Q.Ket(b, np.zeros(len(b), np.complex128))
+    with pytest.raises(AssertionError):
+        expect(3, O.sigmaz(bs), psi)
+    with pytest.raises(O.IncompatibleBases):
+        expect(1, O.sigmaz(bs), psi)
+    with pytest.raises(O.ArgumentError):
+        expect(1, O.sigmaz(bs), Q.Ket(bs, np.zeros(2, np.complex128)))
+    with pytest.raises(TypeError):
+        expect(O.sigmaz(bs))
