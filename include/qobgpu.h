@@ -250,6 +250,13 @@ int qob_dot(qob_ctx* ctx, int dtype, const void* x, const void* y, int64_t n, do
 /* expect(op, psi) = <psi|op|psi> (src/operators.jl:119) */
 int qob_expect(qob_ctx* ctx, qob_op* op, int dtype, const void* psi, int64_t n, double* result,
                void* stream);
+/* expect(op, rho) = sum_ij op[i,j] rho[j,i] = tr(op rho) for a density
+ * operator rho (n x n, column-major, leading dimension ld, on the device)
+ * (src/operators_dense.jl:223-230, src/operators_sparse.jl:36-46; here for
+ * every operator kind): op applied to the columns of rho, then the trace of
+ * the product summed in FP64.  Uses an n x n workspace. */
+int qob_expect_dm(qob_ctx* ctx, qob_op* op, int dtype, const void* rho, int64_t n, int64_t ld, double* result,
+                  void* stream);
 /* variance(op, psi) = <psi|op (op psi)> - <psi|op psi>^2 (src/operators.jl:139-142):
  * two applications of op, two FP64 inner products; result interleaved complex
  * (real for a Hermitian op up to rounding). */

@@ -863,6 +863,27 @@ int qob_expect(qob_ctx* ctx, qob_op* op, int dtype, const void* psi, int64_t n, 
   });
 }
 
+int qob_expect_dm(qob_ctx* ctx, qob_op* op, int dtype, const void* rho, int64_t n, int64_t ld, double* result,
+                  void* stream) {
+  return guard(ctx, [&] {
+    if (!ctx || !op || !rho || !result || n < 0) fail(QOB_ERR_ARG, "qob_expect_dm: bad arguments");
+    check_dtype(dtype);
+    if (op->node->m != n || op->node->n != n) fail(QOB_ERR_DIM, "expect needs a square operator matching the state");
+    if (ld < std::max<int64_t>(n, 1)) fail(QOB_ERR_ARG, "leading dimension smaller than the number of rows");
+    if (n == 0) {
+      result[0] = result[1] = 0.0;
+      return;
+    }
+    const size_t esz = dtype == QOB_C128 ? 16 : 8;
+    const cudaStream_t s = (cudaStream_t)stream;
+    // t = op * rho (every column of rho a vector), then tr(t) = sum_ij op[i,j] rho[j,i]
+    void* t = ctx->c.ws.get(13, (size_t)n * n * esz);
+    Plan& P = get_plan(ctx->c, op, QOB_LEFT, dtype);
+    apply_plan(ctx->c, P, {1.0, 0.0}, rho, 1, ld, {0.0, 0.0}, t, 1, n, n, s, 16);
+    reduce_strided_sum(ctx->c, dtype, t, n, n + 1, result, s);
+  });
+}
+
 int qob_variance(qob_ctx* ctx, qob_op* op, int dtype, const void* psi, int64_t n, double* result, void* stream) {
   return guard(ctx, [&] {
     if (!ctx || !op || !psi || !result) fail(QOB_ERR_ARG, "qob_variance: bad arguments");

@@ -302,6 +302,30 @@ __global__ void k_dot_partial(const CT* __restrict__ x, const CT* __restrict__ y
   if (threadIdx.x == 0) part[blockIdx.x] = make_double2(sre[0], sim[0]);
 }
 
+// sum of x[i * stride] in the same fixed order as k_dot_partial
+template <typename CT>
+__global__ void k_strided_partial(const CT* __restrict__ x, int64_t n, int64_t stride, double2* __restrict__ part) {
+  __shared__ double sre[kRedThreads], sim[kRedThreads];
+  double re = 0.0, im = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)kRedThreads + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kRedThreads) {
+    const CT a = x[i * stride];
+    re += (double)a.x;
+    im += (double)a.y;
+  }
+  sre[threadIdx.x] = re;
+  sim[threadIdx.x] = im;
+  __syncthreads();
+  for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      sre[threadIdx.x] += sre[threadIdx.x + w];
+      sim[threadIdx.x] += sim[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = make_double2(sre[0], sim[0]);
+}
+
 __global__ void k_dot_final(const double2* __restrict__ part, int nparts, double2* out) {
   __shared__ double sre[kRedThreads], sim[kRedThreads];
   double re = 0.0, im = 0.0;
@@ -490,6 +514,27 @@ void launch_modek(int precision, const void* a, bool eye, int64_t s1, int64_t do
                                                          ncols, alpha.re, alpha.im, beta.re, beta.im);
   }
   QOB_LAUNCHED();
+}
+
+void reduce_strided_sum(Context& ctx, int precision, const void* x, int64_t n, int64_t stride, double* out,
+                        cudaStream_t s) {
+  if (ctx.reduce_buf.bytes < (kRedBlocks + 1) * sizeof(double2))
+    ctx.reduce_buf.alloc((kRedBlocks + 1) * sizeof(double2));
+  if (!ctx.reduce_host) QOB_CUDA(cudaMallocHost(&ctx.reduce_host, sizeof(double2)));
+  double2* part = (double2*)ctx.reduce_buf.p;
+  double2* res = part + kRedBlocks;
+  if (precision == QOB_C128)
+    k_strided_partial<double2><<<kRedBlocks, kRedThreads, 0, s>>>((const double2*)x, n, stride, part);
+  else
+    k_strided_partial<float2><<<kRedBlocks, kRedThreads, 0, s>>>((const float2*)x, n, stride, part);
+  QOB_LAUNCHED();
+  k_dot_final<<<1, kRedThreads, 0, s>>>(part, kRedBlocks, res);
+  QOB_LAUNCHED();
+  QOB_CUDA(cudaMemcpyAsync(ctx.reduce_host, res, sizeof(double2), cudaMemcpyDeviceToHost, s));
+  QOB_CUDA(cudaStreamSynchronize(s));
+  const double2 r = *(const double2*)ctx.reduce_host;
+  out[0] = r.x;
+  out[1] = r.y;
 }
 
 // result: interleaved complex dot (norm: sqrt of the real part in out[0]).

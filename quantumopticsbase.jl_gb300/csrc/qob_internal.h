@@ -419,6 +419,9 @@ void launch_axpby(int precision, const void* x, int64_t xes, int64_t xcs, c128 a
                   cudaStream_t s);
 void reduce_dot(Context& ctx, int precision, const void* x, const void* y, int64_t n, bool norm,
                 double* out, cudaStream_t s);
+// sum of x[i * stride], i < n, in FP64 (a trace: stride = leading dimension + 1)
+void reduce_strided_sum(Context& ctx, int precision, const void* x, int64_t n, int64_t stride, double* out,
+                        cudaStream_t s);
 
 // execution (capi.cu)
 void apply_plan(Context& ctx, Plan& plan, c128 alpha, const void* x, int64_t xes, int64_t xcs,

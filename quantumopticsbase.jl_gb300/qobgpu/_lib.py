@@ -60,6 +60,7 @@ SIGNATURES = {
     "qob_dot": (I, [VP, I, VP, VP, I64, DP, VP]),
     "qob_expect": (I, [VP, VP, I, VP, I64, DP, VP]),
     "qob_variance": (I, [VP, VP, I, VP, I64, DP, VP]),
+    "qob_expect_dm": (I, [VP, VP, I, VP, I64, I64, DP, VP]),
     "qob_dot_noalloc": (I, [VP, I, VP, VP, I64, VP, VP]),
     "qob_batch_create": (I, [VP, I, C.POINTER(VP)]),
     "qob_batch_add": (I, [VP, VP, VP, D, D, VP, VP, D, D]),

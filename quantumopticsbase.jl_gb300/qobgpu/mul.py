@@ -233,15 +233,38 @@ def _reduce_op(fn, op, psi) -> complex:
     return complex(out[0], out[1])
 
 
+def _expect_dm(op, rho) -> complex:
+    """tr(op rho) for a density operator with device data (src/operators_dense.jl:223-230)."""
+    if not (op.basis_l == op.basis_r == rho.basis_l == rho.basis_r):
+        raise O.IncompatibleBases()
+    d = rho.data
+    if not _is_torch(d):
+        raise O.ArgumentError("expect(op, rho) on the device needs CUDA tensor data")
+    r, c, ld = _matrix_view(d)
+    if r != c:
+        raise O.DimensionMismatch("a density operator is square")
+    dev = d.device.index
+    ctx = get_context(dev)
+    h = handle(ctx, op)
+    out = (C.c_double * 2)()
+    raise_for(L.lib().qob_expect_dm(ctx.ptr, h.ptr, dtype_code(_np_dtype(d)), C.c_void_p(d.data_ptr()), r, ld, out,
+                                    _stream_ptr(dev)), ctx)
+    return complex(out[0], out[1])
+
+
 def expect(*args) -> complex:
-    """``expect(op, psi) = <psi|op|psi>`` (src/operators.jl:119) in FP64, and
-    ``expect(index, op, psi)``: op on subsystem ``index`` of a composite state,
-    applied as ``LazyTensor(psi.basis, index, op)`` (src/operators_sparse.jl:49-61)."""
+    """``expect(op, psi) = <psi|op|psi>`` (src/operators.jl:119) in FP64;
+    ``expect(op, rho) = tr(op rho)`` for a density operator (src/operators_dense.jl:223-230,
+    src/operators_sparse.jl:36-46); and ``expect(index, op, psi)``: op on
+    subsystem ``index`` of a composite ket, applied as
+    ``LazyTensor(psi.basis, index, op)`` (src/operators_sparse.jl:49-61)."""
     if len(args) == 3:
         index, op, psi = args
         op = _site_operator(index, op, psi)
     elif len(args) == 2:
         op, psi = args
+        if isinstance(psi, O.Operator):
+            return _expect_dm(op, psi)
     else:
         raise TypeError("expect(op, psi) or expect(index, op, psi)")
     return _reduce_op(L.lib().qob_expect, op, psi)

@@ -324,6 +324,44 @@ def test_variance_and_subsystem_expect(dtype, tol):
         assert abs(expect(index, f, dpsi) - ref) <= tol * np.linalg.norm(x), (index, ref)
 
 
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, TOL64), (np.complex64, TOL32)])
+def test_expect_on_density_operators(dtype, tol):
+    """expect(op, rho) = sum_ij op[i,j] rho[j,i] (src/operators_dense.jl:223-230,
+    src/operators_sparse.jl:36-46) for a LazySum, its sparse form and a
+    non-Hermitian dense operator, on a random density operator, also held with a
+    leading dimension larger than its rows; against the oracle's mul! of the
+    operator on rho's columns and the trace summed on the host."""
+    import torch
+
+    from qobgpu.mul import expect, to_device
+
+    H = jaynes_cummings(7, 7)  # 128 x 128
+    b = H.basis_r
+    n = len(b)
+    rho = random_density_columns(n, n, rank=16, seed=151)
+    rng = Q.Rng(152)
+    ops = (H, O.sparse(H), rand_op(rng, b, b))
+    held = rho.astype(dtype).astype(np.complex128)  # what the device holds
+    R = O.Operator(b, b, np.asfortranarray(held))
+    drho = to_device(O.Operator(b, b, rho), dtype=dtype)
+    # the same matrix inside a larger allocation: leading dimension n + 5
+    tdt = torch.complex64 if dtype == np.complex64 else torch.complex128
+    big = torch.zeros((n + 5) * n, dtype=tdt, device="cuda:0")
+    view = big.as_strided((n, n), (1, n + 5))
+    view.copy_(drho.data)
+    dview = O.Operator(b, b, view)
+    for op in ops:
+        t = OR.mul(O.Operator(b, b, np.zeros((n, n), np.complex128, order="F")), op, R, 1.0, 0.0)
+        ref = np.trace(t)
+        scale = np.sum(np.abs(np.diag(t)))
+        for state in (drho, dview):
+            got = expect(op, state)
+            assert abs(got - ref) <= tol * scale, (op, got, ref)
+    # a Hermitian operator on a density operator: real
+    got = expect(H, drho)
+    assert abs(got.imag) <= tol * abs(got.real)
+
+
 @pytest.mark.parametrize("ncols", [1, 3, 13])
 def test_dense_operator_split_columns(ncols):
     """A 700 x 500 DenseOperator (split over column ranges with an ordered

@@ -133,3 +133,20 @@ def test_subsystem_expect_argument_checks():
         expect(1, O.sigmaz(bs), Q.Ket(bs, np.zeros(2, np.complex128)))
     with pytest.raises(TypeError):
         expect(O.sigmaz(bs))
+
+
+def test_density_expect_argument_checks():
+    """expect(op, rho) refuses a density operator on other bases and host data
+    before any device call."""
+    import pytest
+
+    import qobgpu as Q
+    from qobgpu import operators as O
+    from qobgpu.mul import expect
+
+    b2, b3 = Q.GenericBasis(2), Q.GenericBasis(3)
+    op = O.Operator(b2, b2, np.eye(2, dtype=np.complex128, order="F"))
+    with pytest.raises(O.IncompatibleBases):
+        expect(op, O.Operator(b3, b3, np.eye(3, dtype=np.complex128, order="F")))
+    with pytest.raises(O.ArgumentError):
+        expect(op, O.Operator(b2, b2, np.eye(2, dtype=np.complex128, order="F")))
