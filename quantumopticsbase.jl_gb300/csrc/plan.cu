@@ -434,6 +434,9 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
     c128 v;
   };
   std::vector<EllHost> ell;
+  // the device tables index entries, rows and slots with 32-bit integers
+  constexpr int64_t kMaxTable = INT32_MAX;
+  if ((int64_t)H.slots.size() > kMaxTable) fail(QOB_ERR_UNSUPPORTED, "more than 2^31-1 stored entries");
   size_t s0 = 0;
   for (size_t gi = 0; gi < H.groups.size(); ++gi) {
     size_t s1 = s0;
@@ -442,6 +445,8 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
     for (size_t s = s0; s < s1; ++s) nlive += H.live[s];
     if (nlive > 0) {
       const GroupBuild& g = H.groups[gi];
+      if ((int64_t)coloff.size() + nlive > kMaxTable || (int64_t)rowptr.size() + g.nrows + 1 > kMaxTable)
+        fail(QOB_ERR_UNSUPPORTED, "more than 2^31-1 stored entries or rows in the compiled tables");
       GGroup d = make_desc(g, H.S, (int32_t)rowptr.size());
       d.imag = H.group_imag[gi];
       std::vector<int32_t> cnt(g.nrows + 1, 0);
@@ -588,6 +593,8 @@ static void upload_structure(GatherPlan& gp, GatherHost& H, const std::vector<c1
       }
       if (any) {
         const GroupBuild& g = H.groups[gi];
+        if ((int64_t)dtab.size() + g.nrows > INT32_MAX)
+          fail(QOB_ERR_UNSUPPORTED, "more than 2^31-1 rows in the diagonal tables");
         GGroup d = make_desc(g, H.S, (int32_t)dtab.size());  // rowptr_off = table offset
         std::vector<c128> tab(g.nrows, c128{0.0, 0.0});
         for (size_t s = t0; s < t1; ++s)
