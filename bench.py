@@ -11,9 +11,11 @@ HBM.
 
 `value` is the plain ComplexF64 form, device-resident, replayed from a CUDA
 graph and timed with CUDA events on the launching stream.  `e2e` is the same
-metric through the C ABI's host-buffer call (qob_mul_host) with the kets copied
-from pinned host memory and the results copied back every step.  The
-ComplexF32 mode is reported beside it, with its error against the oracle.
+metric through the C ABI's host-buffer calls (qob_mul_host_async +
+qob_host_wait; `sync_value`: qob_mul_host) with the kets copied from pinned host
+memory and the results copied back every step.  The ComplexF32 and the
+double-float modes are reported beside it, with their errors against the
+ComplexF64 result.
 
 `--impl reference` times the CPU restatement of the reference mul! (the
 oracle port; Julia is not available) on all host threads, same workload.
