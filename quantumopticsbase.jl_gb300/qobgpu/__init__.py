@@ -10,7 +10,8 @@ from .bases import (Basis, CompositeBasis, FockBasis, GenericBasis, MomentumBasi
 from .bases import tensor as tensor_basis
 from .operators import *  # noqa: F401,F403
 from .operators import __all__ as _ops_all
-from .states import Bra, Ket, basisstate, dagger_state, tensor_states
+from .states import (Bra, Ket, basisstate, coherentstate, dagger_state, dm, fockstate, spindown, spinup,
+                     tensor_states)
 from .rng import Rng
 
 
@@ -26,4 +27,5 @@ def __getattr__(name):
 __all__ = list(_ops_all) + [
     "Basis", "CompositeBasis", "FockBasis", "GenericBasis", "NLevelBasis", "SpinBasis",
     "tensor_basis", "Ket", "Bra", "basisstate", "dagger_state", "tensor_states", "Rng", "mul_",
+    "coherentstate", "fockstate", "spinup", "spindown", "dm",
 ]

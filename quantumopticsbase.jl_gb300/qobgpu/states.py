@@ -106,3 +106,44 @@ def basisstate(b: Basis, indices, dtype=np.complex128) -> Ket:
     data = np.zeros(len(b), dtype=dtype)
     data[lin] = 1
     return Ket(b, data)
+
+
+def fockstate(b, n: int, dtype=np.complex128) -> Ket:
+    """``fockstate(b, n)``: the Fock state |n> of a FockBasis (src/fock.jl:154-158)."""
+    if not (b.offset <= n <= b.N):
+        raise AssertionError("b.offset <= n <= b.N")
+    return basisstate(b, n - b.offset + 1, dtype)
+
+
+def coherentstate(b, alpha, dtype=np.complex128) -> Ket:
+    """``coherentstate(b, alpha)`` (src/fock.jl:165-196): exp(-|alpha|^2 / 2)
+    alpha^n / sqrt(n!) for n = offset ... N by the same recurrence, not
+    renormalised after the truncation."""
+    alpha = complex(alpha)
+    c = np.exp(-abs(alpha) ** 2 / 2) + 0j
+    for n in range(1, b.offset + 1):
+        c *= alpha / np.sqrt(n)
+    data = np.zeros(len(b), dtype=np.complex128)
+    data[0] = c
+    for n in range(1, b.N - b.offset + 1):
+        data[n] = data[n - 1] * alpha / np.sqrt(n + b.offset)
+    return Ket(b, data.astype(dtype))
+
+
+def spinup(b, dtype=np.complex128) -> Ket:
+    """``spinup(b) = basisstate(b, 1)`` (src/spin.jl:94)."""
+    return basisstate(b, 1, dtype)
+
+
+def spindown(b, dtype=np.complex128) -> Ket:
+    """``spindown(b) = basisstate(b, b.shape[1])`` (src/spin.jl:101)."""
+    return basisstate(b, len(b), dtype)
+
+
+def dm(psi: Ket):
+    """``dm(psi) = tensor(psi, dagger(psi))``: the dense density operator |psi><psi|
+    (src/operators_dense.jl:291)."""
+    from .operators import Operator
+
+    d = psi.to_host()
+    return Operator(psi.basis, psi.basis, np.asfortranarray(np.outer(d, d.conj())))
