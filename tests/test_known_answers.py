@@ -1,10 +1,16 @@
 """Known-answer values of the reference's precompile scenarios
-(benchmark/precompile/scenarios.jl:1-40), for the oracle (CPU) and for the
-device path (GPU):
+(benchmark/precompile/scenarios.jl), for the oracle (CPU) and, for fock() and
+composite(), for the device path (GPU; the device forms of the other two are
+covered by the particle and time-dependent GPU tests):
 
-* fock(): <alpha|a|alpha> = alpha for the coherent state alpha = 1.2 on
+* fock() (:1-14): <alpha|a|alpha> = alpha for the coherent state alpha = 1.2 on
   FockBasis(20) (atol 1e-10), and tr(n dm(alpha)) = |alpha|^2 (atol 1e-9);
-* composite(): H = n (x) I + I (x) 2 sigma+ sigma- + a (x) sigma+ + a^dag (x) sigma-
+* particle() (:61-80): the Gaussian packet (x0 0.1, p0 0.3, sigma 1) on
+  PositionBasis(-10, 10, 200) transformed to momentum space keeps norm 1 and
+  has real(<p>) = 0.3 (atol 1e-12);
+* time_dependent() (:153-166): TimeDependentSum((cos, sin), (sigmax, sigmaz)) at
+  t = 0.25 on spinup equals (cos 0.25 sigmax + sin 0.25 sigmaz) spinup to 1e-12;
+* composite() (:16-40): H = n (x) I + I (x) 2 sigma+ sigma- + a (x) sigma+ + a^dag (x) sigma-
   on FockBasis(20) (x) SpinBasis(1/2) applied to |1> (x) |down> gives
   |1, down> + |0, up> (the scenario checks the basis and a finite norm; the
   state itself follows from the ladder actions: n|1> = |1>, sigma- |down> = 0,
@@ -92,3 +98,28 @@ def test_device_composite_scenario(arith):
         got = out.data.cpu().numpy()
         assert np.array_equal(got, expected)
         assert abs(norm(out) - np.sqrt(2.0)) <= 1e-15
+
+
+def test_oracle_particle_scenario():
+    from qobgpu.bases import MomentumBasis, PositionBasis
+    from qobgpu.particle import gaussianstate, momentum, transform
+
+    bx = PositionBasis(-10, 10, 200)
+    bp = MomentumBasis(bx)
+    psi = gaussianstate(bx, 0.1, 0.3, 1.0)
+    phi = oracle_apply(transform(bp, bx), psi)
+    assert abs(np.linalg.norm(phi) - 1.0) <= 1e-12
+    p_phi = oracle_apply(momentum(bp), Q.Ket(bp, phi))
+    assert abs(np.vdot(phi, p_phi).real - 0.3) <= 1e-12
+
+
+def test_oracle_time_dependent_scenario():
+    b = Q.SpinBasis("1/2")
+    sx, sz = O.sigmax(b), O.sigmaz(b)
+    op = O.TimeDependentSum((np.cos, np.sin), (sx, sz))
+    op.set_time(0.25)
+    assert op.current_time == 0.25
+    up = Q.spinup(b)
+    got = oracle_apply(op.static_op, up)
+    expected = (np.cos(0.25) * sx.data.toarray() + np.sin(0.25) * sz.data.toarray()) @ up.data
+    assert np.linalg.norm(got - expected) < 1e-12
