@@ -225,6 +225,10 @@ def _site_operator(index, op, psi):
 
 
 def _reduce_op(fn, op, psi) -> complex:
+    if not isinstance(psi, Ket):  # the reference defines these for kets (a MethodError otherwise)
+        raise O.ArgumentError("expect / variance of an operator take a Ket (or a density operator)")
+    if not (op.basis_l == op.basis_r == psi.basis):
+        raise O.IncompatibleBases()
     p, dev = _vec_ptr(psi.data)
     ctx = get_context(dev)
     h = handle(ctx, op)

@@ -150,3 +150,21 @@ def test_density_expect_argument_checks():
         expect(op, O.Operator(b3, b3, np.eye(3, dtype=np.complex128, order="F")))
     with pytest.raises(O.ArgumentError):
         expect(op, O.Operator(b2, b2, np.eye(2, dtype=np.complex128, order="F")))
+
+
+def test_ket_expect_and_variance_argument_checks():
+    """expect(op, psi) and variance(op, psi) take a Ket on the operator's basis;
+    a Bra or another basis is refused before any device call."""
+    import pytest
+
+    import qobgpu as Q
+    from qobgpu import operators as O
+    from qobgpu.mul import expect, variance
+
+    b2, b3 = Q.GenericBasis(2), Q.GenericBasis(3)
+    op = O.Operator(b2, b2, np.eye(2, dtype=np.complex128, order="F"))
+    for f in (expect, variance):
+        with pytest.raises(O.ArgumentError):
+            f(op, Q.Bra(b2, np.zeros(2, np.complex128)))
+        with pytest.raises(O.IncompatibleBases):
+            f(op, Q.Ket(b3, np.zeros(3, np.complex128)))
