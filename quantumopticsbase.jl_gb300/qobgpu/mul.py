@@ -210,10 +210,20 @@ def dot(x: StateVector, y: StateVector) -> complex:
     return complex(out[0], out[1])
 
 
-def _site_operator(index, op, psi):
-    """LazyTensor(psi.basis, index, op) for the subsystem forms of expect, with
-    the reference's checks (src/operators_sparse.jl:49-55)."""
-    b = psi.basis
+def _state_basis(state):
+    """The composite basis a subsystem index refers to: a ket's basis, or a
+    density operator's (left = right) basis."""
+    if isinstance(state, O.Operator):
+        if state.basis_l != state.basis_r:
+            raise O.IncompatibleBases()
+        return state.basis_l
+    return state.basis
+
+
+def _site_operator(index, op, state):
+    """LazyTensor(basis, index, op) for the subsystem forms of expect and
+    variance, with the reference's checks (src/operators_sparse.jl:49-55)."""
+    b = _state_basis(state)
     if not isinstance(b, CompositeBasis):
         raise O.ArgumentError("a subsystem expectation value needs a state on a composite basis")
     if not 1 <= int(index) <= len(b.bases):  # check_indices, as LazyTensor's constructor
@@ -224,7 +234,8 @@ def _site_operator(index, op, psi):
     return O.LazyTensor(b, b, (int(index),), (op,))
 
 
-def _reduce_op(fn, op, psi) -> complex:
+def _reduce_op(name, op, psi) -> complex:
+    """qob_expect / qob_variance on a device ket."""
     if not isinstance(psi, Ket):  # the reference defines these for kets (a MethodError otherwise)
         raise O.ArgumentError("expect / variance of an operator take a Ket (or a density operator)")
     if not (op.basis_l == op.basis_r == psi.basis):
@@ -233,6 +244,7 @@ def _reduce_op(fn, op, psi) -> complex:
     ctx = get_context(dev)
     h = handle(ctx, op)
     out = (C.c_double * 2)()
+    fn = getattr(L.lib(), name)
     raise_for(fn(ctx.ptr, h.ptr, dtype_code(_np_dtype(psi.data)), p, psi.data.shape[0], out, _stream_ptr(dev)), ctx)
     return complex(out[0], out[1])
 
@@ -256,26 +268,59 @@ def _expect_dm(op, rho) -> complex:
     return complex(out[0], out[1])
 
 
-def expect(*args) -> complex:
+def _variance_dm(op, rho) -> complex:
+    """variance(op, rho) = expect(op * op, rho) - expect(op, rho)^2, the generic
+    form for density operators (QuantumInterface, a dependency outside the
+    reference tree): X = op rho on the device, then tr(op X) - tr(op rho)^2."""
+    if not (op.basis_l == op.basis_r == rho.basis_l == rho.basis_r):
+        raise O.IncompatibleBases()
+    d = rho.data
+    if not _is_torch(d):
+        raise O.ArgumentError("variance(op, rho) on the device needs CUDA tensor data")
+    n = d.shape[0]
+    X = O.Operator(rho.basis_l, rho.basis_r, d.new_zeros((n, n)).t())  # column-major
+    mul_(X, op, rho, 1.0, 0.0)
+    return _expect_dm(op, X) - _expect_dm(op, rho) ** 2
+
+
+def _split_args(name, args):
+    """(index or None, op, state) of f(op, state) / f(index, op, state)."""
+    if len(args) == 3:
+        return args
+    if len(args) == 2:
+        return (None,) + tuple(args)
+    raise TypeError(f"{name}(op, state) or {name}(index, op, state)")
+
+
+def expect(*args):
     """``expect(op, psi) = <psi|op|psi>`` (src/operators.jl:119) in FP64;
     ``expect(op, rho) = tr(op rho)`` for a density operator (src/operators_dense.jl:223-230,
-    src/operators_sparse.jl:36-46); and ``expect(index, op, psi)``: op on
-    subsystem ``index`` of a composite ket, applied as
-    ``LazyTensor(psi.basis, index, op)`` (src/operators_sparse.jl:49-61)."""
-    if len(args) == 3:
-        index, op, psi = args
-        op = _site_operator(index, op, psi)
-    elif len(args) == 2:
-        op, psi = args
-        if isinstance(psi, O.Operator):
-            return _expect_dm(op, psi)
-    else:
-        raise TypeError("expect(op, psi) or expect(index, op, psi)")
-    return _reduce_op(L.lib().qob_expect, op, psi)
+    src/operators_sparse.jl:36-46); ``expect(index, op, state)``: op on
+    subsystem ``index`` of a composite state, applied as
+    ``LazyTensor(basis, index, op)`` (src/operators_sparse.jl:49-61); a list of
+    states gives the list of values (test/test_operators.jl:54-55)."""
+    index, op, state = _split_args("expect", args)
+    if isinstance(state, (list, tuple)):
+        return [expect(op, s) if index is None else expect(index, op, s) for s in state]
+    if index is not None:
+        op = _site_operator(index, op, state)
+    if isinstance(state, O.Operator):
+        return _expect_dm(op, state)
+    return _reduce_op("qob_expect", op, state)
 
 
-def variance(op, psi: Ket) -> complex:
+def variance(*args):
     """``variance(op, psi) = <psi|op (op psi)> - <psi|op psi>^2``
     (src/operators.jl:139-142): two applications of op on the device and two
-    FP64 inner products."""
-    return _reduce_op(L.lib().qob_variance, op, psi)
+    FP64 inner products; ``variance(op, rho)`` for a density operator;
+    ``variance(index, op, state)`` with op on subsystem ``index``, equal to the
+    variance of the embedded operator (test/test_operators.jl:57-58); a list of
+    states gives the list of values (:59-60)."""
+    index, op, state = _split_args("variance", args)
+    if isinstance(state, (list, tuple)):
+        return [variance(op, s) if index is None else variance(index, op, s) for s in state]
+    if index is not None:
+        op = _site_operator(index, op, state)
+    if isinstance(state, O.Operator):
+        return _variance_dm(op, state)
+    return _reduce_op("qob_variance", op, state)

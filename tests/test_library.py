@@ -168,3 +168,63 @@ def test_ket_expect_and_variance_argument_checks():
             f(op, Q.Bra(b2, np.zeros(2, np.complex128)))
         with pytest.raises(O.IncompatibleBases):
             f(op, Q.Ket(b3, np.zeros(3, np.complex128)))
+
+
+def test_expect_variance_forms_compose_as_the_reference(monkeypatch):
+    """The host front end of expect / variance (test/test_operators.jl:52-60):
+    subsystem forms equal the embedded operator's, lists of states give lists,
+    and variance on a density operator is tr(op op rho) - tr(op rho)^2.  The
+    device calls are replaced by numpy here (the GPU tests run the real ones)."""
+    import torch
+
+    import qobgpu as Q
+    import qobgpu.mul as M
+    from qobgpu import operators as O
+
+    def dense(op):
+        return np.asarray(O.dense(op).data)
+
+    def host(d):
+        return d.cpu().numpy() if hasattr(d, "cpu") else np.asarray(d)
+
+    def reduce_op(name, op, psi):
+        v = host(psi.data)
+        x = dense(op) @ v
+        if name == "qob_expect":
+            return complex(np.vdot(v, x))
+        return complex(np.vdot(v, dense(op) @ x) - np.vdot(v, x) ** 2)
+
+    def expect_dm(op, rho):
+        return complex(np.trace(dense(op) @ host(rho.data)))
+
+    def mul(result, a, b, alpha=1.0, beta=0.0, **kw):
+        result.data.copy_(torch.from_numpy(alpha * dense(a) @ host(b.data)))
+        return result
+
+    monkeypatch.setattr(M, "_reduce_op", reduce_op)
+    monkeypatch.setattr(M, "_expect_dm", expect_dm)
+    monkeypatch.setattr(M, "mul_", mul)
+
+    rng = Q.Rng(77)
+    b1, b2 = Q.FockBasis(3), Q.SpinBasis("1/2")
+    b = Q.tensor_basis(b1, b2)
+    n = len(b)
+    op1 = O.Operator(b1, b1, np.asfortranarray(rng.complex_normal(16).reshape(4, 4)))
+    emb = O.embed(b, b, 1, op1)
+    psi = Q.Ket(b, rng.ket_data(n))
+    A = rng.complex_normal(n * n).reshape(n, n)
+    rho_np = A @ A.conj().T
+    rho_np /= np.trace(rho_np)
+    rho = O.Operator(b, b, torch.from_numpy(np.ascontiguousarray(rho_np.T)).t())  # column-major
+
+    for f in (M.expect, M.variance):
+        assert abs(f(1, op1, rho) - f(emb, rho)) < 1e-12
+        assert abs(f(1, op1, psi) - f(emb, psi)) < 1e-12
+        assert f(emb, [rho, rho]) == [f(emb, rho)] * 2
+        assert f(1, op1, [rho, psi]) == [f(1, op1, rho), f(1, op1, psi)]
+    D = dense(emb)
+    want = np.trace(D @ D @ rho_np) - np.trace(D @ rho_np) ** 2
+    assert abs(M.variance(emb, rho) - want) < 1e-12
+    v = psi.data
+    want = np.vdot(v, D @ D @ v) - np.vdot(v, D @ v) ** 2
+    assert abs(M.variance(1, op1, psi) - want) < 1e-12
