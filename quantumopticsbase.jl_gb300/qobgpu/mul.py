@@ -231,6 +231,8 @@ def _site_operator(index, op, state):
     site = b.bases[int(index) - 1]
     if op.basis_l != site or op.basis_r != site:
         raise O.IncompatibleBases("the operator's bases differ from the subsystem's")
+    if not isinstance(op, O.Operator):  # a lazy subsystem operator: its (small) sparse form
+        op = O.sparse(op)
     return O.LazyTensor(b, b, (int(index),), (op,))
 
 
@@ -300,6 +302,7 @@ def expect(*args):
     ``LazyTensor(basis, index, op)`` (src/operators_sparse.jl:49-61); a list of
     states gives the list of values (test/test_operators.jl:54-55)."""
     index, op, state = _split_args("expect", args)
+    op = O.static_operator(op)  # a TimeDependentSum at its current time (src/time_dependent_operator.jl:76-81)
     if isinstance(state, (list, tuple)):
         return [expect(op, s) if index is None else expect(index, op, s) for s in state]
     if index is not None:
@@ -317,6 +320,7 @@ def variance(*args):
     variance of the embedded operator (test/test_operators.jl:57-58); a list of
     states gives the list of values (:59-60)."""
     index, op, state = _split_args("variance", args)
+    op = O.static_operator(op)
     if isinstance(state, (list, tuple)):
         return [variance(op, s) if index is None else variance(index, op, s) for s in state]
     if index is not None:

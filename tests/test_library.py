@@ -222,6 +222,15 @@ def test_expect_variance_forms_compose_as_the_reference(monkeypatch):
         assert abs(f(1, op1, psi) - f(emb, psi)) < 1e-12
         assert f(emb, [rho, rho]) == [f(emb, rho)] * 2
         assert f(1, op1, [rho, psi]) == [f(1, op1, rho), f(1, op1, psi)]
+    # time-dependent operators at their current time (test/test_time_dependent_operators.jl:40-47)
+    o = O.TimeDependentSum((lambda t: 2.0 * t,), (emb,), init_time=1.0)
+    subo = O.TimeDependentSum((lambda t: 2.0,), (op1,))
+    op1x2 = O.Operator(b1, b1, np.asfortranarray(2.0 * op1.data))
+    emb2 = O.embed(b, b, 1, op1x2)
+    for f in (M.expect, M.variance):
+        for st in (psi, rho):
+            assert abs(f(o, st) - f(emb2, st)) < 1e-12
+            assert abs(f(1, subo, st) - f(1, op1x2, st)) < 1e-12
     D = dense(emb)
     want = np.trace(D @ D @ rho_np) - np.trace(D @ rho_np) ** 2
     assert abs(M.variance(emb, rho) - want) < 1e-12
