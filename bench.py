@@ -42,6 +42,9 @@ ALPHA, BETA = 0.7 - 0.2j, 0.3
 # launch shapes of qob_op_tune, in its order (threads per block, P = persistent, sN = N ket sets per warp)
 SHAPES = ("128", "256", "P256", "128s4", "256s4", "128s8", "256s8", "128s16", "256s16")
 SEED_H = 3
+ORACLE_BUILD = ("oracle/liboref.so, g++ -O3 -ffp-contract=off: every multiply and add rounded separately, as the "
+                "reference's Julia code computes; portable flags (no -march=native), the same binary that checks "
+                "parity")
 L2_NOTE = "20 distinct 64-ket batches rotate: 640 MiB (c128) / 320 MiB (c64) of in+out per rotation, > 2x the 129 MB L2"
 
 
@@ -71,6 +74,9 @@ def parse():
                    help="fixed launch shapes instead of tuning, e.g. c128=4x256s4,c64=4x128 (used for ncu captures)")
     p.add_argument("--suite", action="store_true", help="secondary workloads, one JSON line each")
     p.add_argument("--only", nargs="*", default=None, help="with --suite: these workloads only")
+    p.add_argument("--probe", action="store_true", help="print the device's measured FP64 / FP32 FMA rates")
+    p.add_argument("--no-secondary", action="store_true",
+                   help="leave out the batched and served sub-objects (used for ncu captures)")
     return p.parse_args()
 
 
@@ -201,7 +207,7 @@ def cpu_baseline(H, seconds: float):
     t0 = time.perf_counter()
     OR.mul_kets_threaded(node, ALPHA, Xa, BETA, Ya, threads)
     allc = Xa.shape[1] / (time.perf_counter() - t0)
-    return {"value": single, "unit": UNIT, "cores": 1, "kind": "port",
+    return {"value": single, "unit": UNIT, "cores": 1, "kind": "port", "build": ORACLE_BUILD,
             "sample": f"{n} kets of the 14-spin Heisenberg LazySum, mul!(y, H, x, α, β) one ket at a time on one "
                       f"thread (restated reference CPU path; Julia absent), {seconds:.0f} s bound",
             "all_cores": {"value": allc, "cores": threads, "sample": f"{Xa.shape[1]} kets over {threads} threads"}}
@@ -236,7 +242,7 @@ def run_reference(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
         "data": "synthetic (seeded complex-Gaussian kets)", "config": config(),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "build": ORACLE_BUILD,
                          "sample": f"each step applies H to {threads} kets, one per host thread "
                                    "(restated reference CPU path; Julia absent)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -333,24 +339,42 @@ def run_own(args, rank, world, local_rank):
         return ms, launches, (t_host0, t_host1), (xs, ys)
 
     def step_stats(tdt, code, n=200):
-        """Per-step device times (CUDA events around each single application):
-        cold -- the batches rotate (inputs beyond L2); warm -- one batch again and again."""
+        """Per-step times (CUDA events around each single application):
+        cold -- the batches rotate (inputs beyond L2); warm -- one batch again and
+        again.  host_driven: each step issued as the previous one runs, so a step
+        whose launch the host has not yet issued when the device gets to it
+        counts the wait; device: the same steps queued behind 16 copies of a
+        1 GiB buffer (about 5 ms of device work), so the host is far ahead and
+        the events hold device time only (max_gap_ms: the largest device idle
+        time between two steps, ~0 when the queue stayed full)."""
         xs, ys = batches(tdt)
         argl = [mul_args(xs[b], ys[b], code) for b in range(ROTATE)]
+        blk = torch.empty(2, 1 << 26, dtype=torch.complex128, device=f"cuda:{dev}")  # 2 x 1 GiB
         out = {}
-        for name, pick in (("cold", lambda i: argl[i % ROTATE]), ("warm", lambda i: argl[0])):
-            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
-            with torch.cuda.stream(stream):
-                for i in range(5):
-                    raise_for(lib.qob_mul(*pick(i)), ctx)
-                for i in range(n):
-                    evs[i][0].record(stream)
-                    raise_for(lib.qob_mul(*pick(i)), ctx)
-                    evs[i][1].record(stream)
-            stream.synchronize()
-            t = sorted(a.elapsed_time(b) for a, b in evs)
-            out[name + "_median_ms"] = t[n // 2]
-            out[name + "_p99_ms"] = t[min(n - 1, int(0.99 * n))]
+        for mode in ("host_driven", "device"):
+            for name, pick in (("cold", lambda i: argl[i % ROTATE]), ("warm", lambda i: argl[0])):
+                evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+                with torch.cuda.stream(stream):
+                    for i in range(5):
+                        raise_for(lib.qob_mul(*pick(i)), ctx)
+                    stream.synchronize()
+                    if mode == "device":
+                        for _ in range(16):
+                            blk[1].copy_(blk[0])
+                    for i in range(n):
+                        evs[i][0].record(stream)
+                        raise_for(lib.qob_mul(*pick(i)), ctx)
+                        evs[i][1].record(stream)
+                stream.synchronize()
+                raw = [a.elapsed_time(b) for a, b in evs]
+                t = sorted(raw)
+                key = f"{mode}_{name}"
+                out[key + "_median_ms"] = t[n // 2]
+                out[key + "_p99_ms"] = t[min(n - 1, int(0.99 * n))]
+                out[key + "_max_ms"] = t[-1]
+                if mode == "device":
+                    out[key + "_max_gap_ms"] = max(evs[i][1].elapsed_time(evs[i + 1][0]) for i in range(n - 1))
+        del blk
         return out
 
     def tune(dt):
@@ -392,7 +416,7 @@ def run_own(args, rank, world, local_rank):
     # ComplexF64 data in double-float arithmetic on the FP32 pipes (QOB_C128X)
     msff, launchesff, _, _ = timed(torch.complex128, L.QOB_C128X, K, W)
     valueff = whole_job_rate(BATCH * K, world, msff / 1e3)
-    err32, errff = mode_errors(H, dev) if rank == 0 else (None, None)
+    errs = oracle_errors(lib, ctx, hd, H, dim, stream) if rank == 0 else None
 
     # end to end through the host-buffer C call with pinned host memory
     e2e = None
@@ -403,7 +427,12 @@ def run_own(args, rank, world, local_rank):
         sampler.stop()
     if rank != 0:
         return
+    peaks_live = probe_peaks(dev)
+    batched = served = None
+    if not args.no_secondary:
+        batched, served = secondary(dev, value)
     bytes_per_ket = (2 + (1 if BETA != 0 else 0)) * dim * 16
+    bytes32 = bytes_per_ket // 2 * BATCH
     t_launch = ms64 / 1e3 / K
     achieved = bytes_per_ket * BATCH / t_launch / 1e9
     peaks = read_json(os.path.join(ROOT, "MEASURED_PEAKS.json"))
@@ -412,9 +441,11 @@ def run_own(args, rank, world, local_rank):
     fp64 = None
     if prof.get("dfma_per_launch"):
         fp64_rate = 2.0 * prof["dfma_per_launch"] / t_launch / 1e12
-        fp64 = {"bound": "fp64 FMA pipe", "achieved": fp64_rate, "peak": prof.get("fp64_peak_tflops"),
-                "unit": "TFLOP/s (executed DFMA x2)",
-                "frac": fp64_rate / prof["fp64_peak_tflops"] if prof.get("fp64_peak_tflops") else None}
+        fp64_peak = peaks_live["fp64_fma_tflops"]
+        fp64 = {"bound": "fp64 FMA pipe", "achieved": fp64_rate, "peak": fp64_peak,
+                "unit": "TFLOP/s (executed DFMA + DMUL thread instructions x 2, from the ncu capture)",
+                "frac": fp64_rate / fp64_peak, "peak_source": "qob_probe_peak in this run (FMA chains)",
+                "fp64_ops_per_launch": prof["dfma_per_launch"]}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms64 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -435,16 +466,28 @@ def run_own(args, rank, world, local_rank):
                                          "multiply-add over every term's entries) per apply x applies/s; "
                                          "the compiled kernel executes ~9x fewer FP64 operations"},
         "step_ms": dict(stats64, note="200 single applications timed one by one with CUDA events: cold = "
-                                      "rotating batches (inputs from HBM), warm = one batch repeated (L2-resident)"),
+                                      "rotating batches (inputs from HBM), warm = one batch repeated (L2-resident); "
+                                      "host_driven = issued one after another as they run (host launch latency "
+                                      "included when the device waits for it), device = the same queued behind "
+                                      "~5 ms of device work (device time only)"),
         "plan": plan,
         "tuning": tuning,
         "gpu_launches": launches64,
+        "rel_l2_err_vs_oracle": errs["c128"],
         "fp32_mode": {"value": value32, "unit": UNIT, "ms_per_step": ms32 / K, "vs_fp64": value32 / value,
-                      "rel_l2_err_vs_c128": err32},
+                      "rel_l2_err_vs_oracle": errs["c64"],
+                      "roofline": {"bound": "hbm", "achieved": bytes32 / (ms32 / 1e3 / K) / 1e9, "peak": peak,
+                                   "unit": "GB/s", "frac": bytes32 / (ms32 / 1e3 / K) / 1e9 / peak,
+                                   "algorithmic_bytes_per_launch": bytes32}},
         "ff_mode": {"value": valueff, "unit": UNIT, "ms_per_step": msff / K, "vs_fp64": valueff / value,
-                    "rel_l2_err_vs_c128": errff, "gpu_launches": launchesff,
+                    "rel_l2_err_vs_oracle": errs["c128x"], "gpu_launches": launchesff,
                     "note": "ComplexF64 data, fused gather in double-float (FP32-pair) arithmetic, "
                             "one split launch + one gather launch per step (QOB_C128X)"},
+        "oracle_check": "each form's result on one 64-ket batch of this workload (same qob_mul call, tuned "
+                        "shape) against the oracle (restated reference mul!, host threads, ComplexF64 inputs)",
+        "batched": batched,
+        "served": served,
+        "peaks_live": peaks_live,
         "e2e": e2e,
         "clocks": sampler.summary(*win64) if sampler else None,
     }
@@ -453,26 +496,95 @@ def run_own(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
-def mode_errors(H, dev):
-    """Relative l2 error of the ComplexF32 and the double-float form against the
-    ComplexF64 form (itself held to the oracle at 1e-12 by the tests) on one ket."""
-    import numpy as np
+def probe_peaks(dev):
+    """The device's FP64 and FP32 FMA rates (TFLOP/s) from the library's FMA-chain
+    probe (qob_probe_peak), measured in this run."""
+    import ctypes as C
 
+    from qobgpu import _lib as L
+    from qobgpu.device import get_context, raise_for
+
+    ctx = get_context(dev)
+    out = {}
+    for which, name in ((0, "fp64_fma_tflops"), (1, "fp32_fma_tflops")):
+        r = C.c_double()
+        raise_for(L.lib().qob_probe_peak(ctx.ptr, which, C.byref(r)), ctx)
+        out[name] = r.value
+    out["how"] = ("qob_probe_peak: 8 independent FMA chains per thread, (SMs x 4) blocks of 256 threads, "
+                  "one untimed and one timed launch (CUDA events)")
+    return out
+
+
+def oracle_errors(lib, ctx, hd, H, dim, stream):
+    """Relative l2 error of each form against the oracle (the restated reference
+    mul!) on one 64-ket batch of the bench's workload: the same call (qob_mul,
+    column-major dim x 64, ld = dim, the tuned launch shape), the oracle run on the
+    host's threads with the same ComplexF64 inputs.  Max over the kets, and over
+    the whole batch."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import oracle as OR
     import qobgpu as Q
-    from qobgpu.mul import mul_, to_device
+    from qobgpu import _lib as L
+    from qobgpu.device import raise_for
 
     rng = Q.Rng(97)
-    psi = Q.Ket(H.basis_r, rng.ket_data(len(H.basis_r)))
-    out = Q.Ket(H.basis_l, rng.ket_data(len(H.basis_l)))
+    X = rng.kets_data(dim, BATCH)
+    Y = rng.kets_data(dim, BATCH)
+    ref = np.asfortranarray(Y.copy())
+    OR.mul_kets_threaded(OR.build_node(H), ALPHA, X, BETA, ref, os.cpu_count() or 1)
+    out = {}
+    for name, code, tdt in (("c128", L.QOB_C128, torch.complex128), ("c64", L.QOB_C64, torch.complex64),
+                            ("c128x", L.QOB_C128X, torch.complex128)):
+        xd = torch.as_tensor(np.ascontiguousarray(X.T), device=stream.device).to(tdt).t()
+        yd = torch.as_tensor(np.ascontiguousarray(Y.T), device=stream.device).to(tdt).t()
+        raise_for(lib.qob_mul(ctx.ptr, L.QOB_LEFT, 0, hd.ptr, code, ALPHA.real, ALPHA.imag,
+                              C.c_void_p(xd.data_ptr()), dim, BATCH, dim, BETA, 0.0, C.c_void_p(yd.data_ptr()),
+                              dim, BATCH, dim, C.c_void_p(stream.cuda_stream)), ctx)
+        stream.synchronize()
+        got = yd.cpu().numpy().astype(np.complex128)
+        per = [float(np.linalg.norm(got[:, c] - ref[:, c]) / np.linalg.norm(ref[:, c])) for c in range(BATCH)]
+        out[name] = {"max_over_kets": max(per),
+                     "batch": float(np.linalg.norm(got - ref) / np.linalg.norm(ref))}
+    return out
 
-    def run(dtype, arith=None):
-        d_out = to_device(out, dev, dtype)
-        mul_(d_out, H, to_device(psi, dev, dtype), ALPHA, BETA, arith=arith)
-        return d_out.data.cpu().numpy().astype(np.complex128)
 
-    ref = run(np.complex128)
-    rel = lambda got: float(np.linalg.norm(got - ref) / np.linalg.norm(ref))  # noqa: E731
-    return rel(run(np.complex64)), rel(run(np.complex128, "ff"))
+def secondary(dev, value64):
+    """The batched and served forms of the metric, compact: 256 uneven two-mode
+    cavity models in one persistent launch (CUDA-graph replay), and a served
+    stream of RK4 requests (Poisson arrivals for the latencies; all requests at
+    once for the sustained rate), in ComplexF64, double-float and ComplexF32.
+    ``fp32_vs_plain_fp64`` divides by the headline plain ComplexF64 applies/s."""
+    import torch
+
+    import bench_suite as BS
+    from qobgpu.device import get_context
+
+    ctx = get_context(dev)
+    stream = torch.cuda.Stream(dev)
+    cav = BS.cavities256(ctx, stream)
+    batched = {r["dtype"]: {"applies_per_s": r["applies_per_s"], "us_per_launch": r["us_per_launch"],
+                            "algorithmic_GBps": r["algorithmic_GBps"], "tile": r["tile"]} for r in cav["results"]}
+    batched["config"] = "256 two-mode cavities FockBasis(n1) x FockBasis(n2), n1, n2 ~ U{8..64}, dims 81-4225, one ket each"
+    batched["fp32_vs_plain_fp64"] = batched["complex64"]["applies_per_s"] / value64
+    batched["fp32_vs_batched_fp64"] = batched["complex64"]["applies_per_s"] / batched["complex128"]["applies_per_s"]
+    lat = BS.served(ctx, stream, nreq=128, rate=2000.0)
+    burst = BS.served(ctx, stream, nreq=128, rate=1e9, seed=51)
+    served = {"config": "requests of 100 RK4 steps (dt 1e-3): Heisenberg chains of 8-16 spins, Jaynes-Cummings "
+                        "models of dim 512-8192; 128 Poisson arrivals at 2000/s for the latencies, 128 at once for "
+                        "the sustained rate",
+              "fp32_rel_err_vs_fp64_max": lat["fp32_rel_err_vs_fp64_max"],
+              "double_float_rel_err_vs_fp64_max": lat["double_float_rel_err_vs_fp64_max"]}
+    for k, v in lat["results"].items():
+        served[k] = {"p50_ms": v["p50_ms"], "p99_ms": v["p99_ms"],
+                     "sustained_applies_per_s": burst["results"][k]["applies_per_s"],
+                     "sustained_requests_per_s": burst["results"][k]["requests_per_s"]}
+    served["fp32_vs_fp64_sustained"] = (served["complex64"]["sustained_applies_per_s"]
+                                        / served["complex128"]["sustained_applies_per_s"])
+    return batched, served
 
 
 def end_to_end(lib, ctx, hd, dim, K, dev, world):
@@ -548,9 +660,11 @@ def main():
 
     g.build()
     if args.suite:
-        from qobgpu.suite import run_suite
+        from bench_suite import run_suite
 
         return run_suite(local_rank, args.only)
+    if args.probe:
+        return print(json.dumps(probe_peaks(local_rank)), flush=True)
     run_own(args, rank, world, local_rank)
 
 

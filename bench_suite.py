@@ -1,4 +1,5 @@
-"""Secondary workloads of the benchmark (``python bench.py --suite``).
+"""Secondary workloads of the benchmark (``python bench.py --suite``), and the
+compact batched / served runs the headline line of ``bench.py`` carries.
 
 One JSON line per workload, each timed with CUDA events on the launching
 stream (device-resident data, CUDA-graph replay where the workload is a fixed
@@ -30,11 +31,16 @@ import time
 
 import numpy as np
 
-from . import _lib as L
-from .device import dtype_code, get_context, handle, raise_for
-from .hamiltonians import (heisenberg_chain, jaynes_cummings, jaynes_cummings_sparse, random_density_columns,
-                           two_mode_cavity)
-from .rng import Rng
+import os
+import sys
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "quantumopticsbase.jl_gb300"))
+
+from qobgpu import _lib as L  # noqa: E402
+from qobgpu.device import dtype_code, get_context, handle, raise_for  # noqa: E402
+from qobgpu.hamiltonians import (heisenberg_chain, jaynes_cummings, jaynes_cummings_sparse,  # noqa: E402
+                                 random_density_columns, two_mode_cavity)
+from qobgpu.rng import Rng  # noqa: E402
 
 
 def _timed_graph(ctx, stream, record, reps=20):
@@ -165,7 +171,7 @@ def rho_h8(ctx, stream):
 def cavities256(ctx, stream):
     import torch
 
-    from .evolution import Batch
+    from qobgpu.evolution import Batch
 
     rng = Rng(40)
     models = []
@@ -197,9 +203,9 @@ def lindblad(ctx, stream):
     Liouvillian (the reference's form) at 8 spins."""
     import torch
 
-    from . import operators as O
-    from . import superoperators as SO
-    from .bases import SpinBasis
+    from qobgpu import operators as O
+    from qobgpu import superoperators as SO
+    from qobgpu.bases import SpinBasis
 
     out = []
     for nspins in (8, 10, 12):
@@ -242,10 +248,10 @@ def particle(ctx, stream):
     the bare FFT transform Tpx on the same grids."""
     import torch
 
-    from . import operators as O
-    from .bases import MomentumBasis, PositionBasis
-    from .bases import tensor as tensor_bases
-    from .particle import momentum, potentialoperator, transform
+    from qobgpu import operators as O
+    from qobgpu.bases import MomentumBasis, PositionBasis
+    from qobgpu.bases import tensor as tensor_bases
+    from qobgpu.particle import momentum, potentialoperator, transform
 
     out = []
     grids = [("1d_4096", [PositionBasis(-40.0, 40.0, 4096)]),
@@ -281,7 +287,7 @@ def particle(ctx, stream):
 
 
 def served(ctx, stream, nreq=192, rate=2000.0, seed=50):
-    from .evolution import Server
+    from qobgpu.evolution import Server
 
     rng = Rng(seed)
     pool = [heisenberg_chain(n, seed=60 + n) for n in (8, 10, 12, 14, 16)]
@@ -359,9 +365,9 @@ def modek(ctx, stream):
     kets; and one 64 x 64 dense factor with a 16 x 16 one on a 64 x 16 x 64 space."""
     import torch
 
-    from . import operators as O
-    from .bases import GenericBasis
-    from .bases import tensor as tensor_basis
+    from qobgpu import operators as O
+    from qobgpu.bases import GenericBasis
+    from qobgpu.bases import tensor as tensor_basis
 
     rng = Rng(60)
 
@@ -395,8 +401,8 @@ def modek(ctx, stream):
 def dense(ctx, stream):
     """DenseOperator mul! (gemv / gemm): n x n dense operators, n = 1024 and 4096,
     on 1 and 64 / 16 kets."""
-    from . import operators as O
-    from .bases import GenericBasis
+    from qobgpu import operators as O
+    from qobgpu.bases import GenericBasis
 
     rng = Rng(70)
     out = []

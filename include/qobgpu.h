@@ -74,6 +74,14 @@ int qob_version(void);
  * (diagnostics: lets a caller count the device work behind a call). */
 int64_t qob_kernel_launches(void);
 
+/* Diagnostics: the device's fused multiply-add rate in TFLOP/s (2 flops per
+ * FMA), which = 0 for FP64, 1 for FP32, measured with chains of independent
+ * FMAs over (SMs x 4) blocks of 256 threads (one untimed launch, one timed with
+ * CUDA events; about 2 ms and 1 ms).  The roofline fraction of an FP64-bound
+ * kernel is taken against this number.  No counterpart in the reference.
+ * Synchronous; allocates and frees 8 bytes of device memory. */
+int qob_probe_peak(qob_ctx* ctx, int which, double* tflops);
+
 /* Context on one CUDA device.  flags: reserved, pass 0. */
 int qob_create(qob_ctx** ctx, int device, unsigned flags);
 int qob_destroy(qob_ctx* ctx);
@@ -253,8 +261,10 @@ int qob_expect(qob_ctx* ctx, qob_op* op, int dtype, const void* psi, int64_t n, 
 /* expect(op, rho) = sum_ij op[i,j] rho[j,i] = tr(op rho) for a density
  * operator rho (n x n, column-major, leading dimension ld, on the device)
  * (src/operators_dense.jl:223-230, src/operators_sparse.jl:36-46; here for
- * every operator kind): op applied to the columns of rho, then the trace of
- * the product summed in FP64.  Uses an n x n workspace. */
+ * every operator kind): op applied to blocks of rho's columns, then the
+ * blocks' shares of the trace of the product summed in FP64 in block order.
+ * The workspace holds one block, at most 256 MiB (at least one column), and
+ * stays with the context until qob_destroy. */
 int qob_expect_dm(qob_ctx* ctx, qob_op* op, int dtype, const void* rho, int64_t n, int64_t ld, double* result,
                   void* stream);
 /* variance(op, psi) = <psi|op (op psi)> - <psi|op psi>^2 (src/operators.jl:139-142):

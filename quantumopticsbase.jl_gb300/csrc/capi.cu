@@ -876,11 +876,27 @@ int qob_expect_dm(qob_ctx* ctx, qob_op* op, int dtype, const void* rho, int64_t 
     }
     const size_t esz = dtype == QOB_C128 ? 16 : 8;
     const cudaStream_t s = (cudaStream_t)stream;
-    // t = op * rho (every column of rho a vector), then tr(t) = sum_ij op[i,j] rho[j,i]
-    void* t = ctx->c.ws.get(13, (size_t)n * n * esz);
+    // t = op * rho[:, c0 : c0 + w] for column blocks of rho (every column a
+    // vector), then the block's share of tr(op rho) = sum_ij op[i,j] rho[j,i]:
+    // t[c0 + j, j] for j < w.  The workspace holds one block of at most
+    // kExpectDmWorkspace bytes (at least one column); the blocks' sums are
+    // added in block order in FP64.
+    constexpr size_t kExpectDmWorkspace = 256ull << 20;
+    const int64_t w = std::max<int64_t>(1, std::min<int64_t>(n, (int64_t)(kExpectDmWorkspace / ((size_t)n * esz))));
+    void* t = ctx->c.ws.get(13, (size_t)n * w * esz);
     Plan& P = get_plan(ctx->c, op, QOB_LEFT, dtype);
-    apply_plan(ctx->c, P, {1.0, 0.0}, rho, 1, ld, {0.0, 0.0}, t, 1, n, n, s, 16);
-    reduce_strided_sum(ctx->c, dtype, t, n, n + 1, result, s);
+    double re = 0.0, im = 0.0;
+    for (int64_t c0 = 0; c0 < n; c0 += w) {
+      const int64_t nc = std::min<int64_t>(w, n - c0);
+      const char* rb = static_cast<const char*>(rho) + (size_t)c0 * ld * esz;
+      apply_plan(ctx->c, P, {1.0, 0.0}, rb, 1, ld, {0.0, 0.0}, t, 1, n, nc, s, 16);
+      double part[2];
+      reduce_strided_sum(ctx->c, dtype, static_cast<const char*>(t) + (size_t)c0 * esz, nc, n + 1, part, s);
+      re += part[0];
+      im += part[1];
+    }
+    result[0] = re;
+    result[1] = im;
   });
 }
 

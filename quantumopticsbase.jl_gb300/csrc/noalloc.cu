@@ -27,7 +27,9 @@
 //     first call before any stream capture.
 #include <cuda_runtime.h>
 
+#include <exception>
 #include <mutex>
+#include <new>
 
 #include "qob_internal.h"
 
@@ -146,5 +148,11 @@ extern "C" int qob_dot_noalloc(qob_ctx* ctx, int dtype, const void* x, const voi
   } catch (const qob::Error& e) {
     ctx->c.err = e.msg;
     return e.code;
+  } catch (const std::bad_alloc&) {
+    ctx->c.err = "host out of memory";
+    return QOB_ERR_OOM;
+  } catch (const std::exception& e) {  // e.g. std::system_error from locking the mutex
+    ctx->c.err = e.what();
+    return QOB_ERR_ARG;
   }
 }

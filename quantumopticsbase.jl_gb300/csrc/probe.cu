@@ -1,0 +1,93 @@
+// probe.cu -- qob_probe_peak: the device's FP64 and FP32 fused multiply-add
+// rates, measured with chains of FMAs.
+//
+// The roofline of the ComplexF64 kernels on GB300 is its FP64 pipe, whose rate
+// is far below the FP32 one; this probe measures both on the GPU the library
+// runs on, so the fraction a kernel reaches is taken against a number measured
+// in the same run.  Each thread runs kChains independent chains
+// a = fma(a, b, c) (b, c kernel arguments, so nothing folds), enough chains and
+// resident warps that the FMA latency is covered and the pipe alone bounds the
+// rate.  The grid is (SMs x 4) blocks of 256 threads; one untimed launch, then
+// the timed one between two events on a stream of the probe's own.
+#include <cuda_runtime.h>
+
+#include "qob_internal.h"
+
+namespace {
+
+constexpr int kChains = 8;
+constexpr int kProbeThreads = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(kProbeThreads) k_fma_probe(T* out, int iters, T b, T c) {
+  T a[kChains];
+#pragma unroll
+  for (int k = 0; k < kChains; ++k) a[k] = (T)(threadIdx.x + k) * c;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < kChains; ++k) a[k] = fma(a[k], b, c);
+  }
+  T s = 0;
+#pragma unroll
+  for (int k = 0; k < kChains; ++k) s += a[k];
+  if (s == (T)-1.2345) out[0] = s;  // never true for these arguments; keeps the chains live
+}
+
+template <typename T>
+double probe(int device, int iters) {
+  int sms = 0;
+  QOB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  cudaStream_t s = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  T* out = nullptr;
+  double tflops = 0.0;
+  QOB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  try {
+    QOB_CUDA(cudaEventCreate(&e0));
+    QOB_CUDA(cudaEventCreate(&e1));
+    QOB_CUDA(cudaMalloc(&out, sizeof(T)));
+    const int blocks = sms * 4;
+    const T b = (T)0.999, c = (T)1e-3;
+    k_fma_probe<T><<<blocks, kProbeThreads, 0, s>>>(out, iters, b, c);
+    QOB_LAUNCHED();
+    QOB_CUDA(cudaEventRecord(e0, s));
+    k_fma_probe<T><<<blocks, kProbeThreads, 0, s>>>(out, iters, b, c);
+    QOB_LAUNCHED();
+    QOB_CUDA(cudaEventRecord(e1, s));
+    QOB_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    QOB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    const double fmas = (double)blocks * kProbeThreads * kChains * (double)iters;
+    tflops = 2.0 * fmas / (ms * 1e-3) / 1e12;
+  } catch (...) {
+    if (out) cudaFree(out);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaStreamDestroy(s);
+    throw;
+  }
+  QOB_CUDA(cudaFree(out));
+  QOB_CUDA(cudaEventDestroy(e0));
+  QOB_CUDA(cudaEventDestroy(e1));
+  QOB_CUDA(cudaStreamDestroy(s));
+  return tflops;
+}
+
+}  // namespace
+
+extern "C" int qob_probe_peak(qob_ctx* ctx, int which, double* tflops) {
+  if (!ctx) return QOB_ERR_ARG;
+  try {
+    if (!tflops || (which != 0 && which != 1)) qob::fail(QOB_ERR_ARG, "qob_probe_peak: which must be 0 or 1");
+    QOB_CUDA(cudaSetDevice(ctx->c.device));
+    // about 2 ms (FP64) and 1 ms (FP32) on GB300
+    *tflops = which == 0 ? probe<double>(ctx->c.device, 2048) : probe<float>(ctx->c.device, 32768);
+    return QOB_OK;
+  } catch (const qob::Error& e) {
+    ctx->c.err = e.msg;
+    return e.code;
+  } catch (const std::exception& e) {
+    ctx->c.err = e.what();
+    return QOB_ERR_ARG;
+  }
+}

@@ -40,6 +40,7 @@ SIGNATURES = {
     "qob_create": (I, [C.POINTER(VP), I, C.c_uint]),
     "qob_destroy": (I, [VP]),
     "qob_last_error": (C.c_char_p, [VP]),
+    "qob_probe_peak": (I, [VP, I, DP]),
     "qob_op_sparse": (I, [VP, I64, I64, I64P, I64P, VP, I, I, C.POINTER(VP)]),
     "qob_op_dense": (I, [VP, I64, I64, VP, I64, I, I, C.POINTER(VP)]),
     "qob_op_eye": (I, [VP, I64, I64, C.POINTER(VP)]),

@@ -1,9 +1,11 @@
 """Full-size GPU checks at the benchmark configurations' sizes.
 
-Where the oracle is slow at these sizes, size-independent properties stand in:
-linearity of the application, Hermiticity of H (<a|H b> = conj(<b|H a>)),
-and conservation of the norm under RK4 time evolution.  Tolerances are
-relative and written per assertion.
+The bench's own workload (the 14-spin Heisenberg chain on 64 kets, through
+qob_mul with the autotuned launch shape) is compared with the oracle on every
+ket in ComplexF64 (1e-12), ComplexF32 (1e-5) and double-float (1e-12).  Beside
+that, size-independent properties: linearity of the application, Hermiticity
+of H (<a|H b> = conj(<b|H a>)), and conservation of the norm under RK4 time
+evolution.  Tolerances are relative (l2) and written per assertion.
 """
 import numpy as np
 import pytest
@@ -27,6 +29,52 @@ def test_heisenberg_16_spins_against_oracle():
         r = to_device(out, dtype=dtype)
         mul_(r, H, to_device(psi, dtype=dtype), 0.7 - 0.2j, 0.3)
         assert rel_l2(r.data.cpu().numpy().astype(np.complex128), ref) < tol
+
+
+@pytest.mark.parametrize("form,tol", [("c128", 1e-12), ("c64", 1e-5), ("ff", 1e-12)])
+def test_heisenberg_14_batch64_against_oracle(form, tol):
+    """The bench step: mul!(Y, H, X, 0.7 - 0.2i, 0.3) with H =
+    heisenberg_chain(14, seed=3) on 64 normalised complex-Gaussian kets, X and Y
+    column-major 16384 x 64 with leading dimension 16384, the launch shape
+    qob_op_tune picks for 64 kets, one qob_mul call; every ket against the
+    oracle's mul! (src/operators_lazysum.jl:189-200), which gets the same
+    ComplexF64 inputs."""
+    import ctypes as C
+
+    import torch
+
+    from qobgpu import _lib as L
+    from qobgpu.device import dtype_code, get_context, handle, raise_for
+
+    H = heisenberg_chain(14, seed=3)
+    dim, k = len(H.basis_l), 64
+    rng = Q.Rng(2002)
+    X = rng.kets_data(dim, k)
+    X /= np.linalg.norm(X, axis=0, keepdims=True)
+    Y = rng.kets_data(dim, k)
+    alpha, beta = 0.7 - 0.2j, 0.3
+    ref = np.asfortranarray(Y.copy())
+    OR.mul_kets_threaded(OR.build_node(H), alpha, np.asfortranarray(X), beta, ref, 16)
+
+    lib = L.lib()
+    ctx = get_context(0)
+    hd = handle(ctx, H)
+    code = dtype_code("ff" if form == "ff" else (np.complex64 if form == "c64" else np.complex128))
+    chosen = C.c_int()
+    raise_for(lib.qob_op_tune(ctx.ptr, hd.ptr, L.QOB_LEFT, code, k, None, C.byref(chosen)), ctx)
+    tdt = torch.complex64 if form == "c64" else torch.complex128
+    # column-major dim x 64, ld = dim: the transpose of a contiguous 64 x dim tensor
+    xd = torch.as_tensor(np.ascontiguousarray(X.T), device="cuda:0").to(tdt).t()
+    yd = torch.as_tensor(np.ascontiguousarray(Y.T), device="cuda:0").to(tdt).t()
+    stream = torch.cuda.current_stream(0)
+    raise_for(lib.qob_mul(ctx.ptr, L.QOB_LEFT, 0, hd.ptr, code, alpha.real, alpha.imag, C.c_void_p(xd.data_ptr()),
+                          dim, k, dim, beta, 0.0, C.c_void_p(yd.data_ptr()), dim, k, dim,
+                          C.c_void_p(stream.cuda_stream)), ctx)
+    torch.cuda.synchronize(0)
+    got = yd.cpu().numpy().astype(np.complex128)
+    errs = [rel_l2(got[:, c], ref[:, c]) for c in range(k)]
+    assert max(errs) < tol, (form, max(errs), chosen.value)
+    assert rel_l2(got, ref) < tol
 
 
 def test_heisenberg_14_batch64_linearity_and_hermiticity():

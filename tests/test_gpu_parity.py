@@ -362,6 +362,74 @@ def test_expect_on_density_operators(dtype, tol):
     assert abs(got.imag) <= tol * abs(got.real)
 
 
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, TOL64), (np.complex64, TOL32)])
+def test_expect_on_a_density_operator_in_column_blocks(dtype, tol):
+    """expect(op, rho) on dim 8192 (Jaynes-Cummings, FockBasis(63) x spin x
+    FockBasis(63)): rho is larger than the 256 MiB workspace, so op is applied
+    to 2 (ComplexF32) or 4 (ComplexF64) blocks of its columns.  rho = V V^dagger
+    of rank 4 is formed on the device; the reference is sum_k <v_k|op v_k> with
+    the oracle's mul! (tr(op V V^dagger) = sum_k v_k^dagger op v_k)."""
+    import torch
+
+    from qobgpu.mul import expect
+
+    H = jaynes_cummings(63, 63, seed=3)
+    b = H.basis_r
+    n = len(b)
+    rng = Q.Rng(171)
+    V = rng.kets_data(n, 4) / 2.0
+    tdt = torch.complex64 if dtype == np.complex64 else torch.complex128
+    Vd = torch.as_tensor(V.astype(dtype), device="cuda:0")
+    rho = (Vd @ Vd.conj().t()).t().contiguous().t()  # column-major n x n
+    held = V.astype(dtype).astype(np.complex128)
+    ref, scale = 0j, 0.0
+    for k in range(4):
+        v = np.ascontiguousarray(held[:, k])
+        hv = OR.mul(Q.Ket(b, np.zeros(n, np.complex128)), H, Q.Ket(b, v), 1.0, 0.0)
+        ref += np.vdot(v, hv)
+        scale += np.linalg.norm(v) * np.linalg.norm(hv)
+    got = expect(H, O.Operator(b, b, rho))
+    assert rho.dtype == tdt
+    assert abs(got - ref) <= tol * scale, (got, ref)
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, TOL64), (np.complex64, TOL32)])
+def test_variance_on_density_operators(dtype, tol):
+    """variance(op, rho) = tr(op op rho) - tr(op rho)^2 and variance(index, op,
+    rho) on a composite basis (FockBasis(7) x SpinBasis(1/2) x FockBasis(7)):
+    the device applies op to rho's columns into a column-major workspace X, then
+    takes tr(op X) and tr(op rho); against the oracle's two mul! of op on rho's
+    columns and the traces summed on the host."""
+    from qobgpu.mul import to_device, variance
+
+    H = jaynes_cummings(7, 7)
+    b = H.basis_r
+    n = len(b)
+    rho = random_density_columns(n, n, rank=12, seed=161)
+    held = rho.astype(dtype).astype(np.complex128)  # what the device holds
+    R = O.Operator(b, b, np.asfortranarray(held))
+    drho = to_device(O.Operator(b, b, rho), dtype=dtype)
+    A = O.LazySum(b, b, (1.0, 0.3j - 0.5), (H, O.LazyTensor(b, b, (1,), (O.destroy(b.bases[0]),))))
+
+    def ref_variance(op):
+        zero = O.Operator(b, b, np.zeros((n, n), np.complex128, order="F"))
+        X = OR.mul(zero, op, R, 1.0, 0.0)
+        Z = OR.mul(zero, op, O.Operator(b, b, np.asfortranarray(X)), 1.0, 0.0)
+        t1, t2 = np.trace(Z), np.trace(X)
+        return t1 - t2 ** 2, abs(t1) + abs(t2) ** 2  # value, scale of the two terms
+
+    for op in (H, A, O.sparse(H)):
+        ref, scale = ref_variance(op)
+        got = variance(op, drho)
+        assert abs(got - ref) <= tol * scale, (op, got, ref)
+    got = variance(H, drho)  # Hermitian op, density operator: real
+    assert abs(got.imag) <= tol * abs(got.real)
+    for index, f in ((2, O.sigmax(b.bases[1])), (3, O.number(b.bases[2]))):
+        ref, scale = ref_variance(O.LazyTensor(b, b, (index,), (f,)))
+        got = variance(index, f, drho)
+        assert abs(got - ref) <= tol * scale, (index, got, ref)
+
+
 @pytest.mark.parametrize("ncols", [1, 3, 13])
 def test_dense_operator_split_columns(ncols):
     """A 700 x 500 DenseOperator (split over column ranges with an ordered
