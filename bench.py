@@ -41,6 +41,10 @@ NSPINS, BATCH, ROTATE = 14, 64, 20
 ALPHA, BETA = 0.7 - 0.2j, 0.3
 # launch shapes of qob_op_tune, in its order (threads per block, P = persistent, sN = N ket sets per warp)
 SHAPES = ("128", "256", "P256", "128s4", "256s4", "128s8", "256s8", "128s16", "256s16")
+# staged-tile shapes of qob_op_tune, in its order: (tile bits, kets per thread, ket sets per warp)
+TILE_SHAPES = ((10, 1, 1), (10, 2, 1), (9, 4, 1), (11, 1, 1), (11, 2, 1), (12, 1, 1), (9, 1, 4), (8, 1, 16),
+               (8, 2, 8), (9, 2, 4), (10, 1, 4), (7, 2, 16))
+NCANDS = 36 + len(TILE_SHAPES)
 SEED_H = 3
 ORACLE_BUILD = ("oracle/liboref.so, g++ -O3 -ffp-contract=off: every multiply and add rounded separately, as the "
                 "reference's Julia code computes; portable flags (no -march=native), the same binary that checks "
@@ -378,17 +382,26 @@ def run_own(args, rank, world, local_rank):
         return out
 
     def tune(dt):
-        times = (C.c_double * 36)()
+        times = (C.c_double * NCANDS)()
         chosen = C.c_int()
         raise_for(lib.qob_op_tune(ctx.ptr, hd.ptr, L.QOB_LEFT, dtype_code(dt), BATCH, times, C.byref(chosen)), ctx)
         v = chosen.value
-        return {"kets_per_thread": v & 0xFFFF, "threads_per_block": (v >> 16) & 0x3FF,
+        ms = {f"{1 << (k // 9)}x{SHAPES[k % 9]}": times[k] for k in range(36)}
+        ms.update({f"T{b}:{tc}x256s{ls}": times[36 + i] for i, (b, tc, ls) in enumerate(TILE_SHAPES)})
+        return {"kets_per_thread": v & 0xFF, "tile_bits": (v >> 8) & 0xFF, "threads_per_block": (v >> 16) & 0x3FF,
                 "ket_sets_per_warp": 1 << ((v >> 26) & 0x7), "persistent": bool(v >> 30),
-                "ms_by_kets_per_thread_and_shape": {
-                    f"{1 << (k // 9)}x{SHAPES[k % 9]}": times[k] for k in range(36)}}
+                "ms_by_shape": ms}
 
     def fix(dt, spec):
-        """A launch shape given as <kets per thread>x<threads>[s<ket sets per warp>], P for persistent."""
+        """A launch shape given as <kets per thread>x<threads>[s<ket sets per warp>], P for persistent,
+        or T<tile bits>:<kets per thread>x256[s<ket sets per warp>] for staged tiles."""
+        if spec.startswith("T"):
+            tb, rest = spec[1:].split(":")
+            kt, rest = rest.split("x")
+            split = int(rest.split("s")[1]) if "s" in rest else 1
+            raise_for(lib.qob_op_set_tile(ctx.ptr, hd.ptr, L.QOB_LEFT, dtype_code(dt), int(kt), split, int(tb)), ctx)
+            return {"kets_per_thread": int(kt), "tile_bits": int(tb), "threads_per_block": 256,
+                    "ket_sets_per_warp": split, "persistent": False, "fixed": spec}
         kt, rest = spec.split("x")
         split = int(rest.split("s")[1]) if "s" in rest else 1
         blk = rest.split("s")[0]
@@ -453,10 +466,7 @@ def run_own(args, rank, world, local_rank):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src, "traffic": prof.get("dram_bytes_per_launch"),
                      "algorithmic_bytes_per_launch": bytes_per_ket * BATCH,
-                     "kernel": "{}<double, real values, square, {} kets/thread, real beta> x {} threads, {} ket sets/warp"
-                               .format("k_gather_p" if tuning["c128"]["persistent"] else "k_gather_j",
-                                       tuning["c128"]["kets_per_thread"], tuning["c128"]["threads_per_block"],
-                                       tuning["c128"]["ket_sets_per_warp"]),
+                     "kernel": kernel_name("double", tuning["c128"]),
                      "ncu_kernel": prof.get("kernel"),
                      "binding": "fp64 FMA throughput (GB300 FP64 ~1.25 TFLOP/s), see fp64_compute"},
         "fp64_compute": fp64,
@@ -475,12 +485,13 @@ def run_own(args, rank, world, local_rank):
         "gpu_launches": launches64,
         "rel_l2_err_vs_oracle": errs["c128"],
         "fp32_mode": {"value": value32, "unit": UNIT, "ms_per_step": ms32 / K, "vs_fp64": value32 / value,
-                      "rel_l2_err_vs_oracle": errs["c64"],
+                      "rel_l2_err_vs_oracle": errs["c64"], "kernel": kernel_name("float", tuning["c64"]),
                       "roofline": {"bound": "hbm", "achieved": bytes32 / (ms32 / 1e3 / K) / 1e9, "peak": peak,
                                    "unit": "GB/s", "frac": bytes32 / (ms32 / 1e3 / K) / 1e9 / peak,
                                    "algorithmic_bytes_per_launch": bytes32}},
         "ff_mode": {"value": valueff, "unit": UNIT, "ms_per_step": msff / K, "vs_fp64": valueff / value,
                     "rel_l2_err_vs_oracle": errs["c128x"], "gpu_launches": launchesff,
+                    "kernel": kernel_name("double-float", tuning["c128x"]),
                     "note": "ComplexF64 data, fused gather in double-float (FP32-pair) arithmetic, "
                             "one split launch + one gather launch per step (QOB_C128X)"},
         "oracle_check": "each form's result on one 64-ket batch of this workload (same qob_mul call, tuned "
@@ -494,6 +505,16 @@ def run_own(args, rank, world, local_rank):
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(H, args.cpu_seconds)
     print(json.dumps(line), flush=True)
+
+
+def kernel_name(scalar, t):
+    """The gather kernel a tuned shape runs, as the launch list names it."""
+    if t.get("tile_bits"):
+        return (f"k_gather_t<{scalar}, real values, {t['kets_per_thread']} kets/thread, real beta> x 256 threads, "
+                f"tiles of 2^{t['tile_bits']} indices, {t['ket_sets_per_warp']} ket sets/warp")
+    return "{}<{}, real values, square, {} kets/thread, real beta> x {} threads, {} ket sets/warp".format(
+        "k_gather_p" if t["persistent"] else "k_gather_j", scalar, t["kets_per_thread"], t["threads_per_block"],
+        t["ket_sets_per_warp"])
 
 
 def probe_peaks(dev):

@@ -43,6 +43,7 @@ extern "C" {
 #define QOB_ERR_OOM 6         /* device memory exhausted / admission refused */
 #define QOB_ERR_TIMEOUT 7     /* a bounded device-side wait gave up */
 #define QOB_ERR_STATE 8       /* call not valid in the object's current state */
+#define QOB_ERR_CANCELLED 9   /* the request was cancelled (qob_server_cancel) */
 
 /* element types */
 #define QOB_C128 0 /* ComplexF64 */
@@ -173,16 +174,23 @@ int qob_op_prepare(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t* info)
  * cover 8 output indices x 4 sets of vectors, 5 / 6 = 4 output indices x 8
  * sets, 7 / 8 = 2 output indices x 16 sets (entries that vary with the low
  * index bits then diverge over fewer lanes).  times_ms[9k + b] = milliseconds
- * per application with 2^k vectors per thread and shape b, -1 when not tried
- * (36 entries); *chosen = vectors per thread | (threads per block << 16) |
- * (log2 vector sets per warp << 26) | (1 << 30 when persistent), 0 when the
- * operator has no fused part.  Either pointer may be NULL.  Vector sets (x
- * and y) of 16 MB or more are timed with inputs not in L2 (up to 16 scratch
- * copies, at least 256 MB in all, used in turn), smaller ones L2-resident.
- * Each shape is timed over launches replayed from a CUDA graph on a stream of
- * the context's own (no host launch overhead in the times, as in the recorded
- * loops of qob_rk4 / the server).  Allocates and frees the scratch arrays;
- * synchronous. */
+ * per application with 2^k vectors per thread and shape b (36 entries).  For
+ * plans in the compact form (every merged group one run of power-of-two
+ * subsystems with one entry per row, e.g. spin chains) applied to kets from the
+ * left, twelve staged-tile shapes follow (times_ms[36 + i]): blocks of 256
+ * threads that copy tiles of 2^bits consecutive indices of their kets into
+ * shared memory, for (bits, vectors per thread, vector sets per warp) = (10,1,1)
+ * (10,2,1) (9,4,1) (11,1,1) (11,2,1) (12,1,1) (9,1,4) (8,1,16) (8,2,8) (9,2,4)
+ * (10,1,4) (7,2,16).  -1 marks a shape not tried; times_ms needs 48 entries.
+ * *chosen = vectors per thread | (tile bits << 8, 0 when untiled) | (threads
+ * per block << 16) | (log2 vector sets per warp << 26) | (1 << 30 when
+ * persistent), 0 when the operator has no fused part.  Either pointer may be
+ * NULL.  Vector sets (x and y) of 16 MB or more are timed with inputs not in L2
+ * (up to 16 scratch copies, at least 256 MB in all, used in turn), smaller ones
+ * L2-resident.  Each shape is timed over launches replayed from a CUDA graph on
+ * a stream of the context's own (no host launch overhead in the times, as in
+ * the recorded loops of qob_rk4 / the server).  Allocates and frees the scratch
+ * arrays; synchronous. */
 int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, double* times_ms,
                 int* chosen);
 
@@ -193,6 +201,26 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
  * the next tune or recompilation. */
 int qob_op_set_launch(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_per_thread, int block,
                       int lane_split);
+
+/* Fix a staged-tile shape instead of tuning (compact plans, kets from the
+ * left; other calls keep the untiled kernel with the same vectors per thread
+ * and lane split): tiles of 2^tile_bits indices (6 .. 16), vectors_per_thread
+ * 1, 2 or 4, lane_split as above, 256 threads.  A call whose tile does not fit
+ * (input not 16-byte aligned, or the tile's shared memory over 200 KB) runs the
+ * untiled kernel. */
+int qob_op_set_tile(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_per_thread, int lane_split,
+                    int tile_bits);
+
+/* Device status of the context: kernels with bounded waits (the staged-tile
+ * gather's wait for its copies) record a wait that gave up, and a library built
+ * with QOB_DEBUG_BOUNDS records gathered indices outside their vectors (the
+ * access is skipped), in a status word instead of faulting.  Reads the word
+ * (synchronising `stream`) into *flags (may be NULL) and clears it: 0 and
+ * QOB_OK when nothing was recorded; else QOB_ERR_TIMEOUT (bit 0: a wait gave
+ * up) or QOB_ERR_ARG (bit 1: an index was out of range), with the message in
+ * qob_last_error.  No counterpart in the reference, which only throws on the
+ * host. */
+int qob_device_status(qob_ctx* ctx, void* stream, unsigned* flags);
 
 /* ---------------------------------------------------------------------------
  * Application: the 5-argument mul!.
@@ -409,6 +437,23 @@ int qob_server_stop(qob_server* server);
 int qob_server_poll(qob_server* server, int64_t id, void* psi_out, double* times, int* status);
 int qob_server_wait(qob_server* server, int64_t id, double timeout_s, int* status);
 int qob_server_stats(qob_server* server, int64_t* stats);
+/* stats[0..1]: requests cancelled, allocations refused (by the hook or the device). */
+int qob_server_stats2(qob_server* server, int64_t* stats);
+/* Cancel a request (no counterpart in the reference).  A queued request leaves
+ * at once; a running one leaves before the engine's next iteration (at most 16
+ * steps later), its device memory released.  Its status becomes
+ * -QOB_ERR_CANCELLED and qob_server_wait returns for it.  QOB_ERR_STATE when the
+ * request has already finished or failed. */
+int qob_server_cancel(qob_server* server, int64_t id);
+/* Host-side allocation hook (no counterpart in the reference): hook(user,
+ * bytes) is called, with the server's lock held, before the device memory of
+ * each admission is allocated; a nonzero return refuses the allocation as if
+ * the device were out of memory.  A refused admission leaves the request queued
+ * while other requests run (they free memory when they finish); with nothing
+ * else active it is retried at the next iterations and rejected with
+ * -QOB_ERR_OOM after three refusals in a row.  Device allocation failures take
+ * the same path.  NULL removes the hook.  The hook must not call the server. */
+int qob_server_set_alloc_hook(qob_server* server, int (*hook)(void* user, size_t bytes), void* user);
 int qob_server_destroy(qob_server* server);
 
 /* ---------------------------------------------------------------------------

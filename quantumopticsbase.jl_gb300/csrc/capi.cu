@@ -312,6 +312,9 @@ int qob_create(qob_ctx** ctx, int device, unsigned flags) {
     QOB_CUDA(cudaGetDeviceCount(&n));
     if (device < 0 || device >= n) fail(QOB_ERR_ARG, "no such CUDA device");
     QOB_CUDA(cudaDeviceGetAttribute(&c->c.num_sms, cudaDevAttrMultiProcessorCount, device));
+    QOB_CUDA(cudaSetDevice(device));
+    c->c.status.alloc(16);
+    QOB_CUDA(cudaMemset(c->c.status.p, 0, 16));
   });
   if (rc) {
     delete c;
@@ -514,9 +517,16 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
     constexpr int kShapes = 9;
     const int blocks[kShapes] = {128, 256, -256, 128, 256, 128, 256, 128, 256};
     const int splits[kShapes] = {1, 1, 1, 4, 4, 8, 8, 16, 16};
-    double t[4 * kShapes];
+    // staged tiles (compact plans, vectors from the left): 2^bits indices x
+    // vectors per thread x vector sets per warp, 256 threads
+    constexpr int kTileShapes = 12;
+    const int tbits_c[kTileShapes] = {10, 10, 9, 11, 11, 12, 9, 8, 8, 9, 10, 7};
+    const int ttc_c[kTileShapes] = {1, 2, 4, 1, 2, 1, 1, 1, 2, 2, 1, 2};
+    const int tls_c[kTileShapes] = {1, 1, 1, 1, 1, 1, 4, 16, 8, 4, 4, 16};
+    constexpr int kCands = 4 * kShapes + kTileShapes;
+    double t[kCands];
     for (double& v : t) v = -1.0;
-    int best = 0, best_block = 256, best_split = 1;
+    int best = 0, best_block = 256, best_split = 1, best_tile = 0;
     if (P.gather && P.kind == Plan::Kind::Sum) {
       GatherPlan& g = *P.gather;
       const size_t esz = elem_size(dtype);
@@ -540,17 +550,33 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
       // vectors as the reference lays them out: columns for LEFT, rows for RIGHT
       const int64_t xes = side == QOB_LEFT ? 1 : ncols, xcs = side == QOB_LEFT ? P.n : 1;
       const int64_t yes = side == QOB_LEFT ? 1 : ncols, ycs = side == QOB_LEFT ? P.m : 1;
+      int mbits = 0;
+      while ((int64_t(1) << mbits) < g.m) ++mbits;
+      const bool tiles_ok = g.fast && g.square && side == QOB_LEFT && (int64_t(1) << mbits) == g.m;
       cudaEvent_t e0, e1;
       QOB_CUDA(cudaEventCreate(&e0));
       QOB_CUDA(cudaEventCreate(&e1));
       double best_t = 1e300;
-      for (int k = 0; k < 4 * kShapes; ++k) {
-        const int tc = tiles[k / kShapes], blk = blocks[k % kShapes], ls = splits[k % kShapes];
-        if (tc > ncols || (tc > 1 && side == QOB_RIGHT && ncols > 1)) continue;
-        if (ls > 1 && (tc * ls > ncols || side == QOB_RIGHT)) continue;
+      for (int k = 0; k < kCands; ++k) {
+        int tc, blk, ls, tb = 0;
+        if (k < 4 * kShapes) {
+          tc = tiles[k / kShapes];
+          blk = blocks[k % kShapes];
+          ls = splits[k % kShapes];
+          if (tc > ncols || (tc > 1 && side == QOB_RIGHT && ncols > 1)) continue;
+          if (ls > 1 && (tc * ls > ncols || side == QOB_RIGHT)) continue;
+        } else {
+          const int i = k - 4 * kShapes;
+          tc = ttc_c[i];
+          blk = 256;
+          ls = tls_c[i];
+          tb = tbits_c[i];
+          if (!tiles_ok || tb > mbits || tc * ls > ncols) continue;
+        }
         g.tc = tc;
         g.block = blk;
         g.lane_split = ls;
+        g.tile_bits = tb;
         for (int i = 0; i < 2; ++i)
           apply_plan(ctx->c, P, {1.0, 0.0}, xc(i), xes, xcs, {0.3, 0.0}, yc(i), yes, ycs, ncols, ts, 0);
         const int reps = std::max(8, copies);
@@ -584,20 +610,23 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
           best = tc;
           best_block = blk;
           best_split = ls;
+          best_tile = tb;
         }
       }
       g.tc = best;
       g.block = best_block;
       g.lane_split = best_split;
+      g.tile_bits = best_tile;
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
     }
     if (times_ms)
-      for (int k = 0; k < 4 * kShapes; ++k) times_ms[k] = t[k];
+      for (int k = 0; k < kCands; ++k) times_ms[k] = t[k];
     int lg = 0;
     while ((1 << lg) < best_split) ++lg;
     if (chosen)
-      *chosen = best | ((best_block < 0 ? -best_block : best_block) << 16) | (lg << 26) | (best_block < 0 ? (1 << 30) : 0);
+      *chosen = best | (best_tile << 8) | ((best_block < 0 ? -best_block : best_block) << 16) | (lg << 26) |
+                (best_block < 0 ? (1 << 30) : 0);
   });
 }
 
@@ -616,6 +645,79 @@ int qob_op_set_launch(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors
       P.gather->tc = vectors_per_thread;
       P.gather->block = block;
       P.gather->lane_split = lane_split;
+      P.gather->tile_bits = 0;
+    }
+  });
+}
+
+int qob_op_set_tile(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_per_thread, int lane_split,
+                    int tile_bits) {
+  return guard(ctx, [&] {
+    if (!ctx || !op || (side != QOB_LEFT && side != QOB_RIGHT)) fail(QOB_ERR_ARG, "qob_op_set_tile: bad arguments");
+    check_mul_dtype(dtype);
+    if (vectors_per_thread != 1 && vectors_per_thread != 2 && vectors_per_thread != 4)
+      fail(QOB_ERR_ARG, "vectors per thread must be 1, 2 or 4 for staged tiles");
+    if (lane_split < 1 || lane_split > 32 || (lane_split & (lane_split - 1)) != 0)
+      fail(QOB_ERR_ARG, "lane_split must be 1, 2, 4, 8, 16 or 32");
+    if (tile_bits < 6 || tile_bits > 16) fail(QOB_ERR_ARG, "tile_bits must be in 6 .. 16");
+    Plan& P = get_plan(ctx->c, op, side, dtype);
+    if (P.gather) {
+      P.gather->tc = vectors_per_thread;
+      P.gather->block = 256;
+      P.gather->lane_split = lane_split;
+      P.gather->tile_bits = tile_bits;
+    }
+  });
+}
+
+#ifdef QOB_DEBUG_BOUNDS
+// Bounds-checked build only: moves the input offset of the first stored entry
+// with a nonzero value of op's compiled gather (side, dtype) by col_shift, so
+// that a test can watch the device checks catch an index out of range.
+int qob_debug_shift_slot(qob_ctx* ctx, qob_op* op, int side, int dtype, int col_shift) {
+  return guard(ctx, [&] {
+    if (!ctx || !op || (side != QOB_LEFT && side != QOB_RIGHT)) fail(QOB_ERR_ARG, "qob_debug_shift_slot: bad arguments");
+    check_mul_dtype(dtype);
+    Plan& P = get_plan(ctx->c, op, side, dtype);
+    if (!P.gather || P.gather->ell_slots <= 0) fail(QOB_ERR_UNSUPPORTED, "no fixed-width slots in this plan");
+    GatherPlan& g = *P.gather;
+    const size_t n = (size_t)g.ell_slots;
+    const size_t sz = g.ell.bytes / n;  // slot size: col (int32) first, the value after the padding
+    std::vector<unsigned char> h(n * sz);
+    QOB_CUDA(cudaDeviceSynchronize());
+    QOB_CUDA(cudaMemcpy(h.data(), g.ell.p, h.size(), cudaMemcpyDeviceToHost));
+    const size_t voff = sz >= 16 ? 8 : 4;
+    for (size_t i = 0; i < n; ++i) {
+      unsigned char* e = h.data() + i * sz;
+      bool nonzero = false;
+      for (size_t b = voff; b < sz; ++b) nonzero |= e[b] != 0;
+      if (!nonzero) continue;
+      int32_t col;
+      std::memcpy(&col, e, 4);
+      col += col_shift;
+      std::memcpy(e, &col, 4);
+      QOB_CUDA(cudaMemcpy(g.ell.p, h.data(), h.size(), cudaMemcpyHostToDevice));
+      return;
+    }
+    fail(QOB_ERR_UNSUPPORTED, "no stored entry with a nonzero value");
+  });
+}
+#endif
+
+int qob_device_status(qob_ctx* ctx, void* stream, unsigned* flags) {
+  return guard(ctx, [&] {
+    if (!ctx) fail(QOB_ERR_ARG, "qob_device_status: bad arguments");
+    unsigned w = 0;
+    const cudaStream_t s = (cudaStream_t)stream;
+    QOB_CUDA(cudaMemcpyAsync(&w, ctx->c.status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    QOB_CUDA(cudaStreamSynchronize(s));
+    if (flags) *flags = w;
+    if (w) {
+      QOB_CUDA(cudaMemsetAsync(ctx->c.status.p, 0, sizeof(unsigned), s));
+      QOB_CUDA(cudaStreamSynchronize(s));
+      if (w & 2u)
+        fail(QOB_ERR_ARG, "device status: a kernel met an out-of-range index (bounds-checked build) and skipped it");
+      fail(QOB_ERR_TIMEOUT, "device status: a kernel's bounded wait gave up; its output is incomplete");
     }
   });
 }

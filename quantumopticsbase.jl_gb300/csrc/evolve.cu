@@ -260,6 +260,8 @@ struct Request {
   int step = 0;
   double dt = 0.0;
   int status = 0;  // 0 queued, 1 active, 2 done, negative: error code
+  bool cancel = false;    // cancelled while active: retired at the next engine iteration
+  int alloc_failures = 0;  // refused allocations while nothing else was active
   std::vector<char> psi0, result;
   double t_submit = 0, t_admit = 0, t_done = 0;
   void* dev = nullptr;
@@ -300,16 +302,45 @@ struct qob_server {
   std::thread worker;
   bool stop = false;
   bool running = false;
-  int64_t steps_run = 0, iterations = 0, rejected = 0, completed = 0;
+  int64_t steps_run = 0, iterations = 0, rejected = 0, completed = 0, cancelled = 0, alloc_refusals = 0;
   int last_error = 0;
   std::string last_msg;
+  // host-side allocation hook, asked before every admission's device allocation
+  int (*alloc_hook)(void* user, size_t bytes) = nullptr;
+  void* alloc_user = nullptr;
 };
 
 namespace {
 
 size_t elem_bytes(int dtype) { return dtype == QOB_C64 ? 8 : 16; }
 
-// Admit queued requests while a slot and memory are free (lock held).
+// Consecutive refused allocations, with no other request active, after which a
+// queued request is rejected (nothing in this server will free memory for it).
+constexpr int kMaxAllocFailures = 3;
+
+// A request leaves the server with a final status (lock held): its device
+// memory is released and waiters are woken.
+void retire(qob_server* S, Request* r, int status) {
+  if (r->dev) {
+    cudaFreeAsync(r->dev, S->stream);  // best effort: after a failed iteration the stream may carry the error
+    cudaGetLastError();
+    S->mem_used -= r->bytes;
+    r->dev = nullptr;
+  }
+  r->own_plan.reset();
+  r->rows = qob::DeviceBuf();
+  r->step_ctr = qob::DeviceBuf();
+  r->rows_host.clear();
+  r->status = status;
+  r->t_done = now_s();
+  S->cv.notify_all();
+}
+
+// Admit queued requests while a slot and memory are free (lock held).  An
+// allocation that the hook refuses or that the device cannot serve leaves the
+// request queued while other requests run (their memory comes back when they
+// finish); with nothing active it is retried at the next iterations and the
+// request is rejected with -QOB_ERR_OOM after kMaxAllocFailures refusals.
 void admit(qob_server* S) {
   while (!S->queue.empty() && (int)S->active.size() < S->max_active) {
     Request* r = S->queue.front();
@@ -317,7 +348,22 @@ void admit(qob_server* S) {
     size_t free_b = 0, total_b = 0;
     QOB_CUDA(cudaMemGetInfo(&free_b, &total_b));
     if (S->mem_used + need > S->budget || need + (size_t(256) << 20) > free_b) break;  // wait for memory
-    QOB_CUDA(cudaMallocAsync(&r->dev, need, S->stream));
+    cudaError_t ae = cudaErrorMemoryAllocation;
+    if (!S->alloc_hook || S->alloc_hook(S->alloc_user, need) == 0) ae = cudaMallocAsync(&r->dev, need, S->stream);
+    if (ae != cudaSuccess) {
+      if (ae != cudaErrorMemoryAllocation) QOB_CUDA(ae);
+      cudaGetLastError();
+      r->dev = nullptr;
+      S->alloc_refusals++;
+      if (S->active.empty() && ++r->alloc_failures >= kMaxAllocFailures) {
+        S->queue.pop_front();
+        S->rejected++;
+        retire(S, r, -QOB_ERR_OOM);
+        continue;
+      }
+      break;  // stays queued
+    }
+    r->alloc_failures = 0;
     r->bytes = need;
     S->mem_used += need;
     QOB_CUDA(cudaMemcpyAsync(r->dev, r->psi0.data(), r->psi0.size(), cudaMemcpyHostToDevice, S->stream));
@@ -420,6 +466,24 @@ int iterate(qob_server* S, int max_steps) {
   bool waiting = false;
   {
     std::lock_guard<std::mutex> lk(S->mu);
+    // requests cancelled while active leave between iterations
+    bool any = false;
+    for (Request* r : S->active) any |= r->cancel;
+    if (any) {
+      QOB_CUDA(cudaStreamSynchronize(S->stream));
+      drop_graph(S);
+      std::vector<Request*> keep;
+      for (Request* r : S->active) {
+        if (r->cancel) {
+          S->cancelled++;
+          retire(S, r, -QOB_ERR_CANCELLED);
+        } else {
+          keep.push_back(r);
+        }
+      }
+      S->active.swap(keep);
+      S->dirty = true;
+    }
     admit(S);
     act = S->active;
     waiting = !S->queue.empty();
@@ -506,14 +570,12 @@ void worker_loop(qob_server* S) {
       std::lock_guard<std::mutex> lk(S->mu);
       S->last_error = code;
       S->last_msg = msg;
-      // fail the requests in flight; the server keeps serving new ones
-      for (Request* r : S->active) {
-        r->status = -code;
-        r->t_done = now_s();
-      }
+      // fail the requests in flight and give their memory back; the server
+      // keeps serving new ones
+      drop_graph(S);
+      for (Request* r : S->active) retire(S, r, -code);
       S->active.clear();
       S->dirty = true;
-      S->cv.notify_all();
     }
   }
 }
@@ -689,6 +751,42 @@ int qob_server_stats(qob_server* S, int64_t* out) {
     out[5] = S->iterations;
     out[6] = (int64_t)S->mem_used;
     out[7] = S->last_error;
+  });
+}
+
+int qob_server_stats2(qob_server* S, int64_t* out) {
+  return sguard(S, [&] {
+    if (!out) qob::fail(QOB_ERR_ARG, "qob_server_stats2: null output");
+    std::lock_guard<std::mutex> lk(S->mu);
+    out[0] = S->cancelled;
+    out[1] = S->alloc_refusals;
+  });
+}
+
+int qob_server_cancel(qob_server* S, int64_t id) {
+  return sguard(S, [&] {
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->all.find(id);
+    if (it == S->all.end()) qob::fail(QOB_ERR_ARG, "unknown request id");
+    Request* r = it->second.get();
+    if (r->status == 0) {  // queued: leaves at once
+      S->queue.erase(std::find(S->queue.begin(), S->queue.end(), r));
+      S->cancelled++;
+      retire(S, r, -QOB_ERR_CANCELLED);
+    } else if (r->status == 1) {  // running: leaves before the engine's next iteration
+      r->cancel = true;
+      S->cv.notify_all();
+    } else {
+      qob::fail(QOB_ERR_STATE, "the request has already finished");
+    }
+  });
+}
+
+int qob_server_set_alloc_hook(qob_server* S, int (*hook)(void* user, size_t bytes), void* user) {
+  return sguard(S, [&] {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->alloc_hook = hook;
+    S->alloc_user = user;
   });
 }
 

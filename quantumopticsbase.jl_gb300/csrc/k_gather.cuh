@@ -43,6 +43,22 @@
 namespace qob {
 namespace gather {
 
+// Bounds-checked build (-DQOB_DEBUG_BOUNDS): every slot index and gathered
+// input index is checked before use; an out-of-range one is skipped and
+// recorded in the context's device status word (bit kErrBoundsBit), which
+// qob_device_status reports.  Off in the product build.
+#ifdef QOB_DEBUG_BOUNDS
+constexpr bool kDebugBounds = true;
+#else
+constexpr bool kDebugBounds = false;
+#endif
+constexpr unsigned kErrBoundsBit = 2u;
+__device__ __forceinline__ bool out_of_range(int64_t i, int64_t n, unsigned* status) {
+  if (i >= 0 && i < n) return false;
+  if (status) atomicOr(status, kErrBoundsBit);
+  return true;
+}
+
 __device__ __forceinline__ uint32_t fdiv(uint32_t n, uint32_t d, uint64_t M) {
   return d == 1u ? n : (uint32_t)__umul64hi(M, (uint64_t)n);
 }
@@ -564,9 +580,11 @@ __device__ __forceinline__ void accumulate(const GatherView& g, const SiteTable&
     for (int gi = 0; gi < g.ngroups; ++gi) {
       const int4 f = fg[gi];
       const uint32_t r = (J >> f.x) & (uint32_t)f.y;
+      if (kDebugBounds && out_of_range((int64_t)f.z + r, g.ell_slots, g.status)) continue;
       const ET s = ell[f.z + r];
       const VT v = Ell<R, VM != kComplex>::v(s);
       const CT* xp = xb + ((int64_t)(J - (r << f.x)) + s.col) * es;
+      if (kDebugBounds && nz(v) && out_of_range((int64_t)(J - (r << f.x)) + s.col, g.n, g.status)) continue;
       if (nz(v)) {
         if (VM == kPhased && f.w != 0) {
 #pragma unroll
@@ -588,9 +606,11 @@ __device__ __forceinline__ void accumulate(const GatherView& g, const SiteTable&
       const GGroup& G = sg[gi];
       uint32_t r, sub;
       local_row(G, J, r, sub);
+      if (kDebugBounds && out_of_range((int64_t)G.ell_off + r, g.ell_slots, g.status)) continue;
       const ET s = ell[G.ell_off + r];
       const VT v = Ell<R, VM != kComplex>::v(s);
       const CT* xp = xb + ((int64_t)(J - sub) + s.col) * es;
+      if (kDebugBounds && nz(v) && out_of_range((int64_t)(J - sub) + s.col, g.n, g.status)) continue;
       if (nz(v)) {
         if (VM == kPhased && G.imag != 0) {
 #pragma unroll
@@ -615,8 +635,10 @@ __device__ __forceinline__ void accumulate(const GatherView& g, const SiteTable&
     if (G.width > 0) {
       const ET* e = ell + G.ell_off + (int64_t)r * G.width;
       for (int k = 0; k < G.width; ++k) {
+        if (kDebugBounds && out_of_range((int64_t)G.ell_off + (int64_t)r * G.width + k, g.ell_slots, g.status)) continue;
         const ET s = e[k];
         const VT v = Ell<R, VM != kComplex>::v(s);
+        if (kDebugBounds && nz(v) && out_of_range(base + s.col, g.n, g.status)) continue;
         if (nz(v)) {
           const CT* xp = xb + (base + s.col) * es;
           if (im) {
@@ -634,6 +656,7 @@ __device__ __forceinline__ void accumulate(const GatherView& g, const SiteTable&
       const int p0 = __ldg(g.rowptr + G.rowptr_off + r);
       const int p1 = __ldg(g.rowptr + G.rowptr_off + r + 1);
       for (int p = p0; p < p1; ++p) {
+        if (kDebugBounds && out_of_range(base + __ldg(g.coloff + p), g.n, g.status)) continue;
         const CT* xp = xb + (base + __ldg(g.coloff + p)) * es;
         const VT v = vals[p];
         if (im) {
@@ -767,6 +790,14 @@ __global__ void __launch_bounds__(256) k_gather_c(GatherView g, SiteTable st,
   combine<BMODE>(y + J * yes + c * ycs, acc[0].total(), alpha, beta);
 }
 
+}  // namespace gather
+}  // namespace qob
+
+#include "k_tile.cuh"
+
+namespace qob {
+namespace gather {
+
 // ---------------------------------------------------------------------------
 // host-side dispatch (instantiated per precision)
 
@@ -849,6 +880,24 @@ void launch_tc(const GatherView& v, const SiteTable& st, int tc, const void* x, 
   }
 }
 
+// Shared memory of one staged-tile block at most (GB300: 227 KB per block)
+constexpr size_t kTileSmemMax = 200 * 1024;
+
+template <typename R, int VM, int BMODE>
+void launch_tile_tc(const GatherView& v, int tc, const void* x, int64_t xcs, void* y, int64_t ycs, int64_t ncols,
+                    typename Cx<R>::T a, typename Cx<R>::T b, cudaStream_t s) {
+  switch (tc) {
+    case 4:
+      launch_t<R, VM, 4, BMODE>(v, x, xcs, y, ycs, ncols, a, b, s, v.status);
+      break;
+    case 2:
+      launch_t<R, VM, 2, BMODE>(v, x, xcs, y, ycs, ncols, a, b, s, v.status);
+      break;
+    default:
+      launch_t<R, VM, 1, BMODE>(v, x, xcs, y, ycs, ncols, a, b, s, v.status);
+  }
+}
+
 template <typename R, int VM, bool SQUARE, int BMODE>
 void dispatch_layout(const GatherView& v, const SiteTable& st, int tc, const void* x, int64_t xes,
                      int64_t xcs, void* y, int64_t yes, int64_t ycs, int64_t ncols, typename Cx<R>::T a, typename Cx<R>::T b,
@@ -862,6 +911,26 @@ void dispatch_layout(const GatherView& v, const SiteTable& st, int tc, const voi
   w.ell_smem = (v.ell_slots > 0 && ell_bytes <= kStageSlotsMax && smem + ell_bytes <= kSmemBudget) ? 1 : 0;
   if (w.ell_smem) smem += ell_bytes;
   if (xes == 1 && yes == 1) {
+    if constexpr (SQUARE) {
+      // staged tiles for compact plans (a tuned choice), when the tile and the
+      // bulk copies fit this call; the slots are staged when the budget allows
+      if (v.tile_bits > 0 && v.fast && tile_fits<R>(v, v.tile_bits, x, xcs, ncols)) {
+        const int ttc = tc >= 4 ? 4 : tc;  // the tiled kernel takes 1, 2 or 4 vectors per thread
+        int ls = v.lane_split > 0 ? v.lane_split : 1;
+        while (ls > 1 && (int64_t)ttc * ls > ncols) ls >>= 1;
+        GatherView t = v;
+        t.ell_smem = 1;
+        size_t need = tile_smem<XT, ET>(v.tile_bits, ttc * ls, v.ngroups, v.ell_slots, true);
+        if (v.ell_slots <= 0 || (size_t)v.ell_slots * sizeof(ET) > kStageSlotsMax || need > kTileSmemMax) {
+          t.ell_smem = 0;
+          need = tile_smem<XT, ET>(v.tile_bits, ttc * ls, v.ngroups, v.ell_slots, false);
+        }
+        if (need <= kTileSmemMax) {
+          launch_tile_tc<R, VM, BMODE>(t, ttc, x, xcs, y, ycs, ncols, a, b, s);
+          return;
+        }
+      }
+    }
     if (SQUARE && v.all_w1)
       launch_tc<R, VM, SQUARE, true, BMODE>(w, st, tc, x, xcs, y, ycs, ncols, a, b, smem, s);
     else

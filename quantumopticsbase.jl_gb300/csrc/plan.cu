@@ -843,6 +843,7 @@ static std::unique_ptr<Plan> compile_sum(Context& ctx, const NodeP& root, int si
   for (auto& g : B.groups) any_raw |= !g.raw.empty();
   if (any_raw) {
     P->gather = std::make_unique<GatherPlan>();
+    P->gather->status = static_cast<unsigned*>(ctx.status.p);
     finalize_gather(*P->gather, B, root.get(), precision, P->m, P->n);
   }
   return P;
@@ -1081,6 +1082,8 @@ GatherView GatherPlan::view() const {
   v.fastg = (const int4*)fastg.p;
   v.block = block;
   v.lane_split = lane_split;
+  v.tile_bits = tile_bits;
+  v.status = status;
   return v;
 }
 

@@ -184,6 +184,8 @@ struct GatherView {
   // bits through the operator's sparsity -- averages out over the blocks an SM runs.
   uint32_t jmul;
   int32_t lane_split;  // k_gather_j: vector sets per warp (1, 2, 4 or 8; 32/lane_split indices per warp)
+  int32_t tile_bits;   // > 0: compact plans on kets use k_gather_t with tiles of 2^tile_bits indices
+  unsigned* status;    // the context's device status word (bounded waits that gave up, failed checks)
 };
 
 // A host-side record of how each stored entry is made from the terms, so a
@@ -260,6 +262,8 @@ struct GatherPlan {
   int tc = 0;     // vectors per thread chosen by qob_op_tune (0: automatic)
   int block = 0;  // threads per block chosen by qob_op_tune (0: 256; < 0: persistent grid of -block)
   int lane_split = 1;  // vector sets per warp chosen by qob_op_tune
+  int tile_bits = 0;   // > 0: staged tiles of 2^tile_bits indices (k_gather_t), chosen by qob_op_tune
+  unsigned* status = nullptr;  // the owning context's device status word
   DeviceBuf dgroups, dvals;  // diagonal sources: groups + local diagonal tables
   int ndgroups = 0;
   SiteTable sites{};
@@ -364,6 +368,9 @@ struct Context {
   static constexpr int kTickets = 16;
   cudaEvent_t ticket_done[kTickets] = {};
   uint64_t host_calls = 0;
+  // device status word (one unsigned, zeroed at creation): kernels record
+  // bounded waits that gave up and failed debug checks; read by qob_device_status
+  DeviceBuf status;
   ~Context();
 };
 

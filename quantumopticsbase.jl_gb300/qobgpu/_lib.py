@@ -9,7 +9,10 @@ import ctypes as C
 import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libqobgpu.so")
+# QOB_LIBRARY selects another build of the same library (the bounds-checked
+# build, libqobgpu_debug.so, for its own tests)
+LIB_PATH = os.environ.get("QOB_LIBRARY") or os.path.join(_HERE, "libqobgpu.so")
+ALLOC_HOOK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_size_t)
 
 QOB_OK = 0
 QOB_ERR_DIM = 1
@@ -20,6 +23,7 @@ QOB_ERR_CUDA = 5
 QOB_ERR_OOM = 6
 QOB_ERR_TIMEOUT = 7
 QOB_ERR_STATE = 8
+QOB_ERR_CANCELLED = 9
 QOB_C128 = 0
 QOB_C64 = 1
 QOB_C128X = 2  # ComplexF64 data, fused part in double-float arithmetic
@@ -53,6 +57,8 @@ SIGNATURES = {
     "qob_op_prepare": (I, [VP, VP, I, I, I64P]),
     "qob_op_tune": (I, [VP, VP, I, I, I64, DP, C.POINTER(C.c_int)]),
     "qob_op_set_launch": (I, [VP, VP, I, I, I, I, I]),
+    "qob_op_set_tile": (I, [VP, VP, I, I, I, I, I]),
+    "qob_device_status": (I, [VP, VP, C.POINTER(C.c_uint)]),
     "qob_mul": (I, [VP, I, I, VP, I, D, D, VP, I64, I64, I64, D, D, VP, I64, I64, I64, VP]),
     "qob_mul_host": (I, [VP, I, I, VP, I, D, D, VP, I64, I64, D, D, VP, I64, I64]),
     "qob_mul_host_async": (I, [VP, I, I, VP, I, D, D, VP, I64, I64, D, D, VP, I64, I64, VP]),
@@ -87,6 +93,9 @@ SIGNATURES = {
     "qob_server_poll": (I, [VP, I64, VP, DP, C.POINTER(C.c_int)]),
     "qob_server_wait": (I, [VP, I64, D, C.POINTER(C.c_int)]),
     "qob_server_stats": (I, [VP, I64P]),
+    "qob_server_stats2": (I, [VP, I64P]),
+    "qob_server_cancel": (I, [VP, I64]),
+    "qob_server_set_alloc_hook": (I, [VP, VP, VP]),
     "qob_server_destroy": (I, [VP]),
     "qob_graph_begin": (I, [VP, VP]),
     "qob_graph_end": (I, [VP, VP, C.POINTER(VP)]),

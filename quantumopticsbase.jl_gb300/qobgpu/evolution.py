@@ -180,12 +180,30 @@ class Server:
         raise_for(L.lib().qob_server_stats(self.ptr, v), self.ctx)
         keys = ["queued", "active", "completed", "rejected", "request_steps", "iterations", "device_bytes",
                 "last_error"]
-        return dict(zip(keys, list(v)))
+        w = (C.c_int64 * 2)()
+        raise_for(L.lib().qob_server_stats2(self.ptr, w), self.ctx)
+        return dict(zip(keys, list(v)), cancelled=w[0], alloc_refusals=w[1])
+
+    def cancel(self, rid: int) -> None:
+        """Cancel a queued or running request (status -QOB_ERR_CANCELLED)."""
+        raise_for(L.lib().qob_server_cancel(self.ptr, rid), self.ctx)
+
+    def set_alloc_hook(self, hook) -> None:
+        """``hook(nbytes) -> bool``: asked before each admission's device
+        allocation; False refuses it as if the device were out of memory.  None
+        removes the hook."""
+        if hook is None:
+            self._hook = None
+            raise_for(L.lib().qob_server_set_alloc_hook(self.ptr, None, None), self.ctx)
+            return
+        self._hook = L.ALLOC_HOOK(lambda user, nbytes: 0 if hook(int(nbytes)) else 1)
+        raise_for(L.lib().qob_server_set_alloc_hook(self.ptr, C.cast(self._hook, C.c_void_p), None), self.ctx)
 
     def close(self):
         if self.ptr:
             L.lib().qob_server_destroy(self.ptr)
             self.ptr = None
+            self._hook = None
 
     def __del__(self):
         try:

@@ -176,3 +176,90 @@ def test_server_worker_thread_and_budget_rejection():
     assert stats["completed"] == 6 and stats["rejected"] == 1 and stats["device_bytes"] == 0
     S.stop()
     S.close()
+
+
+def test_server_cancel_queued_and_running():
+    """qob_server_cancel: a queued request leaves at once, a running one before
+    the engine's next iteration; both end with status -QOB_ERR_CANCELLED, their
+    memory back, and the other requests' results are unchanged."""
+    from qobgpu.evolution import Server
+
+    H = heisenberg_chain(8, seed=41)
+    rng = Q.Rng(42)
+    psis = [rng.ket_data(len(H.basis_l)) for _ in range(3)]
+    S = Server(np.complex128, max_active=1)  # one at a time: the second waits in the queue
+    a = S.submit(H, psis[0], 40, 1e-3)
+    b = S.submit(H, psis[1], 40, 1e-3)
+    S.step()  # a runs, b is queued
+    assert S.poll(b)[0] == 0
+    S.cancel(b)
+    assert S.poll(b)[0] == -9
+    c = S.submit(H, psis[2], 400, 1e-3)
+    while S.poll(a)[0] != 2:
+        S.step()
+    S.step()  # c is admitted and runs
+    assert S.poll(c)[0] == 1
+    S.cancel(c)
+    S.step()  # retired before this iteration steps
+    st = S.poll(c)[0]
+    assert st == -9
+    stats = S.stats()
+    assert stats["cancelled"] == 2 and stats["active"] == 0 and stats["device_bytes"] == 0
+    assert rel_l2(S.poll(a)[2], rk4_host(H, psis[0], 1e-3, 40)) < 1e-12
+    d = S.submit(H, psis[1], 20, 1e-3)  # the server goes on
+    while S.step():
+        pass
+    assert S.poll(d)[0] == 2
+    assert rel_l2(S.poll(d)[2], rk4_host(H, psis[1], 1e-3, 20)) < 1e-12
+    import pytest as _pytest
+
+    from qobgpu.device import QobError
+
+    with _pytest.raises(QobError):
+        S.cancel(d)  # already finished: QOB_ERR_STATE
+    S.close()
+
+
+def test_server_alloc_hook_queues_then_rejects():
+    """A host-side allocation hook that refuses memory: with other requests
+    running the new one waits in the queue and runs once the hook allows it (same
+    result as alone); with nothing running it is rejected with -QOB_ERR_OOM
+    after three refusals; the server keeps serving afterwards."""
+    from qobgpu.evolution import Server
+
+    H = heisenberg_chain(8, seed=43)
+    rng = Q.Rng(44)
+    p0, p1, p2 = (rng.ket_data(len(H.basis_l)) for _ in range(3))
+    S = Server(np.complex128)
+    a = S.submit(H, p0, 30, 1e-3)
+    S.step()  # a admitted
+    allow = {"on": False}
+    asked = []
+
+    def hook(nbytes):
+        asked.append(nbytes)
+        return allow["on"]
+
+    S.set_alloc_hook(hook)
+    b = S.submit(H, p1, 30, 1e-3)
+    for _ in range(3):
+        S.step()
+    assert S.poll(b)[0] == 0 and asked  # refused, still queued while a runs
+    allow["on"] = True
+    while S.step():
+        pass
+    assert S.poll(a)[0] == 2 and S.poll(b)[0] == 2
+    assert rel_l2(S.poll(b)[2], rk4_host(H, p1, 1e-3, 30)) < 1e-12
+    allow["on"] = False
+    c = S.submit(H, p2, 10, 1e-3)
+    for _ in range(4):
+        S.step()
+    assert S.poll(c)[0] == -6  # nothing else active: rejected after three refusals
+    st = S.stats()
+    assert st["alloc_refusals"] >= 4 and st["device_bytes"] == 0
+    S.set_alloc_hook(None)
+    d = S.submit(H, p2, 10, 1e-3)
+    while S.step():
+        pass
+    assert S.poll(d)[0] == 2
+    S.close()
