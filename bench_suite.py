@@ -68,14 +68,33 @@ def _timed_graph(ctx, stream, record, reps=20):
     return e0.elapsed_time(e1) / reps
 
 
-def _modes():
+def _modes(dmma=False):
     """(torch dtype, numpy dtype, dtype code, label): ComplexF64, ComplexF64 in
-    double-float arithmetic (QOB_C128X), ComplexF32."""
+    double-float arithmetic (QOB_C128X), ComplexF32; with dmma, also ComplexF64
+    on the FP64 tensor cores (QOB_OPT_FP64_TENSOR), labelled "complex128 DMMA"."""
     import torch
 
-    return ((torch.complex128, np.complex128, L.QOB_C128, "complex128"),
-            (torch.complex128, np.complex128, L.QOB_C128X, "complex128 double-float"),
-            (torch.complex64, np.complex64, L.QOB_C64, "complex64"))
+    out = [(torch.complex128, np.complex128, L.QOB_C128, "complex128"),
+           (torch.complex128, np.complex128, L.QOB_C128X, "complex128 double-float"),
+           (torch.complex64, np.complex64, L.QOB_C64, "complex64")]
+    if dmma:
+        out.insert(1, (torch.complex128, np.complex128, L.QOB_C128, "complex128 DMMA"))
+    return tuple(out)
+
+
+class _Fp64Tensor:
+    """QOB_OPT_FP64_TENSOR on for the rows labelled DMMA."""
+
+    def __init__(self, ctx, label):
+        self.ctx, self.on = ctx, label.endswith("DMMA")
+
+    def __enter__(self):
+        if self.on:
+            raise_for(L.lib().qob_set_option(self.ctx.ptr, L.QOB_OPT_FP64_TENSOR, 1), self.ctx)
+
+    def __exit__(self, *exc):
+        if self.on:
+            raise_for(L.lib().qob_set_option(self.ctx.ptr, L.QOB_OPT_FP64_TENSOR, 0), self.ctx)
 
 
 def _cols(n, k, dt, seed):
@@ -383,13 +402,14 @@ def modek(ctx, stream):
         op = O.LazyTensor(b, b, sites, facs, 0.3)
         h = handle(ctx, op)
         n = len(b)
-        for tdt, npdt, code, label in _modes():
+        for tdt, npdt, code, label in _modes(dmma=True):
             for ncols in (1, 16):
                 x = _cols(n, ncols, tdt, 61)
                 y = _cols(n, ncols, tdt, 62)
                 reps = 5
-                ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, L.QOB_LEFT, n, n, ncols, x, y, code,
-                                                             reps=reps))
+                with _Fp64Tensor(ctx, label):
+                    ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, L.QOB_LEFT, n, n, ncols, x, y, code,
+                                                                 reps=reps))
                 t = ms * 1e-3 / reps
                 flops = 8.0 * n * ncols * sum(dims[s - 1] for s in sites)  # complex FMA = 8 flop per term
                 out.append({"dims": list(dims), "dense_sites": list(sites), "dtype": label, "kets": ncols,
@@ -410,13 +430,14 @@ def dense(ctx, stream):
         b = GenericBasis(nd)
         op = O.Operator(b, b, np.asfortranarray(rng.complex_normal(nd * nd).reshape(nd, nd, order="F")))
         h = handle(ctx, op)
-        for tdt, npdt, code, label in _modes():
+        for tdt, npdt, code, label in _modes(dmma=True):
             for ncols in kets:
                 x = _cols(nd, ncols, tdt, 71)
                 y = _cols(nd, ncols, tdt, 72)
                 reps = 5
-                ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, L.QOB_LEFT, nd, nd, ncols, x, y, code,
-                                                             reps=reps))
+                with _Fp64Tensor(ctx, label):
+                    ms = _timed_graph(ctx, stream, _mul_recorder(ctx, h, L.QOB_LEFT, nd, nd, ncols, x, y, code,
+                                                                 reps=reps))
                 t = ms * 1e-3 / reps
                 s_ = 16 if npdt == np.complex128 else 8
                 out.append({"n": nd, "dtype": label, "kets": ncols, "us_per_call": t * 1e6,

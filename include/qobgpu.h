@@ -88,6 +88,15 @@ int qob_create(qob_ctx** ctx, int device, unsigned flags);
 int qob_destroy(qob_ctx* ctx);
 const char* qob_last_error(qob_ctx* ctx);
 
+/* Context options (no counterpart in the reference, whose BLAS picks its own
+ * kernels).  QOB_OPT_FP64_TENSOR, value 0 (default) or 1: ComplexF64 dense
+ * operators and mode products of dense LazyTensor factors whose contracted
+ * dimension is at least 64 run on the FP64 tensor cores (DMMA,
+ * mma.sync.m8n8k4.f64: four real products per complex 8 x 8 x 4 tile) instead
+ * of the FMA kernels; results agree to rounding (1e-15 relative). */
+#define QOB_OPT_FP64_TENSOR 1
+int qob_set_option(qob_ctx* ctx, int option, int64_t value);
+
 /* ---------------------------------------------------------------------------
  * Operator handles.  Data is copied from host memory at construction; child
  * handles may be freed after being used in a parent (the parent keeps its own

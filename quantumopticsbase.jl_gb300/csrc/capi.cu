@@ -111,7 +111,7 @@ void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, i
         xin = xs;
       }
       launch_dense(P.precision, d.a.p, d.m, d.n, cmul(alpha, coefval(d.coef, P.root)), xin, xes, xcs, b, y,
-                   yes, ycs, ncols, s, &ctx.ws, ws, P.ff);
+                   yes, ycs, ncols, s, &ctx.ws, ws, P.ff, ctx.fp64_tensor);
       b = one;
     }
     for (auto& mk : P.modek) {
@@ -143,12 +143,12 @@ void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, i
         }
         if (k + 1 == nst) {
           launch_modek(P.precision, st.a.p, st.eye, s1, st.dout, st.din, s3, ak, sin, ses, scs, b, y, yes,
-                       ycs, ncols, s, ffs);
+                       ycs, ncols, s, ffs, ctx.fp64_tensor);
         } else {
           const int64_t len = prod_range(next, 0, next.size());
           void* t = ctx.ws.get(ws + (k % 2), (size_t)len * ncols * esz);
           launch_modek(P.precision, st.a.p, st.eye, s1, st.dout, st.din, s3, ak, sin, ses, scs, zero, t, 1,
-                       len, ncols, s, ffs);
+                       len, ncols, s, ffs, ctx.fp64_tensor);
           src = t;
           ses = 1;
           scs = len;
@@ -703,6 +703,16 @@ int qob_debug_shift_slot(qob_ctx* ctx, qob_op* op, int side, int dtype, int col_
   });
 }
 #endif
+
+int qob_set_option(qob_ctx* ctx, int option, int64_t value) {
+  return guard(ctx, [&] {
+    if (!ctx) fail(QOB_ERR_ARG, "qob_set_option: bad arguments");
+    if (option == QOB_OPT_FP64_TENSOR)
+      ctx->c.fp64_tensor = value != 0;
+    else
+      fail(QOB_ERR_ARG, "qob_set_option: unknown option");
+  });
+}
 
 int qob_device_status(qob_ctx* ctx, void* stream, unsigned* flags) {
   return guard(ctx, [&] {

@@ -460,14 +460,18 @@ void dense_ff(const void* a, int64_t m, int64_t n, c128 alpha, const void* x, in
 
 void launch_dense(int precision, const void* a, int64_t m, int64_t n, c128 alpha, const void* x,
                   int64_t xes, int64_t xcs, c128 beta, void* y, int64_t yes, int64_t ycs,
-                  int64_t ncols, cudaStream_t s, Workspace* ws, int slot, bool ff) {
+                  int64_t ncols, cudaStream_t s, Workspace* ws, int slot, bool ff, bool dmma) {
   if (m == 0 || ncols == 0) return;
   const size_t esz = precision == QOB_C128 ? 16 : 8;
   if (ncols > 65535 * 8) {  // grid.y limit: split the vectors
     for (int64_t c0 = 0; c0 < ncols; c0 += 65535 * 8)
       launch_dense(precision, a, m, n, alpha, (const char*)x + c0 * xcs * esz, xes, xcs, beta,
                    (char*)y + c0 * ycs * esz, yes, ycs, std::min<int64_t>(65535 * 8, ncols - c0), s, ws, slot,
-                   ff);
+                   ff, dmma);
+    return;
+  }
+  if (dmma && !ff && precision == QOB_C128 && n >= kDmmaMinK) {
+    launch_dense_dmma(a, m, n, alpha, x, xes, xcs, beta, y, yes, ycs, ncols, s, ws, slot);
     return;
   }
   if (ff)
@@ -480,14 +484,18 @@ void launch_dense(int precision, const void* a, int64_t m, int64_t n, c128 alpha
 
 void launch_modek(int precision, const void* a, bool eye, int64_t s1, int64_t dout, int64_t din,
                   int64_t s3, c128 alpha, const void* x, int64_t xes, int64_t xcs, c128 beta,
-                  void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s, bool ff) {
+                  void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s, bool ff, bool dmma) {
   const int64_t len = s1 * dout * s3;
   if (len == 0 || ncols == 0) return;
+  if (dmma && !ff && !eye && precision == QOB_C128 && din >= kDmmaMinK) {
+    launch_modek_dmma(a, s1, dout, din, s3, alpha, x, xes, xcs, beta, y, yes, ycs, ncols, s);
+    return;
+  }
   const size_t esz = precision == QOB_C128 ? 16 : 8;
   if (ncols > 65535) {  // grid.y limit: split the vectors
     for (int64_t c0 = 0; c0 < ncols; c0 += 65535)
       launch_modek(precision, a, eye, s1, dout, din, s3, alpha, (const char*)x + c0 * xcs * esz, xes, xcs,
-                   beta, (char*)y + c0 * ycs * esz, yes, ycs, std::min<int64_t>(65535, ncols - c0), s, ff);
+                   beta, (char*)y + c0 * ycs * esz, yes, ycs, std::min<int64_t>(65535, ncols - c0), s, ff, dmma);
     return;
   }
   dim3 grid(blocks_for(len, 256), (unsigned)ncols);

@@ -368,6 +368,9 @@ struct Context {
   static constexpr int kTickets = 16;
   cudaEvent_t ticket_done[kTickets] = {};
   uint64_t host_calls = 0;
+  // QOB_OPT_FP64_TENSOR: ComplexF64 dense and mode-product passes whose
+  // contracted dimension is >= kDmmaMinK run on the FP64 tensor cores
+  bool fp64_tensor = false;
   // device status word (one unsigned, zeroed at creation): kernels record
   // bounded waits that gave up and failed debug checks; read by qob_device_status
   DeviceBuf status;
@@ -414,13 +417,24 @@ void launch_scale(int precision, void* y, int64_t rows, int64_t cols, int64_t ld
 // ff: double-float form (a: (hi, lo) quadruples, x split by launch_ff_split)
 void launch_dense(int precision, const void* a, int64_t m, int64_t n, c128 alpha, const void* x,
                   int64_t xes, int64_t xcs, c128 beta, void* y, int64_t yes, int64_t ycs,
-                  int64_t ncols, cudaStream_t s, Workspace* ws = nullptr, int slot = 0, bool ff = false);
+                  int64_t ncols, cudaStream_t s, Workspace* ws = nullptr, int slot = 0, bool ff = false,
+                  bool dmma = false);
+// The same on the FP64 tensor cores (k_dmma.cu; ComplexF64 only).
+void launch_dense_dmma(const void* a, int64_t m, int64_t n, c128 alpha, const void* x, int64_t xes, int64_t xcs,
+                       c128 beta, void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s, Workspace* ws,
+                       int slot);
+void launch_modek_dmma(const void* A, int64_t s1, int64_t dout, int64_t din, int64_t s3, c128 alpha, const void* x,
+                       int64_t xes, int64_t xcs, c128 beta, void* y, int64_t yes, int64_t ycs, int64_t ncols,
+                       cudaStream_t s);
+// contracted dimension from which the FP64 tensor-core option applies
+constexpr int64_t kDmmaMinK = 64;
 // Split of ncols vectors of n ComplexF64 elements (element stride es, vector
 // stride cs) into double-float quadruples at the same offsets of out.
 void launch_ff_split(const void* x, int64_t n, int64_t ncols, int64_t es, int64_t cs, void* out, cudaStream_t s);
 void launch_modek(int precision, const void* a, bool eye, int64_t s1, int64_t dout, int64_t din,
                   int64_t s3, c128 alpha, const void* x, int64_t xes, int64_t xcs, c128 beta,
-                  void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s, bool ff = false);
+                  void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s, bool ff = false,
+                  bool dmma = false);
 void launch_axpby(int precision, const void* x, int64_t xes, int64_t xcs, c128 alpha, void* y,
                   int64_t yes, int64_t ycs, c128 beta, int64_t len, int64_t ncols,
                   cudaStream_t s);

@@ -27,6 +27,7 @@ QOB_ERR_CANCELLED = 9
 QOB_C128 = 0
 QOB_C64 = 1
 QOB_C128X = 2  # ComplexF64 data, fused part in double-float arithmetic
+QOB_OPT_FP64_TENSOR = 1
 QOB_LEFT = 0
 QOB_RIGHT = 1
 
@@ -45,6 +46,7 @@ SIGNATURES = {
     "qob_destroy": (I, [VP]),
     "qob_last_error": (C.c_char_p, [VP]),
     "qob_probe_peak": (I, [VP, I, DP]),
+    "qob_set_option": (I, [VP, I, I64]),
     "qob_op_sparse": (I, [VP, I64, I64, I64P, I64P, VP, I, I, C.POINTER(VP)]),
     "qob_op_dense": (I, [VP, I64, I64, VP, I64, I, I, C.POINTER(VP)]),
     "qob_op_eye": (I, [VP, I64, I64, C.POINTER(VP)]),
