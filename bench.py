@@ -79,6 +79,9 @@ def parse():
     p.add_argument("--suite", action="store_true", help="secondary workloads, one JSON line each")
     p.add_argument("--only", nargs="*", default=None, help="with --suite: these workloads only")
     p.add_argument("--probe", action="store_true", help="print the device's measured FP64 / FP32 FMA rates")
+    p.add_argument("--pdl", type=int, default=0, choices=[0, 1],
+                   help="time every form with programmatic dependent launch (QOB_OPT_PDL) on; the other setting "
+                        "is timed beside it in the pdl sub-object")
     p.add_argument("--no-secondary", action="store_true",
                    help="leave out the batched and served sub-objects (used for ncu captures)")
     return p.parse_args()
@@ -419,6 +422,7 @@ def run_own(args, rank, world, local_rank):
     else:
         tuning = {"c128": tune(np.complex128), "c64": tune(np.complex64), "c128x": tune("ff")}
     K, W = args.steps, max(3, args.warmup)
+    raise_for(lib.qob_set_option(ctx.ptr, L.QOB_OPT_PDL, args.pdl), ctx)
     ms64, launches64, win64, _ = timed(torch.complex128, dtype_code(np.complex128), K, W)
     stats64 = step_stats(torch.complex128, dtype_code(np.complex128))
     value = whole_job_rate(BATCH * K, world, ms64 / 1e3)
@@ -429,6 +433,16 @@ def run_own(args, rank, world, local_rank):
     # ComplexF64 data in double-float arithmetic on the FP32 pipes (QOB_C128X)
     msff, launchesff, _, _ = timed(torch.complex128, L.QOB_C128X, K, W)
     valueff = whole_job_rate(BATCH * K, world, msff / 1e3)
+    # the other launch setting, for comparison
+    raise_for(lib.qob_set_option(ctx.ptr, L.QOB_OPT_PDL, 1 - args.pdl), ctx)
+    pdl_other = {f"{k}_ms_per_step": timed(tdt, code, K, W)[0] / K
+                 for k, tdt, code in (("c128", torch.complex128, dtype_code(np.complex128)),
+                                      ("c64", torch.complex64, dtype_code(np.complex64)),
+                                      ("c128x", torch.complex128, L.QOB_C128X))}
+    raise_for(lib.qob_set_option(ctx.ptr, L.QOB_OPT_PDL, args.pdl), ctx)
+    pdl_info = {"headline_pdl": bool(args.pdl), "other_setting": pdl_other,
+                "note": "programmatic dependent launch (QOB_OPT_PDL): each step's blocks are scheduled while the "
+                        "previous step finishes; other_setting = the same steps timed with the opposite setting"}
     errs = oracle_errors(lib, ctx, hd, H, dim, stream) if rank == 0 else None
 
     # end to end through the host-buffer C call with pinned host memory
@@ -496,6 +510,7 @@ def run_own(args, rank, world, local_rank):
                             "one split launch + one gather launch per step (QOB_C128X)"},
         "oracle_check": "each form's result on one 64-ket batch of this workload (same qob_mul call, tuned "
                         "shape) against the oracle (restated reference mul!, host threads, ComplexF64 inputs)",
+        "pdl": pdl_info,
         "batched": batched,
         "served": served,
         "peaks_live": peaks_live,

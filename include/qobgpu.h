@@ -95,6 +95,19 @@ const char* qob_last_error(qob_ctx* ctx);
  * mma.sync.m8n8k4.f64: four real products per complex 8 x 8 x 4 tile) instead
  * of the FMA kernels; results agree to rounding (1e-15 relative). */
 #define QOB_OPT_FP64_TENSOR 1
+/* QOB_OPT_PDL, value 0 (default) or 1: the fused gather kernels are launched
+ * with programmatic dependent launch, so that an application's blocks are
+ * scheduled while the previous kernel on the stream finishes (each waits for
+ * that kernel's completion before it touches memory).  Shortens back-to-back
+ * applications, e.g. replayed steps. */
+#define QOB_OPT_PDL 2
+/* QOB_OPT_FP32_TENSOR, value 0 (default) or 1: ComplexF32 dense operators whose
+ * sides are both at least 64 run on the 5th-generation tensor cores
+ * (tcgen05.mma kind::tf32 with the accumulator in tensor memory, operand tiles
+ * loaded by TMA) with every operand split into a TF32 head and tail and three
+ * products per tile, which keeps FP32 accuracy (relative error ~1e-7); a real
+ * copy of the matrix (the same size as the complex one) is built on first use. */
+#define QOB_OPT_FP32_TENSOR 3
 int qob_set_option(qob_ctx* ctx, int option, int64_t value);
 
 /* ---------------------------------------------------------------------------

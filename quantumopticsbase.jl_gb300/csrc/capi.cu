@@ -98,7 +98,7 @@ void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, i
       void* ffx = P.gather->ff
                       ? ctx.ws.get(ws, (size_t)((P.n - 1) * xes + (ncols - 1) * xcs + 1) * 16)
                       : nullptr;
-      launch_gather(*P.gather, P.precision, x, xes, xcs, y, yes, ycs, ncols, alpha, b, s, P.n, ffx);
+      launch_gather(*P.gather, P.precision, x, xes, xcs, y, yes, ycs, ncols, alpha, b, s, P.n, ffx, ctx.pdl);
       b = one;
     }
     for (auto& d : P.dense) {
@@ -110,8 +110,15 @@ void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, i
         launch_ff_split(x, P.n, ncols, xes, xcs, xs, s);
         xin = xs;
       }
-      launch_dense(P.precision, d.a.p, d.m, d.n, cmul(alpha, coefval(d.coef, P.root)), xin, xes, xcs, b, y,
-                   yes, ycs, ncols, s, &ctx.ws, ws, P.ff, ctx.fp64_tensor);
+      const c128 ad = cmul(alpha, coefval(d.coef, P.root));
+      if (ctx.fp32_tensor && P.precision == QOB_C64 && !P.ff && d.m >= kDmmaMinK && d.n >= kDmmaMinK) {
+        if (!d.tc.ready) tc_dense_build(d.tc, d.a.p, d.m, d.n, s);
+        launch_dense_tc(d.tc, ad, xin, xes, xcs, b, y, yes, ycs, ncols, s, &ctx.ws, ws,
+                        static_cast<unsigned*>(ctx.status.p), ctx.num_sms);
+      } else {
+        launch_dense(P.precision, d.a.p, d.m, d.n, ad, xin, xes, xcs, b, y, yes, ycs, ncols, s, &ctx.ws, ws, P.ff,
+                     ctx.fp64_tensor);
+      }
       b = one;
     }
     for (auto& mk : P.modek) {
@@ -709,6 +716,10 @@ int qob_set_option(qob_ctx* ctx, int option, int64_t value) {
     if (!ctx) fail(QOB_ERR_ARG, "qob_set_option: bad arguments");
     if (option == QOB_OPT_FP64_TENSOR)
       ctx->c.fp64_tensor = value != 0;
+    else if (option == QOB_OPT_PDL)
+      ctx->c.pdl = value != 0;
+    else if (option == QOB_OPT_FP32_TENSOR)
+      ctx->c.fp32_tensor = value != 0;
     else
       fail(QOB_ERR_ARG, "qob_set_option: unknown option");
   });

@@ -238,8 +238,9 @@ void launch_ff_split(const void* x, int64_t n, int64_t ncols, int64_t es, int64_
 
 void launch_gather(const GatherPlan& g, int precision, const void* x, int64_t xes, int64_t xcs,
                    void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta,
-                   cudaStream_t s, int64_t n, void* ff_x) {
+                   cudaStream_t s, int64_t n, void* ff_x, bool pdl) {
   GatherView v = g.view();
+  v.pdl = pdl ? 1 : 0;
   const int tc = gather_tile(g, ncols);
   if (g.ff) {
     // split x once; the gather then reads the quadruples with x's strides

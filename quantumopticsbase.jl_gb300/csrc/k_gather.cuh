@@ -37,6 +37,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <utility>
 
 #include "qob_internal.h"
 
@@ -188,6 +189,38 @@ __device__ __forceinline__ bool nz(float4 v) {
   return ((__float_as_uint(v.x) | __float_as_uint(v.y) | __float_as_uint(v.z) | __float_as_uint(v.w)) << 1) != 0u;
 }
 
+// Programmatic dependent launch: a gather launched with the programmatic
+// stream-serialization attribute may start while the previous kernel of the
+// stream finishes; it waits here, before its first access to memory, until that
+// kernel has completed and its writes are visible, and lets the next such
+// launch start in turn.  Without the attribute both are no-ops.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// A launch with the programmatic stream-serialization attribute when pdl is set
+// (the kernels call pdl_enter first), else an ordinary one.
+template <typename... KArgs, typename... Args>
+void launch_kernel(bool pdl, void (*kernel)(KArgs...), dim3 grid, unsigned threads, size_t smem, cudaStream_t s,
+                   Args&&... args) {
+  if (!pdl) {
+    kernel<<<grid, threads, smem, s>>>(std::forward<Args>(args)...);
+    return;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  QOB_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
+}
+
 // FP64 accumulator: plain fused multiply-adds.
 struct AccD {
   double re, im;
@@ -220,24 +253,33 @@ struct AccD {
 };
 
 // FP32 accumulator with Kahan compensation (Kahan 1965): c carries the
-// low-order part lost by each addition.
+// low-order part lost by each addition.  The term is formed with the
+// compensation folded in, y = fma(v, x, -c) (one rounding), so a real
+// multiply-add costs four FP32 operations: y, s = acc + y, c = (s - acc) - y.
 struct AccF {
   float re, im, cre, cim;
   __device__ void zero() { re = im = cre = cim = 0.f; }
-  __device__ void add(float tr, float ti) {
-    float yr = tr - cre;
-    float sr = re + yr;
-    cre = (sr - re) - yr;
-    re = sr;
-    float yi = ti - cim;
-    float si = im + yi;
-    cim = (si - im) - yi;
-    im = si;
+  // acc += y where y already holds term - c
+  __device__ __forceinline__ void step(float& a, float& c, float y) {
+    const float s = a + y;
+    c = (s - a) - y;
+    a = s;
   }
-  __device__ void mac(float v, float2 x) { add(v * x.x, v * x.y); }
-  __device__ void mac_i(float v, float2 x) { add(-v * x.y, v * x.x); }
+  __device__ void add(float tr, float ti) {
+    step(re, cre, tr - cre);
+    step(im, cim, ti - cim);
+  }
+  __device__ void mac(float v, float2 x) {
+    step(re, cre, __fmaf_rn(v, x.x, -cre));
+    step(im, cim, __fmaf_rn(v, x.y, -cim));
+  }
+  __device__ void mac_i(float v, float2 x) {
+    step(re, cre, __fmaf_rn(-v, x.y, -cre));
+    step(im, cim, __fmaf_rn(v, x.x, -cim));
+  }
   __device__ void mac(float2 v, float2 x) {
-    add(__fmaf_rn(v.x, x.x, -v.y * x.y), __fmaf_rn(v.x, x.y, v.y * x.x));
+    step(re, cre, __fmaf_rn(v.x, x.x, __fmaf_rn(-v.y, x.y, -cre)));
+    step(im, cim, __fmaf_rn(v.x, x.y, __fmaf_rn(v.y, x.x, -cim)));
   }
   __device__ void mac_i(float2 v, float2 x) { mac(make_float2(-v.y, v.x), x); }
   __device__ void set(float v, float2 x) {
@@ -685,6 +727,7 @@ __global__ void __launch_bounds__(256) k_gather_j(GatherView g, SiteTable st,
   using AT = typename AccOf<R>::T;
   using ET = typename Ell<R, VM != kComplex>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  pdl_enter();
   const ET* ell = stage<ET>(smem_raw, g);
   const GGroup* sg = reinterpret_cast<const GGroup*>(smem_raw);
   // lane split ls: a warp covers 32/ls consecutive output indices and ls
@@ -733,6 +776,7 @@ __global__ void __launch_bounds__(256) k_gather_p(GatherView g, SiteTable st,
   using AT = typename AccOf<R>::T;
   using ET = typename Ell<R, VM != kComplex>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  pdl_enter();
   const ET* ell = stage<ET>(smem_raw, g);
   const GGroup* sg = reinterpret_cast<const GGroup*>(smem_raw);
   // chunks of (32/ls output indices x ls sets of TC vectors), one per warp at a
@@ -780,6 +824,7 @@ __global__ void __launch_bounds__(256) k_gather_c(GatherView g, SiteTable st,
   using AT = typename AccOf<R>::T;
   using ET = typename Ell<R, VM != kComplex>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  pdl_enter();
   const ET* ell = stage<ET>(smem_raw, g);
   const GGroup* sg = reinterpret_cast<const GGroup*>(smem_raw);
   const int64_t J = blockIdx.x;
@@ -837,7 +882,8 @@ void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t x
       w.lane_split = ls;
       const int64_t jw = 32 / ls;
       w.jmul = chunk_multiplier((v.m + jw - 1) / jw);
-      pk<<<(unsigned)(sms * occ), threads, smem, s>>>(w, st, (const XT*)x, xcs, (CT*)y, ycs, (int)ncols, a, b);
+      launch_kernel(v.pdl != 0, pk, dim3((unsigned)(sms * occ)), (unsigned)threads, smem, s, w, st, (const XT*)x,
+                    xcs, (CT*)y, ycs, (int)ncols, a, b);
       QOB_LAUNCHED();
       return;
     }
@@ -856,8 +902,8 @@ void launch_j(const GatherView& v, const SiteTable& st, const void* x, int64_t x
   const int64_t per_y = (int64_t)TC * ls;  // vectors per grid row
   for (int64_t c0 = 0; c0 < ncols; c0 += (int64_t)65535 * per_y) {  // grid.y limit
     const int64_t nc = std::min<int64_t>(ncols - c0, (int64_t)65535 * per_y);
-    kern<<<dim3(gx, (unsigned)((nc + per_y - 1) / per_y)), threads, smem, s>>>(
-        w, st, (const XT*)x + c0 * xcs, xcs, (CT*)y + c0 * ycs, ycs, (int)nc, a, b);
+    launch_kernel(v.pdl != 0, kern, dim3(gx, (unsigned)((nc + per_y - 1) / per_y)), (unsigned)threads, smem, s, w,
+                  st, (const XT*)x + c0 * xcs, xcs, (CT*)y + c0 * ycs, ycs, (int)nc, a, b);
     QOB_LAUNCHED();
   }
 }

@@ -1,0 +1,453 @@
+// k_tc32.cu -- ComplexF32 dense operator times vectors on the 5th-generation
+// tensor cores (tcgen05.mma kind::tf32, accumulator in tensor memory, operand
+// tiles brought in by TMA), for mul! on a DenseOperator
+// (src/operators_dense.jl:394-396, BLAS cgemm in the reference).
+//
+// The complex product is one real GEMM.  The operator is stored (at plan
+// compile time) as the real matrix Ahat of 2m rows, K-major: row 2i holds
+// Re A[i, :], row 2i + 1 holds Im A[i, :] (row length ldk = n rounded up to 32,
+// zero padded).  The vectors are split per call (k_tc_split_b) into Bhat of 2N
+// rows, K-major: row j < N holds Re X[:, j], row N + j holds Im X[:, j].  Then
+// D = Ahat Bhat^T (2m x 2N, FP32 in tensor memory) gives
+//   Re Y[i, c] = D[2i, c] - D[2i+1, N+c],   Im Y[i, c] = D[2i+1, c] + D[2i, N+c]
+// (in the kernel the imaginary rows of Bhat start at BN / 2, BN = the tile's
+// column count, so N above stands for BN / 2).
+// TF32 keeps 10 explicit mantissa bits; to reach FP32 accuracy each operand is
+// split into a TF32 head and a TF32 tail (x = hi + lo, |lo| <= 2^-11 |x|) and
+// D = Ahi Bhi + Ahi Blo + Alo Bhi (three MMAs per k step; the dropped Alo Blo is
+// below 2^-22 of the product), the split of Ahat done in shared memory as its
+// tiles arrive, the split of Bhat once per call.
+//
+// Block (192 threads): warp 0 issues the TMA loads (a 4-, 3- or 2-stage ring
+// of 128 x 32 Ahat tiles and BN x 32 Bhat head / tail tiles, 128-byte
+// swizzle); warps 2-5 split each Ahat tile into head (in place) and tail, then
+// run the epilogue; warp 1 owns the tensor memory and one of its threads
+// issues the MMAs (M = 128 rows, N = BN = 2 x kets, K = 8 per instruction).
+// Blocks cover 64 complex rows each and, when that leaves SMs idle, a range of
+// k blocks whose partial products k_tc_reduce adds in order.  Every wait is
+// bounded: a wait that gives up records kTcErrTimeout in the status word, the
+// block drains its copies and MMAs, frees its tensor memory and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "qob_internal.h"
+
+namespace qob {
+
+namespace {
+
+constexpr int kTcBM = 128;     // rows of Ahat per block (64 complex rows)
+constexpr int kTcBK = 32;      // floats per k block: one 128-byte swizzle span
+constexpr int kTcThreads = 192;
+constexpr unsigned kTcErrTimeout = 1u;
+constexpr int kTcPolls = 1 << 21;
+
+__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void bar_init(uint64_t* b, unsigned n) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(n) : "memory");
+}
+__device__ __forceinline__ void bar_expect(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(b)) : "memory");
+}
+__device__ __forceinline__ bool bar_test(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(saddr(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool bar_wait(uint64_t* b, uint32_t parity) {
+  for (int i = 0; i < kTcPolls; ++i) {
+    if (bar_test(b, parity)) return true;
+    if (i > 64) __nanosleep(32);
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_2d(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* b) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(saddr(dst)),
+      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(saddr(b))
+      : "memory");
+}
+// Shared-memory matrix descriptor of a K-major tile with the 128-byte swizzle:
+// start address, stride between 8-row groups 1024 bytes, descriptor version 1.
+__device__ __forceinline__ uint64_t sw128_desc(const void* tile) {
+  const uint64_t a = (saddr(tile) & 0x3FFFFu) >> 4;
+  return a | (uint64_t(1) << 16) | (uint64_t(1024 >> 4) << 32) | (uint64_t(1) << 46) | (uint64_t(2) << 61);
+}
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* b) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(b))
+               : "memory");
+}
+__device__ __forceinline__ float tf32_rn(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+// 16 consecutive accumulator columns of this warp's 32 lanes
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+      "[%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <int BN>
+struct TcCfg {
+  static constexpr int kStages = BN <= 64 ? 4 : (BN <= 128 ? 3 : 2);
+  static constexpr int kATile = kTcBM * kTcBK * 4;  // 16 KB
+  static constexpr int kBTile = BN * kTcBK * 4;
+  static constexpr int kStage = 2 * kATile + 2 * kBTile;  // A head (in place), A tail, B head, B tail
+  static constexpr int kTmemCols = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
+  static constexpr size_t kSmem = 1024 /* alignment */ + (size_t)kStages * kStage + 256 /* barriers */;
+};
+
+// Y[i, c] (complex rows i < m, kets c < N) = alpha * (Ahat Bhat^T combined) + beta * Y,
+// or the block's partial product into part[kz][c][i] when part != null.
+template <int BN>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_tc_cgemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmBh,
+               const __grid_constant__ CUtensorMap tmBl, int64_t m, int N, int nkb, int kb_per, float2* y, int64_t yes,
+               int64_t ycs, float2 alpha, float2 beta, float2* part, unsigned* status) {
+  using C = TcCfg<BN>;
+  constexpr int S = C::kStages;
+  extern __shared__ __align__(16) unsigned char tc_smem_raw[];
+  unsigned char* base = (unsigned char*)(((uintptr_t)tc_smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + (size_t)S * C::kStage);
+  uint64_t* full = bars;           // TMA landed          (count 1 + tx)
+  uint64_t* conv = bars + S;       // A split done        (count 128)
+  uint64_t* empty = bars + 2 * S;  // MMAs read the stage (count 1, tcgen05.commit)
+  uint64_t* accf = bars + 3 * S;   // all MMAs complete
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3 * S + 1);
+  int* abort_flag = reinterpret_cast<int*>(bars + 3 * S + 2);
+  auto stageA = [&](int s) { return base + (size_t)s * C::kStage; };
+  auto stageAl = [&](int s) { return base + (size_t)s * C::kStage + C::kATile; };
+  auto stageBh = [&](int s) { return base + (size_t)s * C::kStage + 2 * C::kATile; };
+  auto stageBl = [&](int s) { return base + (size_t)s * C::kStage + 2 * C::kATile + C::kBTile; };
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int kb0 = blockIdx.y * kb_per;
+  const int nk = min(nkb - kb0, kb_per);  // >= 1 (the host makes no empty ranges)
+  const int row0 = blockIdx.x * kTcBM;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      bar_init(&full[s], 1);
+      bar_init(&conv[s], 128);
+      bar_init(&empty[s], 1);
+    }
+    bar_init(accf, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(tmem_slot)),
+                 "r"(C::kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {  // producer
+      int issued = 0;
+      for (int it = 0; it < nk; ++it) {
+        const int s = it % S;
+        if (it >= S && !bar_wait(&empty[s], ((it / S) - 1) & 1)) {
+          atomicExch(abort_flag, 1);
+          break;
+        }
+        if (*(volatile int*)abort_flag) break;
+        bar_expect(&full[s], 2 * C::kBTile + C::kATile);
+        const int kc = (kb0 + it) * kTcBK;
+        tma_2d(stageA(s), &tmA, kc, row0, &full[s]);
+        tma_2d(stageBh(s), &tmBh, kc, 0, &full[s]);
+        tma_2d(stageBl(s), &tmBl, kc, 0, &full[s]);
+        issued = it + 1;
+      }
+      // every copy issued has landed before the block's shared memory goes away
+      for (int it = max(0, issued - S); it < issued; ++it) bar_wait(&full[it % S], (it / S) & 1);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      // kind::tf32, FP32 accumulator, A and B K-major, N = BN, M = 128
+      const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kTcBM >> 4) << 24);
+      for (int it = 0; it < nk; ++it) {
+        const int s = it % S;
+        if (!bar_wait(&conv[s], (it / S) & 1)) {
+          atomicExch(abort_flag, 1);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint64_t ah = sw128_desc(stageA(s)), al = sw128_desc(stageAl(s));
+        const uint64_t bh = sw128_desc(stageBh(s)), bl = sw128_desc(stageBl(s));
+#pragma unroll
+        for (int kk = 0; kk < kTcBK / 8; ++kk) {  // 8 TF32 = 32 bytes = 2 descriptor units per step
+          const uint64_t o = (uint64_t)(2 * kk);
+          mma_tf32(tmem, ah + o, bh + o, idesc, (it > 0 || kk > 0) ? 1u : 0u);
+          mma_tf32(tmem, ah + o, bl + o, idesc, 1u);
+          mma_tf32(tmem, al + o, bh + o, idesc, 1u);
+        }
+        mma_commit(&empty[s]);
+      }
+      mma_commit(accf);  // fires when every MMA issued above has completed
+    }
+  } else {
+    // warps 2-5: split each A tile into head (in place) and tail
+    const int ct = threadIdx.x - 64;
+    bool ok = true;
+    for (int it = 0; it < nk; ++it) {
+      const int s = it % S;
+      if (*(volatile int*)abort_flag || !bar_wait(&full[s], (it / S) & 1)) {
+        atomicExch(abort_flag, 1);
+        ok = false;
+        break;
+      }
+      float4* a = reinterpret_cast<float4*>(stageA(s));
+      float4* al = reinterpret_cast<float4*>(stageAl(s));
+#pragma unroll
+      for (int q = 0; q < C::kATile / 16 / 128; ++q) {
+        const int idx = ct + 128 * q;
+        const float4 v = a[idx];
+        float4 h, l;
+        h.x = tf32_rn(v.x);
+        h.y = tf32_rn(v.y);
+        h.z = tf32_rn(v.z);
+        h.w = tf32_rn(v.w);
+        l.x = tf32_rn(v.x - h.x);
+        l.y = tf32_rn(v.y - h.y);
+        l.z = tf32_rn(v.z - h.z);
+        l.w = tf32_rn(v.w - h.w);
+        a[idx] = h;
+        al[idx] = l;
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      bar_arrive(&conv[s]);
+    }
+    // epilogue: this warp reads tensor-memory lanes 32 * (warp % 4) ...
+    // the tensor-memory loads below are warp-wide: decide per warp
+    const bool done = __all_sync(0xffffffffu, bar_wait(accf, 0) && ok && !*(volatile int*)abort_flag);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!done) {
+      if (lane == 0 && status) atomicOr(status, kTcErrTimeout);
+    } else {
+      const int q4 = warp & 3;
+      const int r = q4 * 32 + lane;  // accumulator row = Ahat row row0 + r
+      const int64_t i = (int64_t)(row0 + r) >> 1;
+      const bool even = (lane & 1) == 0;
+      const uint32_t lane_addr = tmem + ((uint32_t)(q4 * 32) << 16);
+      for (int c0 = 0; c0 < N; c0 += 16) {
+        float d[16], e[16];
+        tmem_ld16(lane_addr + (uint32_t)c0, d);        // columns c0 .. c0 + 15: real parts of the kets
+        tmem_ld16(lane_addr + (uint32_t)(BN / 2 + c0), e);  // columns BN/2 + c0 ..: imaginary parts
+#pragma unroll
+        for (int t = 0; t < 16; ++t) {
+          const float other = __shfl_xor_sync(0xffffffffu, e[t], 1);
+          const float v = even ? d[t] - other : d[t] + other;  // even lane: Re Y, odd lane: Im Y
+          const float w = __shfl_xor_sync(0xffffffffu, v, 1);
+          const int c = c0 + t;
+          if (even && i < m && c < N) {
+            if (part) {
+              part[((int64_t)blockIdx.y * N + c) * m + i] = make_float2(v, w);
+            } else {
+              float2* yp = y + i * yes + (int64_t)c * ycs;
+              float re = alpha.x * v - alpha.y * w;
+              float im = alpha.x * w + alpha.y * v;
+              if (beta.x != 0.f || beta.y != 0.f) {
+                const float2 o = *yp;
+                re = __fmaf_rn(beta.x, o.x, __fmaf_rn(-beta.y, o.y, re));
+                im = __fmaf_rn(beta.x, o.y, __fmaf_rn(beta.y, o.x, im));
+              }
+              *yp = make_float2(re, im);
+            }
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::kTmemCols) : "memory");
+  }
+}
+
+// Bhat head and tail: row j = Re X[:, j], row H + j = Im X[:, j] (j < the
+// kets, H = half the tile's columns), TF32-split, K-major with row length ldk
+// (zero beyond n).
+__global__ void k_tc_split_b(const float2* __restrict__ x, int64_t n, int64_t xes, int64_t xcs, int H, int64_t ldk,
+                             float* __restrict__ bh, float* __restrict__ bl) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (k >= ldk) return;
+  float2 v = make_float2(0.f, 0.f);
+  if (k < n) v = x[k * xes + (int64_t)j * xcs];
+  const float hr = tf32_rn(v.x), hi = tf32_rn(v.y);
+  bh[(int64_t)j * ldk + k] = hr;
+  bl[(int64_t)j * ldk + k] = tf32_rn(v.x - hr);
+  bh[(int64_t)(H + j) * ldk + k] = hi;
+  bl[(int64_t)(H + j) * ldk + k] = tf32_rn(v.y - hi);
+}
+
+// y[i, c] = alpha * (sum of the k ranges' partial products, in order) + beta * y[i, c]
+__global__ void k_tc_reduce(const float2* __restrict__ part, int kchunks, int64_t m, int N, float2* __restrict__ y,
+                            int64_t yes, int64_t ycs, float2 alpha, float2 beta) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (i >= m) return;
+  float sr = 0.f, si = 0.f;
+  for (int z = 0; z < kchunks; ++z) {
+    const float2 p = part[((int64_t)z * N + c) * m + i];
+    sr += p.x;
+    si += p.y;
+  }
+  float2* yp = y + i * yes + (int64_t)c * ycs;
+  float re = alpha.x * sr - alpha.y * si;
+  float im = alpha.x * si + alpha.y * sr;
+  if (beta.x != 0.f || beta.y != 0.f) {
+    const float2 o = *yp;
+    re = __fmaf_rn(beta.x, o.x, __fmaf_rn(-beta.y, o.y, re));
+    im = __fmaf_rn(beta.x, o.y, __fmaf_rn(beta.y, o.x, im));
+  }
+  *yp = make_float2(re, im);
+}
+
+// cuTensorMapEncodeTiled from the driver, looked up once.
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    cudaGetLastError();
+  });
+  if (!fn) fail(QOB_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  return fn;
+}
+
+// rows x ldk FP32, K-major, boxes of box_rows x 32 with the 128-byte swizzle
+CUtensorMap kmajor_map(const void* p, int64_t rows, int64_t ldk, int box_rows) {
+  CUtensorMap m;
+  const cuuint64_t dims[2] = {(cuuint64_t)ldk, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ldk * 4};
+  const cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
+  const cuuint32_t es[2] = {1, 1};
+  const CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(p), dims, strides, box, es,
+                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) fail(QOB_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+  return m;
+}
+
+template <int BN>
+void run_tc(const TcDense& d, int64_t n, const float2* x, int64_t xes, int64_t xcs, int N, float2* y, int64_t yes,
+            int64_t ycs, float2 alpha, float2 beta, Workspace* ws, int slot, cudaStream_t s, unsigned* status,
+            int num_sms) {
+  using C = TcCfg<BN>;
+  const int64_t ldk = d.ldk;
+  // split vectors: head and tail of Bhat, BN rows each (rows N .. BN/2 unused when N < BN/2)
+  const size_t bbytes = (size_t)BN * ldk * 4;
+  char* w = static_cast<char*>(ws->get(slot, 2 * bbytes + 256));
+  float* bh = reinterpret_cast<float*>(w);
+  float* bl = reinterpret_cast<float*>(w + bbytes);
+  if (N < BN / 2) QOB_CUDA(cudaMemsetAsync(w, 0, 2 * bbytes, s));
+  k_tc_split_b<<<dim3((unsigned)((ldk + 255) / 256), (unsigned)N), 256, 0, s>>>(x, n, xes, xcs, BN / 2, ldk, bh, bl);
+  QOB_LAUNCHED();
+  const CUtensorMap mb_h = kmajor_map(bh, BN, ldk, BN), mb_l = kmajor_map(bl, BN, ldk, BN);
+  const int nkb = (int)(ldk / kTcBK);
+  const int mt = (int)((2 * d.m + kTcBM - 1) / kTcBM);
+  // k ranges so that the blocks cover the SMs (each range at least 8 k blocks)
+  int kchunks = std::max(1, std::min((num_sms + mt - 1) / mt, nkb / 8));
+  const int kb_per = (nkb + kchunks - 1) / kchunks;
+  kchunks = (nkb + kb_per - 1) / kb_per;
+  float2* part = nullptr;
+  if (kchunks > 1) part = static_cast<float2*>(ws->get(slot + 1, (size_t)kchunks * N * d.m * sizeof(float2)));
+  auto kern = k_tc_cgemm<BN>;
+  QOB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::kSmem));
+  kern<<<dim3((unsigned)mt, (unsigned)kchunks), kTcThreads, C::kSmem, s>>>(d.map, mb_h, mb_l, d.m, N, nkb, kb_per, y,
+                                                                         yes, ycs, alpha, beta, part, status);
+  QOB_LAUNCHED();
+  if (part) {
+    k_tc_reduce<<<dim3((unsigned)((d.m + 127) / 128), (unsigned)N), 128, 0, s>>>(part, kchunks, d.m, N, y, yes, ycs,
+                                                                                alpha, beta);
+    QOB_LAUNCHED();
+  }
+}
+
+// Ahat of the stored ComplexF32 matrix (column-major m x n, on the device),
+// built once on first use: row 2i = Re A[i, :], row 2i + 1 = Im A[i, :].
+__global__ void k_tc_build_ahat(const float2* __restrict__ a, int64_t m, int64_t n, int64_t ldk, float* __restrict__ ah) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // complex row
+  const int64_t k = blockIdx.y;
+  if (i >= m || k >= ldk) return;
+  const float2 v = k < n ? a[i + k * m] : make_float2(0.f, 0.f);
+  ah[(2 * i) * ldk + k] = v.x;
+  ah[(2 * i + 1) * ldk + k] = v.y;
+}
+
+}  // namespace
+
+void tc_dense_build(TcDense& d, const void* a, int64_t m, int64_t n, cudaStream_t s) {
+  d.m = m;
+  d.n = n;
+  d.ldk = (n + kTcBK - 1) / kTcBK * kTcBK;
+  if (d.ldk > 65535) fail(QOB_ERR_UNSUPPORTED, "tensor-core dense path: more than 65535 columns");
+  d.ahat.alloc((size_t)2 * m * d.ldk * sizeof(float));
+  k_tc_build_ahat<<<dim3((unsigned)((m + 127) / 128), (unsigned)d.ldk), 128, 0, s>>>(
+      static_cast<const float2*>(a), m, n, d.ldk, static_cast<float*>(d.ahat.p));
+  QOB_LAUNCHED();
+  d.map = kmajor_map(d.ahat.p, 2 * m, d.ldk, kTcBM);
+  d.ready = true;
+}
+
+bool launch_dense_tc(const TcDense& d, c128 alpha, const void* x, int64_t xes, int64_t xcs, c128 beta, void* y,
+                     int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s, Workspace* ws, int slot,
+                     unsigned* status, int num_sms) {
+  if (!d.ready || ncols < 1) return false;
+  const float2 a = make_float2((float)alpha.re, (float)alpha.im), b = make_float2((float)beta.re, (float)beta.im);
+  for (int64_t c0 = 0; c0 < ncols; c0 += 64) {  // up to 64 kets per pass (BN = 128 columns)
+    const int N = (int)std::min<int64_t>(64, ncols - c0);
+    const float2* xc = static_cast<const float2*>(x) + c0 * xcs;
+    float2* yc = static_cast<float2*>(y) + c0 * ycs;
+    if (N <= 16)
+      run_tc<32>(d, d.n, xc, xes, xcs, N, yc, yes, ycs, a, b, ws, slot, s, status, num_sms);
+    else if (N <= 32)
+      run_tc<64>(d, d.n, xc, xes, xcs, N, yc, yes, ycs, a, b, ws, slot, s, status, num_sms);
+    else
+      run_tc<128>(d, d.n, xc, xes, xcs, N, yc, yes, ycs, a, b, ws, slot, s, status, num_sms);
+  }
+  return true;
+}
+
+}  // namespace qob

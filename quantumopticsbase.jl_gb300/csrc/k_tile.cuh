@@ -116,6 +116,7 @@ __global__ void __launch_bounds__(256) k_gather_t(GatherView g, const typename I
   int4* rec = reinterpret_cast<int4*>(tile_smem_raw + off);
   off += (size_t)g.ngroups * sizeof(int4);
 
+  pdl_enter();
   if (threadIdx.x == 0) mbar_init(bar, 1);
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -247,8 +248,8 @@ void launch_t(const GatherView& v, const void* x, int64_t xcs, void* y, int64_t 
   for (int64_t c0 = 0; c0 < ncols; c0 += groups_per_launch * kpc) {
     const int64_t nc = std::min<int64_t>(ncols - c0, groups_per_launch * kpc);
     const int64_t blocks = ntiles * ((nc + kpc - 1) / kpc);
-    kern<<<(unsigned)blocks, threads, smem, s>>>(w, (const XT*)x + c0 * xcs, xcs, (CT*)y + c0 * ycs, ycs, (int)nc, a,
-                                                 b, tbits, status);
+    launch_kernel(v.pdl != 0, kern, dim3((unsigned)blocks), (unsigned)threads, smem, s, w, (const XT*)x + c0 * xcs,
+                  xcs, (CT*)y + c0 * ycs, ycs, (int)nc, a, b, tbits, status);
     QOB_LAUNCHED();
   }
 }

@@ -1084,6 +1084,7 @@ GatherView GatherPlan::view() const {
   v.lane_split = lane_split;
   v.tile_bits = tile_bits;
   v.status = status;
+  v.pdl = 0;
   return v;
 }
 

@@ -3,6 +3,7 @@
 // ("plan") that the kernels execute.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (TMA descriptors; the driver entry point is looked up at run time)
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -185,6 +186,7 @@ struct GatherView {
   uint32_t jmul;
   int32_t lane_split;  // k_gather_j: vector sets per warp (1, 2, 4 or 8; 32/lane_split indices per warp)
   int32_t tile_bits;   // > 0: compact plans on kets use k_gather_t with tiles of 2^tile_bits indices
+  int32_t pdl;         // 1: launched with programmatic stream serialization (QOB_OPT_PDL)
   unsigned* status;    // the context's device status word (bounded waits that gave up, failed checks)
 };
 
@@ -281,12 +283,24 @@ struct GatherPlan {
   GatherView view() const;
 };
 
+// The tensor-core form of a ComplexF32 dense pass (k_tc32.cu): the matrix as
+// a real K-major 2m x ldk array (rows 2i / 2i + 1: real / imaginary parts of
+// row i) and its TMA descriptor, built on first use.
+struct TcDense {
+  int64_t m = 0, n = 0, ldk = 0;
+  DeviceBuf ahat;
+  CUtensorMap map;
+  bool ready = false;
+};
+
 // Dense full-space term (GEMM / GEMV pass) or a mode-k sequence.
 struct DensePass {
   TermCoef coef;
   int64_t m, n;
   DeviceBuf a;  // m x n column-major in the plan's precision (already transposed for RIGHT)
+  TcDense tc;   // ComplexF32 plans: the tensor-core form (QOB_OPT_FP32_TENSOR)
 };
+
 
 struct ModekStep {
   int site;
@@ -371,6 +385,11 @@ struct Context {
   // QOB_OPT_FP64_TENSOR: ComplexF64 dense and mode-product passes whose
   // contracted dimension is >= kDmmaMinK run on the FP64 tensor cores
   bool fp64_tensor = false;
+  // QOB_OPT_PDL: fused gathers launched with programmatic dependent launch
+  bool pdl = false;
+  // QOB_OPT_FP32_TENSOR: ComplexF32 dense operators with both sides >= 64 run
+  // on the tensor cores (tcgen05, TF32 head + tail split)
+  bool fp32_tensor = false;
   // device status word (one unsigned, zeroed at creation): kernels record
   // bounded waits that gave up and failed debug checks; read by qob_device_status
   DeviceBuf status;
@@ -394,7 +413,7 @@ void device_refresh(GatherPlan& g, const double2* factors_dev, cudaStream_t s, c
 // elements, 16 bytes each); unused otherwise.  n = x's length.
 void launch_gather(const GatherPlan& g, int precision, const void* x, int64_t xes, int64_t xcs,
                    void* y, int64_t yes, int64_t ycs, int64_t ncols, c128 alpha, c128 beta,
-                   cudaStream_t s, int64_t n = 0, void* ff_x = nullptr);
+                   cudaStream_t s, int64_t n = 0, void* ff_x = nullptr, bool pdl = false);
 void launch_build_diag(const GatherPlan& g, cudaStream_t s);
 // Factors at factors_dev, or, with a device step counter, at row 2 * *step + off
 // of the table factors_dev (nf factors per row).
@@ -426,6 +445,12 @@ void launch_dense_dmma(const void* a, int64_t m, int64_t n, c128 alpha, const vo
 void launch_modek_dmma(const void* A, int64_t s1, int64_t dout, int64_t din, int64_t s3, c128 alpha, const void* x,
                        int64_t xes, int64_t xcs, c128 beta, void* y, int64_t yes, int64_t ycs, int64_t ncols,
                        cudaStream_t s);
+void tc_dense_build(TcDense& d, const void* a, int64_t m, int64_t n, cudaStream_t s);
+// y = alpha * A x + beta * y for ComplexF32 vectors on the tensor cores;
+// false when d is not built.  Workspace slots slot, slot + 1.
+bool launch_dense_tc(const TcDense& d, c128 alpha, const void* x, int64_t xes, int64_t xcs, c128 beta, void* y,
+                     int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s, Workspace* ws, int slot,
+                     unsigned* status, int num_sms);
 // contracted dimension from which the FP64 tensor-core option applies
 constexpr int64_t kDmmaMinK = 64;
 // Split of ncols vectors of n ComplexF64 elements (element stride es, vector

@@ -28,6 +28,8 @@ QOB_C128 = 0
 QOB_C64 = 1
 QOB_C128X = 2  # ComplexF64 data, fused part in double-float arithmetic
 QOB_OPT_FP64_TENSOR = 1
+QOB_OPT_PDL = 2
+QOB_OPT_FP32_TENSOR = 3
 QOB_LEFT = 0
 QOB_RIGHT = 1
 

@@ -1,0 +1,72 @@
+"""ComplexF32 dense operators on the 5th-generation tensor cores
+(QOB_OPT_FP32_TENSOR: tcgen05.mma kind::tf32, accumulator in tensor memory,
+operand tiles loaded by TMA, each operand split into a TF32 head and tail)
+against the oracle (the reference's dense mul!, src/operators_dense.jl:394-396,
+restated in FP64), at the ComplexF32 tolerance 1e-5 (relative l2): kets from
+the left in every tile width the kernel has (1 .. 100 kets: 16, 32 and 64 kets
+per pass), rows of an operator from the right, beta = 0 over a NaN-filled
+output, a matrix whose sides are not multiples of the tile sizes, and the
+4096 x 4096 operator on 16 kets; the device status word stays clear.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import qobgpu as Q
+from helpers import rand_op
+from qobgpu import operators as O
+from test_gpu_parity import check
+
+pytestmark = pytest.mark.gpu
+
+TOL32 = 1e-5
+AL = 0.7 - 0.2j
+BE = 0.4 - 0.9j
+
+
+@pytest.fixture
+def fp32_tensor():
+    from qobgpu import _lib as L
+    from qobgpu.device import get_context, raise_for
+
+    ctx = get_context(0)
+    raise_for(L.lib().qob_set_option(ctx.ptr, L.QOB_OPT_FP32_TENSOR, 1), ctx)
+    yield
+    raise_for(L.lib().qob_set_option(ctx.ptr, L.QOB_OPT_FP32_TENSOR, 0), ctx)
+    flags = C.c_uint()
+    raise_for(L.lib().qob_device_status(ctx.ptr, None, C.byref(flags)), ctx)
+    assert flags.value == 0
+
+
+@pytest.mark.parametrize("ncols", [1, 3, 16, 17, 40, 64, 100])
+def test_tc32_dense_left(fp32_tensor, ncols):
+    rng = Q.Rng(300 + ncols)
+    bl, br = Q.GenericBasis(700), Q.GenericBasis(500)
+    D = rand_op(rng, bl, br)
+    X = O.Operator(br, Q.GenericBasis(ncols), rng.kets_data(500, ncols))
+    Y = O.Operator(bl, Q.GenericBasis(ncols), rng.kets_data(700, ncols))
+    check(Y, D, X, AL, BE, TOL32, np.complex64)
+    Yn = O.Operator(bl, Q.GenericBasis(ncols), np.full((700, ncols), np.nan, np.complex128, order="F"))
+    check(Yn, D, X, AL, 0.0, TOL32, np.complex64)
+
+
+def test_tc32_dense_right_and_odd_sizes(fp32_tensor):
+    rng = Q.Rng(320)
+    bl, br = Q.GenericBasis(333), Q.GenericBasis(257)
+    D = rand_op(rng, bl, br)
+    R = O.Operator(Q.GenericBasis(5), bl, np.asfortranarray(rng.complex_normal(5 * 333).reshape(5, 333, order="F")))
+    Z = O.Operator(Q.GenericBasis(5), br, np.asfortranarray(rng.complex_normal(5 * 257).reshape(5, 257, order="F")))
+    check(Z, R, D, AL, BE, TOL32, np.complex64)
+    X = O.Operator(br, Q.GenericBasis(7), rng.kets_data(257, 7))
+    Y = O.Operator(bl, Q.GenericBasis(7), rng.kets_data(333, 7))
+    check(Y, D, X, AL, BE, TOL32, np.complex64)
+
+
+def test_tc32_dense_4096_on_16_kets(fp32_tensor):
+    rng = Q.Rng(330)
+    b = Q.GenericBasis(4096)
+    D = rand_op(rng, b, b)
+    X = O.Operator(b, Q.GenericBasis(16), rng.kets_data(4096, 16))
+    Y = O.Operator(b, Q.GenericBasis(16), rng.kets_data(4096, 16))
+    check(Y, D, X, AL, BE, TOL32, np.complex64)

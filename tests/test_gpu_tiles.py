@@ -152,3 +152,64 @@ def test_tune_considers_tiles_and_result_stays_exact():
                           n, 32, n, BE, 0.0, C.c_void_p(yd.data_ptr()), n, 32, n, None), ctx)
     torch.cuda.synchronize(0)
     assert rel_l2(yd.cpu().numpy().astype(np.complex128), _oracle(H, X, Y, AL, BE)) < 1e-5
+
+
+@pytest.mark.parametrize("tile", [None, (10, 2, 1)])
+def test_pdl_keeps_chained_applications_ordered(tile):
+    """QOB_OPT_PDL: each application's blocks may be scheduled while the previous
+    kernel finishes, and wait for it before touching memory.  A chain
+    y1 = H x, y2 = H y1, y3 = H y2 recorded into a CUDA graph and replayed (each
+    step reading the one before) equals the oracle's chain, and is bitwise
+    equal to the same chain without PDL."""
+    import torch
+
+    from qobgpu import _lib as L
+    from qobgpu.device import dtype_code, get_context, handle, raise_for
+
+    H = heisenberg_chain(12, seed=9)
+    n, k = len(H.basis_l), 16
+    rng = Q.Rng(720)
+    X = rng.kets_data(n, k)
+    lib = L.lib()
+    ctx = get_context(0)
+    hd = handle(ctx, H)
+    code = dtype_code(np.complex128)
+    if tile:
+        raise_for(lib.qob_op_set_tile(ctx.ptr, hd.ptr, L.QOB_LEFT, code, tile[1], tile[2], tile[0]), ctx)
+    else:
+        raise_for(lib.qob_op_set_launch(ctx.ptr, hd.ptr, L.QOB_LEFT, code, 2, 128, 1), ctx)
+    ref = [np.asfortranarray(X)]
+    for _ in range(3):
+        ref.append(_oracle(H, ref[-1], np.zeros_like(X), 1.0, 0.0))
+    outs = {}
+    stream = torch.cuda.Stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    for pdl in (0, 1):
+        raise_for(lib.qob_set_option(ctx.ptr, L.QOB_OPT_PDL, pdl), ctx)
+        bufs = [torch.as_tensor(np.ascontiguousarray(X.T), device="cuda:0").t()]
+        bufs += [torch.zeros(k, n, dtype=torch.complex128, device="cuda:0").t() for _ in range(3)]
+
+        def chain():
+            for i in range(3):
+                raise_for(lib.qob_mul(ctx.ptr, L.QOB_LEFT, 0, hd.ptr, code, 1.0, 0.0, C.c_void_p(bufs[i].data_ptr()),
+                                      n, k, n, 0.0, 0.0, C.c_void_p(bufs[i + 1].data_ptr()), n, k, n, sp), ctx)
+
+        torch.cuda.synchronize()
+        chain()  # direct launches
+        stream.synchronize()
+        g = C.c_void_p()
+        raise_for(lib.qob_graph_begin(ctx.ptr, sp), ctx)
+        chain()
+        raise_for(lib.qob_graph_end(ctx.ptr, sp, C.byref(g)), ctx)
+        for b in bufs[1:]:
+            b.zero_()
+        torch.cuda.synchronize()
+        for _ in range(3):
+            raise_for(lib.qob_graph_launch(ctx.ptr, g, sp), ctx)
+        stream.synchronize()
+        lib.qob_graph_free(ctx.ptr, g)
+        outs[pdl] = [b.cpu().numpy() for b in bufs[1:]]
+    raise_for(lib.qob_set_option(ctx.ptr, L.QOB_OPT_PDL, 0), ctx)
+    for i in range(3):
+        assert rel_l2(outs[1][i], ref[i + 1]) < 1e-12
+        assert np.array_equal(outs[1][i], outs[0][i])
