@@ -68,10 +68,12 @@ def _timed_graph(ctx, stream, record, reps=20):
     return e0.elapsed_time(e1) / reps
 
 
-def _modes(dmma=False):
+def _modes(dmma=False, tc32=False):
     """(torch dtype, numpy dtype, dtype code, label): ComplexF64, ComplexF64 in
     double-float arithmetic (QOB_C128X), ComplexF32; with dmma, also ComplexF64
-    on the FP64 tensor cores (QOB_OPT_FP64_TENSOR), labelled "complex128 DMMA"."""
+    on the FP64 tensor cores (QOB_OPT_FP64_TENSOR, "complex128 DMMA"); with
+    tc32, also ComplexF32 on the tcgen05 tensor cores (QOB_OPT_FP32_TENSOR,
+    "complex64 tcgen05")."""
     import torch
 
     out = [(torch.complex128, np.complex128, L.QOB_C128, "complex128"),
@@ -79,22 +81,27 @@ def _modes(dmma=False):
            (torch.complex64, np.complex64, L.QOB_C64, "complex64")]
     if dmma:
         out.insert(1, (torch.complex128, np.complex128, L.QOB_C128, "complex128 DMMA"))
+    if tc32:
+        out.append((torch.complex64, np.complex64, L.QOB_C64, "complex64 tcgen05"))
     return tuple(out)
 
 
 class _Fp64Tensor:
-    """QOB_OPT_FP64_TENSOR on for the rows labelled DMMA."""
+    """The tensor-core option of a row: QOB_OPT_FP64_TENSOR for the rows
+    labelled DMMA, QOB_OPT_FP32_TENSOR for those labelled tcgen05."""
 
     def __init__(self, ctx, label):
-        self.ctx, self.on = ctx, label.endswith("DMMA")
+        self.ctx = ctx
+        self.opt = (L.QOB_OPT_FP64_TENSOR if label.endswith("DMMA")
+                    else L.QOB_OPT_FP32_TENSOR if label.endswith("tcgen05") else None)
 
     def __enter__(self):
-        if self.on:
-            raise_for(L.lib().qob_set_option(self.ctx.ptr, L.QOB_OPT_FP64_TENSOR, 1), self.ctx)
+        if self.opt:
+            raise_for(L.lib().qob_set_option(self.ctx.ptr, self.opt, 1), self.ctx)
 
     def __exit__(self, *exc):
-        if self.on:
-            raise_for(L.lib().qob_set_option(self.ctx.ptr, L.QOB_OPT_FP64_TENSOR, 0), self.ctx)
+        if self.opt:
+            raise_for(L.lib().qob_set_option(self.ctx.ptr, self.opt, 0), self.ctx)
 
 
 def _cols(n, k, dt, seed):
@@ -430,7 +437,7 @@ def dense(ctx, stream):
         b = GenericBasis(nd)
         op = O.Operator(b, b, np.asfortranarray(rng.complex_normal(nd * nd).reshape(nd, nd, order="F")))
         h = handle(ctx, op)
-        for tdt, npdt, code, label in _modes(dmma=True):
+        for tdt, npdt, code, label in _modes(dmma=True, tc32=True):
             for ncols in kets:
                 x = _cols(nd, ncols, tdt, 71)
                 y = _cols(nd, ncols, tdt, 72)
