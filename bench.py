@@ -387,7 +387,8 @@ def run_own(args, rank, world, local_rank):
     def tune(dt):
         times = (C.c_double * NCANDS)()
         chosen = C.c_int()
-        raise_for(lib.qob_op_tune(ctx.ptr, hd.ptr, L.QOB_LEFT, dtype_code(dt), BATCH, times, C.byref(chosen)), ctx)
+        raise_for(lib.qob_op_tune_ex(ctx.ptr, hd.ptr, L.QOB_LEFT, dtype_code(dt), BATCH, times, NCANDS,
+                                     C.byref(chosen)), ctx)
         v = chosen.value
         ms = {f"{1 << (k // 9)}x{SHAPES[k % 9]}": times[k] for k in range(36)}
         ms.update({f"T{b}:{tc}x256s{ls}": times[36 + i] for i, (b, tc, ls) in enumerate(TILE_SHAPES)})

@@ -76,9 +76,9 @@ int qob_version(void);
 int64_t qob_kernel_launches(void);
 
 /* Diagnostics: the device's fused multiply-add rate in TFLOP/s (2 flops per
- * FMA), which = 0 for FP64, 1 for FP32, measured with chains of independent
- * FMAs over (SMs x 4) blocks of 256 threads (one untimed launch, one timed with
- * CUDA events; about 2 ms and 1 ms).  The roofline fraction of an FP64-bound
+ * FMA), which = 0 for FP64, 1 for FP32, measured with 16 independent chains of
+ * FMAs per thread over (SMs x 8) blocks of 256 threads (one untimed launch, the
+ * best of three timed with CUDA events; a few ms).  The roofline fraction of an FP64-bound
  * kernel is taken against this number.  No counterpart in the reference.
  * Synchronous; allocates and frees 8 bytes of device memory. */
 int qob_probe_peak(qob_ctx* ctx, int which, double* tflops);
@@ -104,9 +104,10 @@ const char* qob_last_error(qob_ctx* ctx);
 /* QOB_OPT_FP32_TENSOR, value 0 (default) or 1: ComplexF32 dense operators whose
  * sides are both at least 64 run on the 5th-generation tensor cores
  * (tcgen05.mma kind::tf32 with the accumulator in tensor memory, operand tiles
- * loaded by TMA) with every operand split into a TF32 head and tail and three
- * products per tile, which keeps FP32 accuracy (relative error ~1e-7); a real
- * copy of the matrix (the same size as the complex one) is built on first use. */
+ * brought into shared memory by bulk asynchronous copies) with every operand
+ * split into a TF32 head and tail and three products per tile, which keeps FP32
+ * accuracy (relative error ~1e-7); a real, tiled copy of the matrix (the size
+ * of the complex one, rounded up to 64 rows x 32 columns) is built on first use. */
 #define QOB_OPT_FP32_TENSOR 3
 int qob_set_option(qob_ctx* ctx, int option, int64_t value);
 
@@ -196,25 +197,31 @@ int qob_op_prepare(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t* info)
  * cover 8 output indices x 4 sets of vectors, 5 / 6 = 4 output indices x 8
  * sets, 7 / 8 = 2 output indices x 16 sets (entries that vary with the low
  * index bits then diverge over fewer lanes).  times_ms[9k + b] = milliseconds
- * per application with 2^k vectors per thread and shape b (36 entries).  For
- * plans in the compact form (every merged group one run of power-of-two
- * subsystems with one entry per row, e.g. spin chains) applied to kets from the
- * left, twelve staged-tile shapes follow (times_ms[36 + i]): blocks of 256
- * threads that copy tiles of 2^bits consecutive indices of their kets into
- * shared memory, for (bits, vectors per thread, vector sets per warp) = (10,1,1)
- * (10,2,1) (9,4,1) (11,1,1) (11,2,1) (12,1,1) (9,1,4) (8,1,16) (8,2,8) (9,2,4)
- * (10,1,4) (7,2,16).  -1 marks a shape not tried; times_ms needs 48 entries.
- * *chosen = vectors per thread | (tile bits << 8, 0 when untiled) | (threads
- * per block << 16) | (log2 vector sets per warp << 26) | (1 << 30 when
- * persistent), 0 when the operator has no fused part.  Either pointer may be
- * NULL.  Vector sets (x and y) of 16 MB or more are timed with inputs not in L2
- * (up to 16 scratch copies, at least 256 MB in all, used in turn), smaller ones
- * L2-resident.  Each shape is timed over launches replayed from a CUDA graph on
- * a stream of the context's own (no host launch overhead in the times, as in
- * the recorded loops of qob_rk4 / the server).  Allocates and frees the scratch
- * arrays; synchronous. */
+ * per application with 2^k vectors per thread and shape b, -1 when not tried
+ * (36 entries).  For plans in the compact form (every merged group one run of
+ * power-of-two subsystems with one entry per row, e.g. spin chains) applied to
+ * kets from the left, twelve staged-tile shapes are timed as well (their times
+ * are reported by qob_op_tune_ex).  *chosen = vectors per thread | (tile bits
+ * << 8, 0 when untiled) | (threads per block << 16) | (log2 vector sets per
+ * warp << 26) | (1 << 30 when persistent), 0 when the operator has no fused
+ * part.  Either pointer may be NULL.  Vector sets (x and y) of 16 MB or more
+ * are timed with inputs not in L2 (up to 16 scratch copies, at least 256 MB in
+ * all, used in turn), smaller ones L2-resident.  Each shape is timed over
+ * launches replayed from a CUDA graph on a stream of the context's own (no host
+ * launch overhead in the times, as in the recorded loops of qob_rk4 / the
+ * server).  Allocates and frees the scratch arrays; synchronous. */
 int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, double* times_ms,
                 int* chosen);
+
+/* qob_op_tune with the length of times_ms given: writes min(times_len, 48)
+ * times, the 36 of qob_op_tune followed by the twelve staged-tile shapes
+ * (times_ms[36 + i]): blocks of 256 threads that copy tiles of 2^bits
+ * consecutive indices of their kets into shared memory, for (bits, vectors per
+ * thread, vector sets per warp) = (10,1,1) (10,2,1) (9,4,1) (11,1,1) (11,2,1)
+ * (12,1,1) (9,1,4) (8,1,16) (8,2,8) (9,2,4) (10,1,4) (7,2,16); -1 when not
+ * tried. */
+int qob_op_tune_ex(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, double* times_ms, int times_len,
+                   int* chosen);
 
 /* Fix the launch shape instead of tuning: vectors_per_thread 1, 2, 4 or 8;
  * block 128 or 256 threads, or -256 for the persistent grid; lane_split 1, 2,

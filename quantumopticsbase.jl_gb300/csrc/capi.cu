@@ -512,9 +512,12 @@ int qob_op_prepare(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t* info)
   });
 }
 
-int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, double* times_ms, int* chosen) {
+namespace {
+// The autotuner; writes min(times_len, 48) timings.
+int tune_impl(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, double* times_ms, int times_len,
+              int* chosen) {
   return guard(ctx, [&] {
-    if (!ctx || !op || ncols < 1 || (side != QOB_LEFT && side != QOB_RIGHT))
+    if (!ctx || !op || ncols < 1 || (side != QOB_LEFT && side != QOB_RIGHT) || times_len < 0)
       fail(QOB_ERR_ARG, "qob_op_tune: bad arguments");
     check_mul_dtype(dtype);
     Plan& P = get_plan(ctx->c, op, side, dtype);
@@ -628,13 +631,23 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
       cudaEventDestroy(e1);
     }
     if (times_ms)
-      for (int k = 0; k < kCands; ++k) times_ms[k] = t[k];
+      for (int k = 0; k < kCands && k < times_len; ++k) times_ms[k] = t[k];
     int lg = 0;
     while ((1 << lg) < best_split) ++lg;
     if (chosen)
       *chosen = best | (best_tile << 8) | ((best_block < 0 ? -best_block : best_block) << 16) | (lg << 26) |
                 (best_block < 0 ? (1 << 30) : 0);
   });
+}
+}  // namespace
+
+int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, double* times_ms, int* chosen) {
+  return tune_impl(ctx, op, side, dtype, ncols, times_ms, 36, chosen);
+}
+
+int qob_op_tune_ex(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, double* times_ms, int times_len,
+                   int* chosen) {
+  return tune_impl(ctx, op, side, dtype, ncols, times_ms, times_len, chosen);
 }
 
 int qob_op_set_launch(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_per_thread, int block,

@@ -3,11 +3,16 @@
 // tiles brought in by TMA), for mul! on a DenseOperator
 // (src/operators_dense.jl:394-396, BLAS cgemm in the reference).
 //
-// The complex product is one real GEMM.  The operator is stored (at plan
-// compile time) as the real matrix Ahat of 2m rows, K-major: row 2i holds
-// Re A[i, :], row 2i + 1 holds Im A[i, :] (row length ldk = n rounded up to 32,
-// zero padded).  The vectors are split per call (k_tc_split_b) into Bhat of 2N
-// rows, K-major: row j < N holds Re X[:, j], row N + j holds Im X[:, j].  Then
+// The complex product is one real GEMM.  The operator is stored (built on
+// first use) as the real matrix Ahat of 2m rows, K-major: row 2i holds
+// Re A[i, :], row 2i + 1 holds Im A[i, :] (n rounded up to 32, zero padded).
+// The vectors are split per call (k_tc_split_b) into Bhat of 2N rows, K-major:
+// row j < N holds Re X[:, j], row N + j holds Im X[:, j].  Both are kept in
+// memory as tiles (128 rows x 32 floats of Ahat, BN rows x 32 floats of Bhat),
+// each tile one contiguous block laid out exactly as the MMA reads it from
+// shared memory (rows of 128 bytes, 16-byte chunk c of row r at position
+// c ^ (r mod 8): the 128-byte swizzle), so a stage arrives with one bulk copy
+// per operand (cp.async.bulk) that streams a contiguous block.  Then
 // D = Ahat Bhat^T (2m x 2N, FP32 in tensor memory) gives
 //   Re Y[i, c] = D[2i, c] - D[2i+1, N+c],   Im Y[i, c] = D[2i+1, c] + D[2i, N+c]
 // (in the kernel the imaginary rows of Bhat start at BN / 2, BN = the tile's
@@ -18,21 +23,19 @@
 // below 2^-22 of the product), the split of Ahat done in shared memory as its
 // tiles arrive, the split of Bhat once per call.
 //
-// Block (192 threads): warp 0 issues the TMA loads (a 4-, 3- or 2-stage ring
-// of 128 x 32 Ahat tiles and BN x 32 Bhat head / tail tiles, 128-byte
-// swizzle); warps 2-5 split each Ahat tile into head (in place) and tail, then
+// Block (192 threads): warp 0 issues the bulk copies (a 5-, 4- or 3-stage ring
+// of Ahat tiles and Bhat head / tail tiles); warps 2-5 split each Ahat tile
+// into head (in place) and tail, then
 // run the epilogue; warp 1 owns the tensor memory and one of its threads
 // issues the MMAs (M = 128 rows, N = BN = 2 x kets, K = 8 per instruction).
 // Blocks cover 64 complex rows each and, when that leaves SMs idle, a range of
-// k blocks whose partial products k_tc_reduce adds in order.  Every wait is
+// k blocks whose partial products k_tc_reduce adds in order; the grid is one
+// wave (one block per SM by its shared memory).  Every wait is
 // bounded: a wait that gives up records kTcErrTimeout in the status word, the
 // block drains its copies and MMAs, frees its tensor memory and returns.
-#include <cuda.h>
-#include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <mutex>
 
 #include "qob_internal.h"
 
@@ -73,13 +76,15 @@ __device__ __forceinline__ bool bar_wait(uint64_t* b, uint32_t parity) {
   }
   return false;
 }
-__device__ __forceinline__ void tma_2d(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* b) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
-          "r"(saddr(dst)),
-      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(saddr(b))
-      : "memory");
+// bytes (a multiple of 16) from global src to shared dst, both 16-byte aligned, counted on b
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, uint64_t* b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   saddr(dst)),
+               "l"(src), "r"(bytes), "r"(saddr(b))
+               : "memory");
 }
+// float offset of element (row r, column k) inside a swizzled tile of 32-float rows
+__host__ __device__ __forceinline__ int swz(int r, int k) { return r * 32 + ((((k >> 2) ^ (r & 7)) << 2) | (k & 3)); }
 // Shared-memory matrix descriptor of a K-major tile with the 128-byte swizzle:
 // start address, stride between 8-row groups 1024 bytes, descriptor version 1.
 __device__ __forceinline__ uint64_t sw128_desc(const void* tile) {
@@ -118,7 +123,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 
 template <int BN>
 struct TcCfg {
-  static constexpr int kStages = BN <= 64 ? 4 : (BN <= 128 ? 3 : 2);
+  static constexpr int kStages = BN <= 32 ? 5 : (BN <= 64 ? 4 : 3);
   static constexpr int kATile = kTcBM * kTcBK * 4;  // 16 KB
   static constexpr int kBTile = BN * kTcBK * 4;
   static constexpr int kStage = 2 * kATile + 2 * kBTile;  // A head (in place), A tail, B head, B tail
@@ -130,9 +135,9 @@ struct TcCfg {
 // or the block's partial product into part[kz][c][i] when part != null.
 template <int BN>
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_tc_cgemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmBh,
-               const __grid_constant__ CUtensorMap tmBl, int64_t m, int N, int nkb, int kb_per, float2* y, int64_t yes,
-               int64_t ycs, float2 alpha, float2 beta, float2* part, unsigned* status) {
+    k_tc_cgemm(const float* __restrict__ ahat, const float* __restrict__ bh_t, const float* __restrict__ bl_t,
+               int64_t m, int N, int nkb, int kb_per, float2* y, int64_t yes, int64_t ycs, float2 alpha, float2 beta,
+               float2* part, unsigned* status) {
   using C = TcCfg<BN>;
   constexpr int S = C::kStages;
   extern __shared__ __align__(16) unsigned char tc_smem_raw[];
@@ -152,7 +157,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int kb0 = blockIdx.y * kb_per;
   const int nk = min(nkb - kb0, kb_per);  // >= 1 (the host makes no empty ranges)
-  const int row0 = blockIdx.x * kTcBM;
+  const int row0 = blockIdx.x * kTcBM;  // first Ahat row of this block
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
@@ -186,10 +191,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         if (*(volatile int*)abort_flag) break;
         bar_expect(&full[s], 2 * C::kBTile + C::kATile);
-        const int kc = (kb0 + it) * kTcBK;
-        tma_2d(stageA(s), &tmA, kc, row0, &full[s]);
-        tma_2d(stageBh(s), &tmBh, kc, 0, &full[s]);
-        tma_2d(stageBl(s), &tmBl, kc, 0, &full[s]);
+        const int kb = kb0 + it;
+        bulk_copy(stageA(s), ahat + ((int64_t)blockIdx.x * nkb + kb) * (C::kATile / 4), C::kATile, &full[s]);
+        bulk_copy(stageBh(s), bh_t + (int64_t)kb * (C::kBTile / 4), C::kBTile, &full[s]);
+        bulk_copy(stageBl(s), bl_t + (int64_t)kb * (C::kBTile / 4), C::kBTile, &full[s]);
         issued = it + 1;
       }
       // every copy issued has landed before the block's shared memory goes away
@@ -301,20 +306,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 }
 
 // Bhat head and tail: row j = Re X[:, j], row H + j = Im X[:, j] (j < the
-// kets, H = half the tile's columns), TF32-split, K-major with row length ldk
-// (zero beyond n).
-__global__ void k_tc_split_b(const float2* __restrict__ x, int64_t n, int64_t xes, int64_t xcs, int H, int64_t ldk,
+// kets, H = half the tile's BN columns), TF32-split, as swizzled tiles of BN
+// rows x 32 floats, one per k block (zero beyond n).
+__global__ void k_tc_split_b(const float2* __restrict__ x, int64_t n, int64_t xes, int64_t xcs, int BN, int64_t nkb,
                              float* __restrict__ bh, float* __restrict__ bl) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
-  if (k >= ldk) return;
+  if (k >= nkb * kTcBK) return;
   float2 v = make_float2(0.f, 0.f);
   if (k < n) v = x[k * xes + (int64_t)j * xcs];
   const float hr = tf32_rn(v.x), hi = tf32_rn(v.y);
-  bh[(int64_t)j * ldk + k] = hr;
-  bl[(int64_t)j * ldk + k] = tf32_rn(v.x - hr);
-  bh[(int64_t)(H + j) * ldk + k] = hi;
-  bl[(int64_t)(H + j) * ldk + k] = tf32_rn(v.y - hi);
+  const int64_t tile = (k / kTcBK) * (int64_t)BN * kTcBK;
+  const int kk = (int)(k % kTcBK);
+  const int64_t o_re = tile + swz(j, kk), o_im = tile + swz(BN / 2 + j, kk);
+  bh[o_re] = hr;
+  bl[o_re] = tf32_rn(v.x - hr);
+  bh[o_im] = hi;
+  bl[o_im] = tf32_rn(v.y - hi);
 }
 
 // y[i, c] = alpha * (sum of the k ranges' partial products, in order) + beta * y[i, c]
@@ -340,63 +348,31 @@ __global__ void k_tc_reduce(const float2* __restrict__ part, int kchunks, int64_
   *yp = make_float2(re, im);
 }
 
-// cuTensorMapEncodeTiled from the driver, looked up once.
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    cudaGetLastError();
-  });
-  if (!fn) fail(QOB_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-  return fn;
-}
-
-// rows x ldk FP32, K-major, boxes of box_rows x 32 with the 128-byte swizzle
-CUtensorMap kmajor_map(const void* p, int64_t rows, int64_t ldk, int box_rows) {
-  CUtensorMap m;
-  const cuuint64_t dims[2] = {(cuuint64_t)ldk, (cuuint64_t)rows};
-  const cuuint64_t strides[1] = {(cuuint64_t)ldk * 4};
-  const cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
-  const cuuint32_t es[2] = {1, 1};
-  const CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(p), dims, strides, box, es,
-                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) fail(QOB_ERR_CUDA, "cuTensorMapEncodeTiled failed");
-  return m;
-}
-
 template <int BN>
 void run_tc(const TcDense& d, int64_t n, const float2* x, int64_t xes, int64_t xcs, int N, float2* y, int64_t yes,
             int64_t ycs, float2 alpha, float2 beta, Workspace* ws, int slot, cudaStream_t s, unsigned* status,
             int num_sms) {
   using C = TcCfg<BN>;
-  const int64_t ldk = d.ldk;
-  // split vectors: head and tail of Bhat, BN rows each (rows N .. BN/2 unused when N < BN/2)
-  const size_t bbytes = (size_t)BN * ldk * 4;
+  const int64_t nkb = d.ldk / kTcBK;
+  // split vectors: head and tail tiles of Bhat (rows N .. BN/2 - 1 and BN/2 + N .. BN - 1 stay zero)
+  const size_t bbytes = (size_t)nkb * C::kBTile;
   char* w = static_cast<char*>(ws->get(slot, 2 * bbytes + 256));
   float* bh = reinterpret_cast<float*>(w);
   float* bl = reinterpret_cast<float*>(w + bbytes);
   if (N < BN / 2) QOB_CUDA(cudaMemsetAsync(w, 0, 2 * bbytes, s));
-  k_tc_split_b<<<dim3((unsigned)((ldk + 255) / 256), (unsigned)N), 256, 0, s>>>(x, n, xes, xcs, BN / 2, ldk, bh, bl);
+  k_tc_split_b<<<dim3((unsigned)((d.ldk + 255) / 256), (unsigned)N), 256, 0, s>>>(x, n, xes, xcs, BN, nkb, bh, bl);
   QOB_LAUNCHED();
-  const CUtensorMap mb_h = kmajor_map(bh, BN, ldk, BN), mb_l = kmajor_map(bl, BN, ldk, BN);
-  const int nkb = (int)(ldk / kTcBK);
-  const int mt = (int)((2 * d.m + kTcBM - 1) / kTcBM);
-  // k ranges so that the blocks cover the SMs (each range at least 8 k blocks)
-  int kchunks = std::max(1, std::min((num_sms + mt - 1) / mt, nkb / 8));
-  const int kb_per = (nkb + kchunks - 1) / kchunks;
-  kchunks = (nkb + kb_per - 1) / kb_per;
+  const int mt = (int)d.mtiles;
+  // k ranges so that the blocks fill the SMs in one wave (each range at least 4 k blocks)
+  int kchunks = (int)std::max<int64_t>(1, std::min<int64_t>(num_sms / std::max(1, mt), nkb / 4));
+  const int kb_per = (int)((nkb + kchunks - 1) / kchunks);
+  kchunks = (int)((nkb + kb_per - 1) / kb_per);
   float2* part = nullptr;
   if (kchunks > 1) part = static_cast<float2*>(ws->get(slot + 1, (size_t)kchunks * N * d.m * sizeof(float2)));
   auto kern = k_tc_cgemm<BN>;
   QOB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::kSmem));
-  kern<<<dim3((unsigned)mt, (unsigned)kchunks), kTcThreads, C::kSmem, s>>>(d.map, mb_h, mb_l, d.m, N, nkb, kb_per, y,
-                                                                         yes, ycs, alpha, beta, part, status);
+  kern<<<dim3((unsigned)mt, (unsigned)kchunks), kTcThreads, C::kSmem, s>>>(
+      static_cast<const float*>(d.ahat.p), bh, bl, d.m, N, (int)nkb, kb_per, y, yes, ycs, alpha, beta, part, status);
   QOB_LAUNCHED();
   if (part) {
     k_tc_reduce<<<dim3((unsigned)((d.m + 127) / 128), (unsigned)N), 128, 0, s>>>(part, kchunks, d.m, N, y, yes, ycs,
@@ -405,15 +381,20 @@ void run_tc(const TcDense& d, int64_t n, const float2* x, int64_t xes, int64_t x
   }
 }
 
-// Ahat of the stored ComplexF32 matrix (column-major m x n, on the device),
-// built once on first use: row 2i = Re A[i, :], row 2i + 1 = Im A[i, :].
-__global__ void k_tc_build_ahat(const float2* __restrict__ a, int64_t m, int64_t n, int64_t ldk, float* __restrict__ ah) {
+// Ahat of the stored ComplexF32 matrix (column-major m x n, on the device) as
+// swizzled 128 x 32 tiles, tile (t, b) at float offset (t * nkb + b) * 4096:
+// row 2i = Re A[i, :], row 2i + 1 = Im A[i, :]; zero beyond the matrix.
+__global__ void k_tc_build_ahat(const float2* __restrict__ a, int64_t m, int64_t n, int64_t nkb, float* __restrict__ ah) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // complex row
   const int64_t k = blockIdx.y;
-  if (i >= m || k >= ldk) return;
-  const float2 v = k < n ? a[i + k * m] : make_float2(0.f, 0.f);
-  ah[(2 * i) * ldk + k] = v.x;
-  ah[(2 * i + 1) * ldk + k] = v.y;
+  const int64_t mpad = (2 * m + kTcBM - 1) / kTcBM * kTcBM / 2;
+  if (i >= mpad || k >= nkb * kTcBK) return;
+  const float2 v = (i < m && k < n) ? a[i + k * m] : make_float2(0.f, 0.f);
+  const int64_t r = 2 * i;  // Ahat row of the real part; the imaginary part is the next row of the same tile
+  const int64_t tile = ((r / kTcBM) * nkb + k / kTcBK) * (int64_t)(kTcBM * kTcBK);
+  const int rr = (int)(r % kTcBM), kk = (int)(k % kTcBK);
+  ah[tile + swz(rr, kk)] = v.x;
+  ah[tile + swz(rr + 1, kk)] = v.y;
 }
 
 }  // namespace
@@ -422,12 +403,14 @@ void tc_dense_build(TcDense& d, const void* a, int64_t m, int64_t n, cudaStream_
   d.m = m;
   d.n = n;
   d.ldk = (n + kTcBK - 1) / kTcBK * kTcBK;
+  d.mtiles = (2 * m + kTcBM - 1) / kTcBM;
   if (d.ldk > 65535) fail(QOB_ERR_UNSUPPORTED, "tensor-core dense path: more than 65535 columns");
-  d.ahat.alloc((size_t)2 * m * d.ldk * sizeof(float));
-  k_tc_build_ahat<<<dim3((unsigned)((m + 127) / 128), (unsigned)d.ldk), 128, 0, s>>>(
-      static_cast<const float2*>(a), m, n, d.ldk, static_cast<float*>(d.ahat.p));
+  const int64_t nkb = d.ldk / kTcBK;
+  d.ahat.alloc((size_t)d.mtiles * nkb * kTcBM * kTcBK * sizeof(float));
+  const int64_t mpad = d.mtiles * kTcBM / 2;
+  k_tc_build_ahat<<<dim3((unsigned)((mpad + 127) / 128), (unsigned)d.ldk), 128, 0, s>>>(
+      static_cast<const float2*>(a), m, n, nkb, static_cast<float*>(d.ahat.p));
   QOB_LAUNCHED();
-  d.map = kmajor_map(d.ahat.p, 2 * m, d.ldk, kTcBM);
   d.ready = true;
 }
 

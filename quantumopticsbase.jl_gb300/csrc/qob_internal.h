@@ -3,7 +3,6 @@
 // ("plan") that the kernels execute.
 #pragma once
 
-#include <cuda.h>  // CUtensorMap (TMA descriptors; the driver entry point is looked up at run time)
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -284,12 +283,11 @@ struct GatherPlan {
 };
 
 // The tensor-core form of a ComplexF32 dense pass (k_tc32.cu): the matrix as
-// a real K-major 2m x ldk array (rows 2i / 2i + 1: real / imaginary parts of
-// row i) and its TMA descriptor, built on first use.
+// a real K-major array of 2m rows (rows 2i / 2i + 1: real / imaginary parts of
+// row i, n padded to ldk), stored as swizzled 128 x 32 tiles; built on first use.
 struct TcDense {
-  int64_t m = 0, n = 0, ldk = 0;
+  int64_t m = 0, n = 0, ldk = 0, mtiles = 0;
   DeviceBuf ahat;
-  CUtensorMap map;
   bool ready = false;
 };
 

@@ -60,6 +60,7 @@ SIGNATURES = {
     "qob_op_shape": (I, [VP, VP, I64P, I64P]),
     "qob_op_prepare": (I, [VP, VP, I, I, I64P]),
     "qob_op_tune": (I, [VP, VP, I, I, I64, DP, C.POINTER(C.c_int)]),
+    "qob_op_tune_ex": (I, [VP, VP, I, I, I64, DP, I, C.POINTER(C.c_int)]),
     "qob_op_set_launch": (I, [VP, VP, I, I, I, I, I]),
     "qob_op_set_tile": (I, [VP, VP, I, I, I, I, I]),
     "qob_device_status": (I, [VP, VP, C.POINTER(C.c_uint)]),

@@ -128,8 +128,9 @@ def test_tile_equals_untiled_bitwise_on_bench_workload(form):
 
 
 def test_tune_considers_tiles_and_result_stays_exact():
-    """qob_op_tune times the staged-tile shapes for a compact plan (48 times
-    reported); whatever it picks matches the oracle."""
+    """qob_op_tune_ex reports the staged-tile shapes' times for a compact plan
+    (48 times) and writes no more than the length it is given; whatever the
+    tuner picks matches the oracle."""
     from qobgpu import _lib as L
     from qobgpu.device import get_context, handle, raise_for
 
@@ -139,8 +140,12 @@ def test_tune_considers_tiles_and_result_stays_exact():
     hd = handle(ctx, H)
     times = (C.c_double * 48)()
     chosen = C.c_int()
-    raise_for(lib.qob_op_tune(ctx.ptr, hd.ptr, L.QOB_LEFT, L.QOB_C64, 32, times, C.byref(chosen)), ctx)
+    raise_for(lib.qob_op_tune_ex(ctx.ptr, hd.ptr, L.QOB_LEFT, L.QOB_C64, 32, times, 48, C.byref(chosen)), ctx)
     assert sum(1 for t in times[36:] if t > 0) >= 10
+    short = (C.c_double * 37)()  # a shorter array gets only its own length
+    short[36] = 12345.0
+    raise_for(lib.qob_op_tune_ex(ctx.ptr, hd.ptr, L.QOB_LEFT, L.QOB_C64, 32, short, 36, C.byref(chosen)), ctx)
+    assert short[36] == 12345.0
     n = len(H.basis_l)
     rng = Q.Rng(712)
     X, Y = rng.kets_data(n, 32), rng.kets_data(n, 32)
