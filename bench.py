@@ -547,8 +547,8 @@ def probe_peaks(dev):
         r = C.c_double()
         raise_for(L.lib().qob_probe_peak(ctx.ptr, which, C.byref(r)), ctx)
         out[name] = r.value
-    out["how"] = ("qob_probe_peak: 8 independent FMA chains per thread, (SMs x 4) blocks of 256 threads, "
-                  "one untimed and one timed launch (CUDA events)")
+    out["how"] = ("qob_probe_peak: 16 independent FMA chains per thread, (SMs x 8) blocks of 256 threads, "
+                  "one untimed launch, best of three timed (CUDA events)")
     return out
 
 

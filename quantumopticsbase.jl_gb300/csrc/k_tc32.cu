@@ -25,7 +25,8 @@
 //
 // Block (192 threads): warp 0 issues the bulk copies (a 5-, 4- or 3-stage ring
 // of Ahat tiles and Bhat head / tail tiles); warps 2-5 split each Ahat tile
-// into head (in place) and tail, then
+// into head (in place) and tail, add each k block's accumulator to registers
+// (see k_tc_cgemm), then
 // run the epilogue; warp 1 owns the tensor memory and one of its threads
 // issues the MMAs (M = 128 rows, N = BN = 2 x kets, K = 8 per instruction).
 // Blocks cover 64 complex rows each and, when that leaves SMs idle, a range of
@@ -127,12 +128,19 @@ struct TcCfg {
   static constexpr int kATile = kTcBM * kTcBK * 4;  // 16 KB
   static constexpr int kBTile = BN * kTcBK * 4;
   static constexpr int kStage = 2 * kATile + 2 * kBTile;  // A head (in place), A tail, B head, B tail
-  static constexpr int kTmemCols = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
+  static constexpr int kTmemCols = 2 * BN;                // two accumulators of BN columns
   static constexpr size_t kSmem = 1024 /* alignment */ + (size_t)kStages * kStage + 256 /* barriers */;
 };
 
 // Y[i, c] (complex rows i < m, kets c < N) = alpha * (Ahat Bhat^T combined) + beta * Y,
 // or the block's partial product into part[kz][c][i] when part != null.
+//
+// Accumulation: each k block (32 terms, twelve MMAs) starts a fresh
+// accumulator in tensor memory, two of them used in turn; the split warps read
+// the finished one and add it to FP32 registers, rounding to nearest.  The
+// tensor cores' own accumulation (which does not round to nearest) then spans
+// 32 terms only, which keeps the FP32 accuracy of the ComplexF32 mode for long
+// rows (the error no longer grows with n).
 template <int BN>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_tc_cgemm(const float* __restrict__ ahat, const float* __restrict__ bh_t, const float* __restrict__ bl_t,
@@ -143,12 +151,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   extern __shared__ __align__(16) unsigned char tc_smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)tc_smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* bars = reinterpret_cast<uint64_t*>(base + (size_t)S * C::kStage);
-  uint64_t* full = bars;           // TMA landed          (count 1 + tx)
-  uint64_t* conv = bars + S;       // A split done        (count 128)
-  uint64_t* empty = bars + 2 * S;  // MMAs read the stage (count 1, tcgen05.commit)
-  uint64_t* accf = bars + 3 * S;   // all MMAs complete
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3 * S + 1);
-  int* abort_flag = reinterpret_cast<int*>(bars + 3 * S + 2);
+  uint64_t* full = bars;           // copies landed            (count 1 + tx)
+  uint64_t* conv = bars + S;       // A tile split             (count 128)
+  uint64_t* empty = bars + 2 * S;  // MMAs read the stage      (count 1, tcgen05.commit)
+  uint64_t* accf = bars + 3 * S;   // [2] accumulator written  (count 1, tcgen05.commit)
+  uint64_t* acce = bars + 3 * S + 2;  // [2] accumulator read  (count 128)
+  uint64_t* fin = bars + 3 * S + 4;   // every MMA issued has completed (count 1, tcgen05.commit)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3 * S + 5);
+  int* abort_flag = reinterpret_cast<int*>(bars + 3 * S + 6);
   auto stageA = [&](int s) { return base + (size_t)s * C::kStage; };
   auto stageAl = [&](int s) { return base + (size_t)s * C::kStage + C::kATile; };
   auto stageBh = [&](int s) { return base + (size_t)s * C::kStage + 2 * C::kATile; };
@@ -157,7 +167,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int kb0 = blockIdx.y * kb_per;
   const int nk = min(nkb - kb0, kb_per);  // >= 1 (the host makes no empty ranges)
-  const int row0 = blockIdx.x * kTcBM;  // first Ahat row of this block
+  const int row0 = blockIdx.x * kTcBM;    // first Ahat row of this block
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
@@ -165,7 +175,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       bar_init(&conv[s], 128);
       bar_init(&empty[s], 1);
     }
-    bar_init(accf, 1);
+    for (int b = 0; b < 2; ++b) {
+      bar_init(&accf[b], 1);
+      bar_init(&acce[b], 128);
+    }
+    bar_init(fin, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -205,33 +219,57 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       // kind::tf32, FP32 accumulator, A and B K-major, N = BN, M = 128
       const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kTcBM >> 4) << 24);
       for (int it = 0; it < nk; ++it) {
-        const int s = it % S;
-        if (!bar_wait(&conv[s], (it / S) & 1)) {
+        const int s = it % S, b = it & 1;
+        if (!bar_wait(&conv[s], (it / S) & 1) || (it >= 2 && !bar_wait(&acce[b], ((it >> 1) - 1) & 1))) {
           atomicExch(abort_flag, 1);
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t d = tmem + (uint32_t)(b * BN);
         const uint64_t ah = sw128_desc(stageA(s)), al = sw128_desc(stageAl(s));
         const uint64_t bh = sw128_desc(stageBh(s)), bl = sw128_desc(stageBl(s));
 #pragma unroll
         for (int kk = 0; kk < kTcBK / 8; ++kk) {  // 8 TF32 = 32 bytes = 2 descriptor units per step
           const uint64_t o = (uint64_t)(2 * kk);
-          mma_tf32(tmem, ah + o, bh + o, idesc, (it > 0 || kk > 0) ? 1u : 0u);
-          mma_tf32(tmem, ah + o, bl + o, idesc, 1u);
-          mma_tf32(tmem, al + o, bh + o, idesc, 1u);
+          mma_tf32(d, ah + o, bh + o, idesc, kk > 0 ? 1u : 0u);
+          mma_tf32(d, ah + o, bl + o, idesc, 1u);
+          mma_tf32(d, al + o, bh + o, idesc, 1u);
         }
         mma_commit(&empty[s]);
+        mma_commit(&accf[b]);
       }
-      mma_commit(accf);  // fires when every MMA issued above has completed
+      mma_commit(fin);  // also after an early exit: fires when every MMA above has completed
     }
   } else {
-    // warps 2-5: split each A tile into head (in place) and tail
+    // warps 2-5: split each A tile into head (in place) and tail; after each
+    // k block, add its accumulator (this warp's 32 rows) to registers
     const int ct = threadIdx.x - 64;
+    const int q4 = warp & 3;  // tensor-memory lanes 32 * q4 .. 32 * q4 + 31
+    const uint32_t lane_addr = tmem + ((uint32_t)(q4 * 32) << 16);
+    float acc[BN];
+#pragma unroll
+    for (int c = 0; c < BN; ++c) acc[c] = 0.f;
     bool ok = true;
-    for (int it = 0; it < nk; ++it) {
+    auto drain = [&](int j) {
+      const int b = j & 1;
+      if (!__all_sync(0xffffffffu, bar_wait(&accf[b], (j >> 1) & 1) && !*(volatile int*)abort_flag)) {
+        ok = false;
+        return;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        float v[16];
+        tmem_ld16(lane_addr + (uint32_t)(b * BN + c0), v);
+#pragma unroll
+        for (int t = 0; t < 16; ++t) acc[c0 + t] += v[t];
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      bar_arrive(&acce[b]);
+    };
+    for (int it = 0; it < nk && ok; ++it) {
       const int s = it % S;
       if (*(volatile int*)abort_flag || !bar_wait(&full[s], (it / S) & 1)) {
-        atomicExch(abort_flag, 1);
         ok = false;
         break;
       }
@@ -255,48 +293,43 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       bar_arrive(&conv[s]);
+      if (it >= 1) drain(it - 1);
     }
-    // epilogue: this warp reads tensor-memory lanes 32 * (warp % 4) ...
-    // the tensor-memory loads below are warp-wide: decide per warp
-    const bool done = __all_sync(0xffffffffu, bar_wait(accf, 0) && ok && !*(volatile int*)abort_flag);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (!done) {
+    if (ok) drain(nk - 1);
+    ok = __all_sync(0xffffffffu, ok && !*(volatile int*)abort_flag);
+    if (!ok) {
+      atomicExch(abort_flag, 1);
       if (lane == 0 && status) atomicOr(status, kTcErrTimeout);
     } else {
-      const int q4 = warp & 3;
       const int r = q4 * 32 + lane;  // accumulator row = Ahat row row0 + r
       const int64_t i = (int64_t)(row0 + r) >> 1;
       const bool even = (lane & 1) == 0;
-      const uint32_t lane_addr = tmem + ((uint32_t)(q4 * 32) << 16);
-      for (int c0 = 0; c0 < N; c0 += 16) {
-        float d[16], e[16];
-        tmem_ld16(lane_addr + (uint32_t)c0, d);        // columns c0 .. c0 + 15: real parts of the kets
-        tmem_ld16(lane_addr + (uint32_t)(BN / 2 + c0), e);  // columns BN/2 + c0 ..: imaginary parts
 #pragma unroll
-        for (int t = 0; t < 16; ++t) {
-          const float other = __shfl_xor_sync(0xffffffffu, e[t], 1);
-          const float v = even ? d[t] - other : d[t] + other;  // even lane: Re Y, odd lane: Im Y
-          const float w = __shfl_xor_sync(0xffffffffu, v, 1);
-          const int c = c0 + t;
-          if (even && i < m && c < N) {
-            if (part) {
-              part[((int64_t)blockIdx.y * N + c) * m + i] = make_float2(v, w);
-            } else {
-              float2* yp = y + i * yes + (int64_t)c * ycs;
-              float re = alpha.x * v - alpha.y * w;
-              float im = alpha.x * w + alpha.y * v;
-              if (beta.x != 0.f || beta.y != 0.f) {
-                const float2 o = *yp;
-                re = __fmaf_rn(beta.x, o.x, __fmaf_rn(-beta.y, o.y, re));
-                im = __fmaf_rn(beta.x, o.y, __fmaf_rn(beta.y, o.x, im));
-              }
-              *yp = make_float2(re, im);
+      for (int c = 0; c < BN / 2; ++c) {
+        // columns c: real parts of the kets, BN/2 + c: imaginary parts
+        const float other = __shfl_xor_sync(0xffffffffu, acc[BN / 2 + c], 1);
+        const float v = even ? acc[c] - other : acc[c] + other;  // even lane: Re Y, odd lane: Im Y
+        const float w = __shfl_xor_sync(0xffffffffu, v, 1);
+        if (even && i < m && c < N) {
+          if (part) {
+            part[((int64_t)blockIdx.y * N + c) * m + i] = make_float2(v, w);
+          } else {
+            float2* yp = y + i * yes + (int64_t)c * ycs;
+            float re = alpha.x * v - alpha.y * w;
+            float im = alpha.x * w + alpha.y * v;
+            if (beta.x != 0.f || beta.y != 0.f) {
+              const float2 o = *yp;
+              re = __fmaf_rn(beta.x, o.x, __fmaf_rn(-beta.y, o.y, re));
+              im = __fmaf_rn(beta.x, o.y, __fmaf_rn(beta.y, o.x, im));
             }
+            *yp = make_float2(re, im);
           }
         }
       }
     }
   }
+  // every MMA issued has completed before the tensor memory is freed
+  if (warp == 1 && lane == 0) bar_wait(fin, 0);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 1) {

@@ -13,7 +13,8 @@
 // the high subsystems) gather from global memory, where the partner tile is
 // another block's input and sits in L2.  The arithmetic and its order are those
 // of k_gather_j: the merged diagonal first, then the groups in plan order, then
-// y = alpha * acc + beta * y, so both kernels give the same bits.
+// y = alpha * acc + beta * y (the two agree to rounding: the compiler may fuse a
+// multiply and an add differently in the two kernels).
 //
 // Threads: a warp covers 32 / ls consecutive J x ls sets of TC kets (ket q + k
 // * ls of the block for set q), as in k_gather_j's lane split; the staged rows

@@ -66,10 +66,10 @@ for tile in (False, True):
     assert rc == 0 and fl == 0 and err < 1e-12, (tile, rc, fl, err)
     bad = heisenberg_chain(6, seed=2)
     hd = handle(ctx, bad)
-    raise_for(lib.qob_mul(ctx.ptr, L.QOB_LEFT, 1, hd.ptr, L.QOB_C128, 1.0, 0.0,
-                          C.c_void_p(torch.zeros(n, dtype=torch.complex128, device="cuda:0").data_ptr()), n, 1, n,
-                          0.0, 0.0, C.c_void_p(torch.zeros(n, dtype=torch.complex128, device="cuda:0").data_ptr()),
-                          n, 1, n, None), ctx)  # compiles the plan
+    z_in = torch.zeros(n, dtype=torch.complex128, device="cuda:0")
+    z_out = torch.zeros(n, dtype=torch.complex128, device="cuda:0")
+    raise_for(lib.qob_mul(ctx.ptr, L.QOB_LEFT, 1, hd.ptr, L.QOB_C128, 1.0, 0.0, C.c_void_p(z_in.data_ptr()), n, 1, n,
+                          0.0, 0.0, C.c_void_p(z_out.data_ptr()), n, 1, n, None), ctx)  # compiles the plan
     torch.cuda.synchronize()
     raise_for(lib.qob_debug_shift_slot(ctx.ptr, hd.ptr, L.QOB_LEFT, L.QOB_C128, n), ctx)
     rc, fl, msg, err = run(bad, tile)
