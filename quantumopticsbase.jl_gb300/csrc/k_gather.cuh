@@ -616,52 +616,26 @@ __device__ __forceinline__ void accumulate(const GatherView& g, const SiteTable&
   }
   if (W1 && g.fast) {
     // every group: one run of power-of-two subsystems, one slot per row; its
-    // shift, mask and first slot sit in one 16-byte word after the descriptors.
-    // Groups go in chunks of kFastChunk: the chunk's gathers are all issued
-    // (predicated on a nonzero entry) before any of them is accumulated, so a
-    // warp keeps kFastChunk x TC loads in flight instead of waiting on each
-    // one; the accumulation order is the groups' order, as before.
-    constexpr int kFastChunk = 4;
+    // shift, mask and first slot sit in one 16-byte word after the descriptors
     const int4* fg = reinterpret_cast<const int4*>(sg + g.ngroups);
-    for (int g0 = 0; g0 < g.ngroups; g0 += kFastChunk) {
-      VT v[kFastChunk];
-      const CT* xp[kFastChunk];
-      bool act[kFastChunk], im[kFastChunk];
-#pragma unroll
-      for (int u = 0; u < kFastChunk; ++u) {
-        v[u] = VT();
-        xp[u] = xb;
-        act[u] = false;
-        im[u] = false;
-        if (g0 + u < g.ngroups) {
-          const int4 f = fg[g0 + u];
-          const uint32_t r = (J >> f.x) & (uint32_t)f.y;
-          if (kDebugBounds && out_of_range((int64_t)f.z + r, g.ell_slots, g.status)) continue;
-          const ET s = ell[f.z + r];
-          v[u] = Ell<R, VM != kComplex>::v(s);
-          const int64_t idx = (int64_t)(J - (r << f.x)) + s.col;
-          act[u] = nz(v[u]) && !(kDebugBounds && out_of_range(idx, g.n, g.status));
-          im[u] = VM == kPhased && f.w != 0;
-          xp[u] = xb + idx * es;
-        }
-      }
-      CT xv[kFastChunk][TC];
-#pragma unroll
-      for (int u = 0; u < kFastChunk; ++u)
-#pragma unroll
-        for (int t = 0; t < TC; ++t)
-          if (act[u] && t < nt) xv[u][t] = ld(xp[u] + t * xcs);
-#pragma unroll
-      for (int u = 0; u < kFastChunk; ++u) {
-        if (!act[u]) continue;
-        if (im[u]) {
+#pragma unroll 4
+    for (int gi = 0; gi < g.ngroups; ++gi) {
+      const int4 f = fg[gi];
+      const uint32_t r = (J >> f.x) & (uint32_t)f.y;
+      if (kDebugBounds && out_of_range((int64_t)f.z + r, g.ell_slots, g.status)) continue;
+      const ET s = ell[f.z + r];
+      const VT v = Ell<R, VM != kComplex>::v(s);
+      const CT* xp = xb + ((int64_t)(J - (r << f.x)) + s.col) * es;
+      if (kDebugBounds && nz(v) && out_of_range((int64_t)(J - (r << f.x)) + s.col, g.n, g.status)) continue;
+      if (nz(v)) {
+        if (VM == kPhased && f.w != 0) {
 #pragma unroll
           for (int t = 0; t < TC; ++t)
-            if (t < nt) acc[t].mac_i(v[u], xv[u][t]);
+            if (t < nt) acc[t].mac_i(v, ld(xp + t * xcs));
         } else {
 #pragma unroll
           for (int t = 0; t < TC; ++t)
-            if (t < nt) acc[t].mac(v[u], xv[u][t]);
+            if (t < nt) acc[t].mac(v, ld(xp + t * xcs));
         }
       }
     }

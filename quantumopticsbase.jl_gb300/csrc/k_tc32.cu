@@ -17,16 +17,18 @@
 //   Re Y[i, c] = D[2i, c] - D[2i+1, N+c],   Im Y[i, c] = D[2i+1, c] + D[2i, N+c]
 // (in the kernel the imaginary rows of Bhat start at BN / 2, BN = the tile's
 // column count, so N above stands for BN / 2).
-// TF32 keeps 10 explicit mantissa bits; to reach FP32 accuracy each operand is
-// split into a TF32 head and a TF32 tail (x = hi + lo, |lo| <= 2^-11 |x|) and
-// D = Ahi Bhi + Ahi Blo + Alo Bhi (three MMAs per k step; the dropped Alo Blo is
-// below 2^-22 of the product), the split of Ahat done in shared memory as its
-// tiles arrive, the split of Bhat once per call.
+// TF32 keeps 10 explicit mantissa bits, and an MMA of kind tf32 reads an FP32
+// operand as TF32 by dropping its 13 low mantissa bits.  To reach FP32
+// accuracy each operand x is used as its head hi (x itself, read truncated)
+// and its tail lo = x - hi (exact in FP32, |lo| < 2^-10 |x|, read truncated in
+// turn: within 2^-20 |x|), and D = Ahi Bhi + Ahi Blo + Alo Bhi (three MMAs per
+// k step; the dropped Alo Blo is below 2^-20 of the product): about 1e-6
+// relative.  The tails of Ahat are written into shared memory beside each tile
+// as it arrives, those of Bhat once per call.
 //
-// Block (192 threads): warp 0 issues the bulk copies (a 5-, 4- or 3-stage ring
-// of Ahat tiles and Bhat head / tail tiles); warps 2-5 split each Ahat tile
-// into head (in place) and tail, add each k block's accumulator to registers
-// (see k_tc_cgemm), then
+// Block (320 threads): warp 0 issues the bulk copies (a 5-, 4- or 3-stage ring
+// of Ahat tiles and Bhat head / tail tiles); warps 2-9 write each Ahat tile's
+// tail, add each k block's accumulator to registers (see k_tc_cgemm), then
 // run the epilogue; warp 1 owns the tensor memory and one of its threads
 // issues the MMAs (M = 128 rows, N = BN = 2 x kets, K = 8 per instruction).
 // Blocks cover 64 complex rows each and, when that leaves SMs idle, a range of
@@ -46,7 +48,8 @@ namespace {
 
 constexpr int kTcBM = 128;     // rows of Ahat per block (64 complex rows)
 constexpr int kTcBK = 32;      // floats per k block: one 128-byte swizzle span
-constexpr int kTcThreads = 192;
+constexpr int kTcThreads = 320;  // warp 0: copies, warp 1: MMAs, warps 2-9: splits + accumulators
+constexpr int kTcWork = 256;     // threads of warps 2-9
 constexpr unsigned kTcErrTimeout = 1u;
 constexpr int kTcPolls = 1 << 21;
 
@@ -103,10 +106,18 @@ __device__ __forceinline__ void mma_commit(uint64_t* b) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(b))
                : "memory");
 }
-__device__ __forceinline__ float tf32_rn(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
+// x minus its TF32 truncation (the 13 low mantissa bits): the part of x that
+// an MMA reading x as TF32 drops; exact in FP32
+__device__ __forceinline__ float tf32_tail(float x) { return x - __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+// 8 consecutive accumulator columns of this warp's 32 lanes
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 // 16 consecutive accumulator columns of this warp's 32 lanes
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
@@ -127,7 +138,7 @@ struct TcCfg {
   static constexpr int kStages = BN <= 32 ? 5 : (BN <= 64 ? 4 : 3);
   static constexpr int kATile = kTcBM * kTcBK * 4;  // 16 KB
   static constexpr int kBTile = BN * kTcBK * 4;
-  static constexpr int kStage = 2 * kATile + 2 * kBTile;  // A head (in place), A tail, B head, B tail
+  static constexpr int kStage = 2 * kATile + 2 * kBTile;  // A (its head), A tail, B head, B tail
   static constexpr int kTmemCols = 2 * BN;                // two accumulators of BN columns
   static constexpr size_t kSmem = 1024 /* alignment */ + (size_t)kStages * kStage + 256 /* barriers */;
 };
@@ -152,10 +163,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   unsigned char* base = (unsigned char*)(((uintptr_t)tc_smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* bars = reinterpret_cast<uint64_t*>(base + (size_t)S * C::kStage);
   uint64_t* full = bars;           // copies landed            (count 1 + tx)
-  uint64_t* conv = bars + S;       // A tile split             (count 128)
+  uint64_t* conv = bars + S;       // A tail written           (count kTcWork)
   uint64_t* empty = bars + 2 * S;  // MMAs read the stage      (count 1, tcgen05.commit)
   uint64_t* accf = bars + 3 * S;   // [2] accumulator written  (count 1, tcgen05.commit)
-  uint64_t* acce = bars + 3 * S + 2;  // [2] accumulator read  (count 128)
+  uint64_t* acce = bars + 3 * S + 2;  // [2] accumulator read  (count kTcWork)
   uint64_t* fin = bars + 3 * S + 4;   // every MMA issued has completed (count 1, tcgen05.commit)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3 * S + 5);
   int* abort_flag = reinterpret_cast<int*>(bars + 3 * S + 6);
@@ -172,12 +183,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       bar_init(&full[s], 1);
-      bar_init(&conv[s], 128);
+      bar_init(&conv[s], kTcWork);
       bar_init(&empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
       bar_init(&accf[b], 1);
-      bar_init(&acce[b], 128);
+      bar_init(&acce[b], kTcWork);
     }
     bar_init(fin, 1);
     *abort_flag = 0;
@@ -241,14 +252,18 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       mma_commit(fin);  // also after an early exit: fires when every MMA above has completed
     }
   } else {
-    // warps 2-5: split each A tile into head (in place) and tail; after each
-    // k block, add its accumulator (this warp's 32 rows) to registers
+    // warps 2-9: write each A tile's tail; after each k block, add the
+    // accumulator to registers.  Warps w and w + 4 share tensor-memory lanes
+    // 32 * (w % 4) ..; warp half h keeps the kets [h * BN/4, (h + 1) * BN/4):
+    // their real-part columns and, BN/2 further, their imaginary-part columns.
     const int ct = threadIdx.x - 64;
-    const int q4 = warp & 3;  // tensor-memory lanes 32 * q4 .. 32 * q4 + 31
+    const int q4 = warp & 3;
+    const int half = (warp - 2) >> 2;
+    constexpr int KQ = BN / 4;  // kets per warp half
     const uint32_t lane_addr = tmem + ((uint32_t)(q4 * 32) << 16);
-    float acc[BN];
+    float acc_re[KQ], acc_im[KQ];
 #pragma unroll
-    for (int c = 0; c < BN; ++c) acc[c] = 0.f;
+    for (int c = 0; c < KQ; ++c) acc_re[c] = acc_im[c] = 0.f;
     bool ok = true;
     auto drain = [&](int j) {
       const int b = j & 1;
@@ -257,12 +272,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         return;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t col = lane_addr + (uint32_t)(b * BN + half * KQ);
 #pragma unroll
-      for (int c0 = 0; c0 < BN; c0 += 16) {
-        float v[16];
-        tmem_ld16(lane_addr + (uint32_t)(b * BN + c0), v);
+      for (int c0 = 0; c0 < KQ; c0 += 8) {
+        float v[8], w[8];
+        tmem_ld8(col + (uint32_t)c0, v);
+        tmem_ld8(col + (uint32_t)(BN / 2 + c0), w);
 #pragma unroll
-        for (int t = 0; t < 16; ++t) acc[c0 + t] += v[t];
+        for (int t = 0; t < 8; ++t) {
+          acc_re[c0 + t] += v[t];
+          acc_im[c0 + t] += w[t];
+        }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       bar_arrive(&acce[b]);
@@ -273,23 +293,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         ok = false;
         break;
       }
-      float4* a = reinterpret_cast<float4*>(stageA(s));
+      // the MMAs read the raw tile as TF32 (its head, truncated); the tail goes beside it
+      const float4* a = reinterpret_cast<const float4*>(stageA(s));
       float4* al = reinterpret_cast<float4*>(stageAl(s));
 #pragma unroll
-      for (int q = 0; q < C::kATile / 16 / 128; ++q) {
-        const int idx = ct + 128 * q;
+      for (int q = 0; q < C::kATile / 16 / kTcWork; ++q) {
+        const int idx = ct + kTcWork * q;
         const float4 v = a[idx];
-        float4 h, l;
-        h.x = tf32_rn(v.x);
-        h.y = tf32_rn(v.y);
-        h.z = tf32_rn(v.z);
-        h.w = tf32_rn(v.w);
-        l.x = tf32_rn(v.x - h.x);
-        l.y = tf32_rn(v.y - h.y);
-        l.z = tf32_rn(v.z - h.z);
-        l.w = tf32_rn(v.w - h.w);
-        a[idx] = h;
-        al[idx] = l;
+        al[idx] = make_float4(tf32_tail(v.x), tf32_tail(v.y), tf32_tail(v.z), tf32_tail(v.w));
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       bar_arrive(&conv[s]);
@@ -305,10 +316,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const int64_t i = (int64_t)(row0 + r) >> 1;
       const bool even = (lane & 1) == 0;
 #pragma unroll
-      for (int c = 0; c < BN / 2; ++c) {
-        // columns c: real parts of the kets, BN/2 + c: imaginary parts
-        const float other = __shfl_xor_sync(0xffffffffu, acc[BN / 2 + c], 1);
-        const float v = even ? acc[c] - other : acc[c] + other;  // even lane: Re Y, odd lane: Im Y
+      for (int t = 0; t < KQ; ++t) {
+        const int c = half * KQ + t;
+        const float other = __shfl_xor_sync(0xffffffffu, acc_im[t], 1);
+        const float v = even ? acc_re[t] - other : acc_re[t] + other;  // even lane: Re Y, odd lane: Im Y
         const float w = __shfl_xor_sync(0xffffffffu, v, 1);
         if (even && i < m && c < N) {
           if (part) {
@@ -339,7 +350,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 }
 
 // Bhat head and tail: row j = Re X[:, j], row H + j = Im X[:, j] (j < the
-// kets, H = half the tile's BN columns), TF32-split, as swizzled tiles of BN
+// kets, H = half the tile's BN columns), value and TF32 tail, as swizzled tiles of BN
 // rows x 32 floats, one per k block (zero beyond n).
 __global__ void k_tc_split_b(const float2* __restrict__ x, int64_t n, int64_t xes, int64_t xcs, int BN, int64_t nkb,
                              float* __restrict__ bh, float* __restrict__ bl) {
@@ -348,14 +359,13 @@ __global__ void k_tc_split_b(const float2* __restrict__ x, int64_t n, int64_t xe
   if (k >= nkb * kTcBK) return;
   float2 v = make_float2(0.f, 0.f);
   if (k < n) v = x[k * xes + (int64_t)j * xcs];
-  const float hr = tf32_rn(v.x), hi = tf32_rn(v.y);
   const int64_t tile = (k / kTcBK) * (int64_t)BN * kTcBK;
   const int kk = (int)(k % kTcBK);
   const int64_t o_re = tile + swz(j, kk), o_im = tile + swz(BN / 2 + j, kk);
-  bh[o_re] = hr;
-  bl[o_re] = tf32_rn(v.x - hr);
-  bh[o_im] = hi;
-  bl[o_im] = tf32_rn(v.y - hi);
+  bh[o_re] = v.x;  // read as TF32 by the MMA: its truncated head
+  bl[o_re] = tf32_tail(v.x);
+  bh[o_im] = v.y;
+  bl[o_im] = tf32_tail(v.y);
 }
 
 // y[i, c] = alpha * (sum of the k ranges' partial products, in order) + beta * y[i, c]
