@@ -139,19 +139,22 @@ struct TcCfg {
   static constexpr int kATile = kTcBM * kTcBK * 4;  // 16 KB
   static constexpr int kBTile = BN * kTcBK * 4;
   static constexpr int kStage = 2 * kATile + 2 * kBTile;  // A (its head), A tail, B head, B tail
-  static constexpr int kTmemCols = 2 * BN;                // two accumulators of BN columns
+  static constexpr int kAcc = 4;                          // accumulators of BN columns, used in turn
+  static constexpr int kGroup = 2;                        // k blocks summed in one accumulator
+  static constexpr int kTmemCols = kAcc * BN;
   static constexpr size_t kSmem = 1024 /* alignment */ + (size_t)kStages * kStage + 256 /* barriers */;
 };
 
 // Y[i, c] (complex rows i < m, kets c < N) = alpha * (Ahat Bhat^T combined) + beta * Y,
 // or the block's partial product into part[kz][c][i] when part != null.
 //
-// Accumulation: each k block (32 terms, twelve MMAs) starts a fresh
-// accumulator in tensor memory, two of them used in turn; the split warps read
-// the finished one and add it to FP32 registers, rounding to nearest.  The
-// tensor cores' own accumulation (which does not round to nearest) then spans
-// 32 terms only, which keeps the FP32 accuracy of the ComplexF32 mode for long
-// rows (the error no longer grows with n).
+// Accumulation: each group of kGroup k blocks (64 terms, 24 MMAs) starts a
+// fresh accumulator in tensor memory, kAcc of them used in turn; the split
+// warps read each finished one and add it to FP32 registers, rounding to
+// nearest.  The tensor cores' own accumulation (which does not round to
+// nearest) then spans 64 terms only, which keeps the FP32 accuracy of the
+// ComplexF32 mode for long rows (the error no longer grows with n), and the
+// MMAs of group q + kAcc wait only for the registers to take group q.
 template <int BN>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_tc_cgemm(const float* __restrict__ ahat, const float* __restrict__ bh_t, const float* __restrict__ bl_t,
@@ -165,11 +168,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint64_t* full = bars;           // copies landed            (count 1 + tx)
   uint64_t* conv = bars + S;       // A tail written           (count kTcWork)
   uint64_t* empty = bars + 2 * S;  // MMAs read the stage      (count 1, tcgen05.commit)
-  uint64_t* accf = bars + 3 * S;   // [2] accumulator written  (count 1, tcgen05.commit)
-  uint64_t* acce = bars + 3 * S + 2;  // [2] accumulator read  (count kTcWork)
-  uint64_t* fin = bars + 3 * S + 4;   // every MMA issued has completed (count 1, tcgen05.commit)
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3 * S + 5);
-  int* abort_flag = reinterpret_cast<int*>(bars + 3 * S + 6);
+  constexpr int NA = C::kAcc, G = C::kGroup;
+  uint64_t* accf = bars + 3 * S;       // [NA] accumulator written (count 1, tcgen05.commit)
+  uint64_t* acce = bars + 3 * S + NA;  // [NA] accumulator read    (count kTcWork)
+  uint64_t* fin = bars + 3 * S + 2 * NA;  // every MMA issued has completed (count 1, tcgen05.commit)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3 * S + 2 * NA + 1);
+  int* abort_flag = reinterpret_cast<int*>(bars + 3 * S + 2 * NA + 2);
   auto stageA = [&](int s) { return base + (size_t)s * C::kStage; };
   auto stageAl = [&](int s) { return base + (size_t)s * C::kStage + C::kATile; };
   auto stageBh = [&](int s) { return base + (size_t)s * C::kStage + 2 * C::kATile; };
@@ -186,7 +190,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       bar_init(&conv[s], kTcWork);
       bar_init(&empty[s], 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < NA; ++b) {
       bar_init(&accf[b], 1);
       bar_init(&acce[b], kTcWork);
     }
@@ -230,8 +234,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       // kind::tf32, FP32 accumulator, A and B K-major, N = BN, M = 128
       const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kTcBM >> 4) << 24);
       for (int it = 0; it < nk; ++it) {
-        const int s = it % S, b = it & 1;
-        if (!bar_wait(&conv[s], (it / S) & 1) || (it >= 2 && !bar_wait(&acce[b], ((it >> 1) - 1) & 1))) {
+        const int s = it % S, q = it / G, b = q % NA;
+        const bool first = it % G == 0, last = it % G == G - 1 || it == nk - 1;
+        if (!bar_wait(&conv[s], (it / S) & 1) || (first && q >= NA && !bar_wait(&acce[b], ((q / NA) - 1) & 1))) {
           atomicExch(abort_flag, 1);
           break;
         }
@@ -242,12 +247,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
         for (int kk = 0; kk < kTcBK / 8; ++kk) {  // 8 TF32 = 32 bytes = 2 descriptor units per step
           const uint64_t o = (uint64_t)(2 * kk);
-          mma_tf32(d, ah + o, bh + o, idesc, kk > 0 ? 1u : 0u);
+          mma_tf32(d, ah + o, bh + o, idesc, (kk > 0 || !first) ? 1u : 0u);
           mma_tf32(d, ah + o, bl + o, idesc, 1u);
           mma_tf32(d, al + o, bh + o, idesc, 1u);
         }
         mma_commit(&empty[s]);
-        mma_commit(&accf[b]);
+        if (last) mma_commit(&accf[b]);
       }
       mma_commit(fin);  // also after an early exit: fires when every MMA above has completed
     }
@@ -265,9 +270,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
     for (int c = 0; c < KQ; ++c) acc_re[c] = acc_im[c] = 0.f;
     bool ok = true;
-    auto drain = [&](int j) {
-      const int b = j & 1;
-      if (!__all_sync(0xffffffffu, bar_wait(&accf[b], (j >> 1) & 1) && !*(volatile int*)abort_flag)) {
+    auto drain = [&](int q) {  // accumulator of k-block group q
+      const int b = q % NA;
+      if (!__all_sync(0xffffffffu, bar_wait(&accf[b], (q / NA) & 1) && !*(volatile int*)abort_flag)) {
         ok = false;
         return;
       }
@@ -304,9 +309,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       bar_arrive(&conv[s]);
-      if (it >= 1) drain(it - 1);
+      if (it % G == 0 && it >= G) drain(it / G - 1);  // the previous group, once this one has begun
     }
-    if (ok) drain(nk - 1);
+    if (ok) drain((nk - 1) / G);  // the last group (the one before it was drained in the loop)
     ok = __all_sync(0xffffffffu, ok && !*(volatile int*)abort_flag);
     if (!ok) {
       atomicExch(abort_flag, 1);
