@@ -49,6 +49,10 @@ SEED_H = 3
 ORACLE_BUILD = ("oracle/liboref.so, g++ -O3 -ffp-contract=off: every multiply and add rounded separately, as the "
                 "reference's Julia code computes; portable flags (no -march=native), the same binary that checks "
                 "parity")
+# GB300's FP64 pipe: 2 DFMA lanes per SM clock (ncu's peak_sustained for
+# sm__sass_thread_inst_executed_op_dfma_pred_on; the dense ComplexF64 product
+# sustains 1.96 of them)
+FP64_LANES_PER_SM_CLOCK = 2
 L2_NOTE = "20 distinct 64-ket batches rotate: 640 MiB (c128) / 320 MiB (c64) of in+out per rotation, > 2x the 129 MB L2"
 
 
@@ -467,12 +471,21 @@ def run_own(args, rank, world, local_rank):
     peak, peak_src = (peaks["hbm_gbs"], "measured") if peaks and "hbm_gbs" in peaks else (6800.0, "fallback")
     prof = read_json(os.path.join(ROOT, "profiles", "gather_heisenberg14_batch64.json")) or {}
     fp64 = None
+    clocks = sampler.summary(*win64) if sampler else None
     if prof.get("dfma_per_launch"):
         fp64_rate = 2.0 * prof["dfma_per_launch"] / t_launch / 1e12
-        fp64_peak = peaks_live["fp64_fma_tflops"]
+        sm_mhz = (clocks or {}).get("sm_mhz") or peaks_live["fp64_probe_sm_mhz"]
+        fp64_peak = fp64_pipe_tflops(peaks_live["sms"], sm_mhz)
         fp64 = {"bound": "fp64 FMA pipe", "achieved": fp64_rate, "peak": fp64_peak,
                 "unit": "TFLOP/s (executed DFMA + DMUL thread instructions x 2, from the ncu capture)",
-                "frac": fp64_rate / fp64_peak, "peak_source": "qob_probe_peak in this run (FMA chains)",
+                "frac": fp64_rate / fp64_peak,
+                "peak_source": (f"{FP64_LANES_PER_SM_CLOCK} FP64 lanes per SM clock x 2 flops x {peaks_live['sms']} SMs "
+                                f"x the {sm_mhz:.0f} MHz SM clock sampled during the timed steps"),
+                "probe": {"tflops": peaks_live["fp64_fma_tflops"],
+                          "lanes_per_sm_clock": peaks_live["fp64_fma_lanes_per_sm_clock"],
+                          "frac_of_probe": fp64_rate / peaks_live["fp64_fma_tflops"],
+                          "note": "qob_probe_peak_ex: chains of FMAs reach 1.68 of the 2 lanes per clock; the "
+                                  "dense ComplexF64 product reaches 1.96, so the pipe's 2 is the denominator"},
                 "fp64_ops_per_launch": prof["dfma_per_launch"]}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -516,7 +529,7 @@ def run_own(args, rank, world, local_rank):
         "served": served,
         "peaks_live": peaks_live,
         "e2e": e2e,
-        "clocks": sampler.summary(*win64) if sampler else None,
+        "clocks": clocks,
     }
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(H, args.cpu_seconds)
@@ -538,18 +551,28 @@ def probe_peaks(dev):
     probe (qob_probe_peak), measured in this run."""
     import ctypes as C
 
+    import torch
     from qobgpu import _lib as L
     from qobgpu.device import get_context, raise_for
 
     ctx = get_context(dev)
-    out = {}
-    for which, name in ((0, "fp64_fma_tflops"), (1, "fp32_fma_tflops")):
-        r = C.c_double()
-        raise_for(L.lib().qob_probe_peak(ctx.ptr, which, C.byref(r)), ctx)
-        out[name] = r.value
-    out["how"] = ("qob_probe_peak: 16 independent FMA chains per thread, (SMs x 8) blocks of 256 threads, "
-                  "one untimed launch, best of three timed (CUDA events)")
+    out = {"sms": torch.cuda.get_device_properties(dev).multi_processor_count}
+    for which, name in ((0, "fp64"), (1, "fp32")):
+        r, lanes, mhz = C.c_double(), C.c_double(), C.c_double()
+        raise_for(L.lib().qob_probe_peak_ex(ctx.ptr, which, C.byref(r), C.byref(lanes), C.byref(mhz)), ctx)
+        out[name + "_fma_tflops"] = r.value
+        out[name + "_fma_lanes_per_sm_clock"] = lanes.value
+        out[name + "_probe_sm_mhz"] = mhz.value
+    out["how"] = ("qob_probe_peak_ex: 16 independent FMA chains per thread, one full wave of 256-thread blocks, "
+                  "one untimed launch, best of three timed (CUDA events); lanes per SM clock from each SM's "
+                  "cycle counter over its blocks, and the SM clock of that launch")
     return out
+
+
+def fp64_pipe_tflops(sms, sm_mhz):
+    """The FP64 pipe's rate at the SM clock a kernel ran at: FMA lanes per SM
+    clock x 2 flops x SMs x clock."""
+    return FP64_LANES_PER_SM_CLOCK * 2 * sms * sm_mhz * 1e6 / 1e12
 
 
 def oracle_errors(lib, ctx, hd, H, dim, stream):

@@ -77,11 +77,19 @@ int64_t qob_kernel_launches(void);
 
 /* Diagnostics: the device's fused multiply-add rate in TFLOP/s (2 flops per
  * FMA), which = 0 for FP64, 1 for FP32, measured with 16 independent chains of
- * FMAs per thread over (SMs x 8) blocks of 256 threads (one untimed launch, the
- * best of three timed with CUDA events; a few ms).  The roofline fraction of an FP64-bound
- * kernel is taken against this number.  No counterpart in the reference.
- * Synchronous; allocates and frees 8 bytes of device memory. */
+ * FMAs per thread over one full wave of 256-thread blocks (SMs x the blocks the
+ * occupancy calculator admits per SM; one untimed launch, the best of three
+ * timed with CUDA events; a few ms).  No counterpart in the reference.
+ * Synchronous; allocates and frees a few KB of device memory. */
 int qob_probe_peak(qob_ctx* ctx, int which, double* tflops);
+
+/* qob_probe_peak with two more figures of the same best launch (either pointer
+ * may be NULL): lanes_per_clock = FMA lanes per SM clock (per SM: the FMAs of
+ * its blocks over the span of the SM's cycle counter, median over the SMs),
+ * independent of the clock the launch ran at; sm_mhz = the SM clock of that
+ * launch (the longest SM span in cycles over the event time).  The roofline of
+ * an FP64-bound kernel is lanes_per_clock x 2 x SMs x the SM clock it ran at. */
+int qob_probe_peak_ex(qob_ctx* ctx, int which, double* tflops, double* lanes_per_clock, double* sm_mhz);
 
 /* Context on one CUDA device.  flags: reserved, pass 0. */
 int qob_create(qob_ctx** ctx, int device, unsigned flags);

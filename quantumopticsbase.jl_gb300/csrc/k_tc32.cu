@@ -21,21 +21,24 @@
 // operand as TF32 by dropping its 13 low mantissa bits.  To reach FP32
 // accuracy each operand x is used as its head hi (x itself, read truncated)
 // and its tail lo = x - hi (exact in FP32, |lo| < 2^-10 |x|, read truncated in
-// turn: within 2^-20 |x|), and D = Ahi Bhi + Ahi Blo + Alo Bhi (three MMAs per
-// k step; the dropped Alo Blo is below 2^-20 of the product): about 1e-6
-// relative.  The tails of Ahat are written into shared memory beside each tile
-// as it arrives, those of Bhat once per call.
+// turn: within 2^-20 |x|), and D = Ahi Bhi + Ahi Blo + Alo Bhi (three products
+// per k step, two MMAs when B's head and tail tiles are one operand of twice
+// the columns; the dropped Alo Blo is below 2^-20 of the product): about 1e-6
+// relative.  Each Ahat tile is moved from shared memory into tensor memory
+// as it arrives, value and tail side by side, and the MMAs read A from there;
+// the tails of Bhat are made once per call, beside its values.
 //
-// Block (320 threads): warp 0 issues the bulk copies (a 5-, 4- or 3-stage ring
-// of Ahat tiles and Bhat head / tail tiles); warps 2-9 write each Ahat tile's
-// tail, add each k block's accumulator to registers (see k_tc_cgemm), then
+// Block (320 threads): warp 0 issues the bulk copies (a ring of Ahat tiles and
+// a ring of Bhat head / tail tiles); warps 2-9 move each Ahat tile into tensor
+// memory, add each group's accumulator to registers (see k_tc_cgemm), then
 // run the epilogue; warp 1 owns the tensor memory and one of its threads
-// issues the MMAs (M = 128 rows, N = BN = 2 x kets, K = 8 per instruction).
+// issues the MMAs (M = 128 rows, N = BN or 2 x BN, K = 8 per instruction).
 // Blocks cover 64 complex rows each and, when that leaves SMs idle, a range of
 // k blocks whose partial products k_tc_reduce adds in order; the grid is one
-// wave (one block per SM by its shared memory).  Every wait is
-// bounded: a wait that gives up records kTcErrTimeout in the status word, the
-// block drains its copies and MMAs, frees its tensor memory and returns.
+// wave (one block per SM by its shared memory, which also gives each block
+// the SM's whole tensor memory).  Every wait is bounded: a wait that gives up
+// records kTcErrTimeout in the status word, the block drains its copies and
+// MMAs, frees its tensor memory and returns.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -50,6 +53,7 @@ constexpr int kTcBM = 128;     // rows of Ahat per block (64 complex rows)
 constexpr int kTcBK = 32;      // floats per k block: one 128-byte swizzle span
 constexpr int kTcThreads = 320;  // warp 0: copies, warp 1: MMAs, warps 2-9: splits + accumulators
 constexpr int kTcWork = 256;     // threads of warps 2-9
+constexpr int kTcTmemCols = 512;  // the whole tensor memory of the SM (one block per SM)
 constexpr unsigned kTcErrTimeout = 1u;
 constexpr int kTcPolls = 1 << 21;
 
@@ -95,11 +99,13 @@ __device__ __forceinline__ uint64_t sw128_desc(const void* tile) {
   const uint64_t a = (saddr(tile) & 0x3FFFFu) >> 4;
   return a | (uint64_t(1) << 16) | (uint64_t(1024 >> 4) << 32) | (uint64_t(1) << 46) | (uint64_t(2) << 61);
 }
-__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+// D (tensor memory) += A B^T with A read from tensor memory (a_tmem: the column
+// of A's first K element, lane 0) and B from shared memory (descriptor bd)
+__device__ __forceinline__ void mma_tf32_ts(uint32_t tmem, uint32_t a_tmem, uint64_t bd, uint32_t idesc, uint32_t acc) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem),
+      "r"(a_tmem), "l"(bd), "r"(idesc), "r"(acc)
       : "memory");
 }
 __device__ __forceinline__ void mma_commit(uint64_t* b) {
@@ -119,65 +125,77 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
 #pragma unroll
   for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
-// 16 consecutive accumulator columns of this warp's 32 lanes
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
+// 16 consecutive columns of this warp's 32 lanes from registers (completion: tcgen05.wait::st)
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
-      "[%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16};" ::"r"(taddr),
+      "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+      "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+      "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+      "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15]))
+      : "memory");
 }
-
 template <int BN>
 struct TcCfg {
-  static constexpr int kStages = BN <= 32 ? 5 : (BN <= 64 ? 4 : 3);
-  static constexpr int kATile = kTcBM * kTcBK * 4;  // 16 KB
+  // head x [B head | B tail] as one MMA of N = 2 BN (the MMA's time is flat up
+  // to N = 64: about 55 cycles for M = 128, K = 8), the tail product beside it
+  static constexpr bool kMerge = BN <= 64;
+  static constexpr int kAccCols = kMerge ? 2 * BN : BN;  // columns of one accumulator
+  static constexpr int kAcc = BN <= 32 ? 4 : 2;          // accumulators, used in turn
+  static constexpr int kGroup = 2;                       // k blocks summed in one accumulator
+  static constexpr int kSlots = 4;                       // B stages = tensor-memory A slots
+  static constexpr int kSlotCol0 = kAcc * kAccCols;      // first column of the A slots (64 each)
+  static constexpr int kATile = kTcBM * kTcBK * 4;       // 16 KB
   static constexpr int kBTile = BN * kTcBK * 4;
-  static constexpr int kStage = 2 * kATile + 2 * kBTile;  // A (its head), A tail, B head, B tail
-  static constexpr int kAcc = 4;                          // accumulators of BN columns, used in turn
-  static constexpr int kGroup = 2;                        // k blocks summed in one accumulator
-  static constexpr int kTmemCols = kAcc * BN;
-  static constexpr size_t kSmem = 1024 /* alignment */ + (size_t)kStages * kStage + 256 /* barriers */;
+  static constexpr int kBStage = 2 * kBTile;             // B head tile, then B tail tile
+  static constexpr int kAStages = BN <= 32 ? 10 : (BN <= 64 ? 8 : 5);
+  static constexpr int kBarBytes = 512;
+  static constexpr size_t kSmem = 1024 /* alignment */ + (size_t)kAStages * kATile + (size_t)kSlots * kBStage + kBarBytes;
+  static_assert(kSlotCol0 + 64 * kSlots <= kTcTmemCols, "tensor-memory budget");
+  static_assert(8 * (2 * kAStages + 3 * kSlots + 2 * kAcc + 1) + 8 <= kBarBytes, "barrier area");
+  static_assert(kSmem <= 227 * 1024, "shared-memory budget");
 };
 
 // Y[i, c] (complex rows i < m, kets c < N) = alpha * (Ahat Bhat^T combined) + beta * Y,
 // or the block's partial product into part[kz][c][i] when part != null.
 //
-// Accumulation: each group of kGroup k blocks (64 terms, 24 MMAs) starts a
-// fresh accumulator in tensor memory, kAcc of them used in turn; the split
-// warps read each finished one and add it to FP32 registers, rounding to
-// nearest.  The tensor cores' own accumulation (which does not round to
-// nearest) then spans 64 terms only, which keeps the FP32 accuracy of the
-// ComplexF32 mode for long rows (the error no longer grows with n), and the
-// MMAs of group q + kAcc wait only for the registers to take group q.
+// Pipeline.  Ahat tiles arrive in a ring of kAStages shared-memory stages; the
+// split warps copy each into a tensor-memory slot (its value, read by the MMA
+// as the TF32 head, and its tail: 32 + 32 columns) and release the stage at
+// once, so that ring turns over at the speed of the copies, not of the MMAs.
+// The Bhat tiles of a k block and the tensor-memory slot share an index in a
+// second ring of kSlots, released by the MMAs' commit.  The MMAs read A from
+// tensor memory and B from shared memory.
+//
+// Accumulation: each group of kGroup k blocks (64 terms) starts a fresh
+// accumulator in tensor memory, kAcc of them used in turn; the split warps
+// read each finished one and add it to FP32 registers, rounding to nearest.
+// The tensor cores' own accumulation (which does not round to nearest) then
+// spans 64 terms only, which keeps the FP32 accuracy of the ComplexF32 mode
+// for long rows (the error does not grow with n).
 template <int BN>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_tc_cgemm(const float* __restrict__ ahat, const float* __restrict__ bh_t, const float* __restrict__ bl_t,
                int64_t m, int N, int nkb, int kb_per, float2* y, int64_t yes, int64_t ycs, float2 alpha, float2 beta,
                float2* part, unsigned* status) {
   using C = TcCfg<BN>;
-  constexpr int S = C::kStages;
+  constexpr int SA = C::kAStages, K = C::kSlots, NA = C::kAcc, G = C::kGroup;
   extern __shared__ __align__(16) unsigned char tc_smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)tc_smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(base + (size_t)S * C::kStage);
-  uint64_t* full = bars;           // copies landed            (count 1 + tx)
-  uint64_t* conv = bars + S;       // A tail written           (count kTcWork)
-  uint64_t* empty = bars + 2 * S;  // MMAs read the stage      (count 1, tcgen05.commit)
-  constexpr int NA = C::kAcc, G = C::kGroup;
-  uint64_t* accf = bars + 3 * S;       // [NA] accumulator written (count 1, tcgen05.commit)
-  uint64_t* acce = bars + 3 * S + NA;  // [NA] accumulator read    (count kTcWork)
-  uint64_t* fin = bars + 3 * S + 2 * NA;  // every MMA issued has completed (count 1, tcgen05.commit)
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3 * S + 2 * NA + 1);
-  int* abort_flag = reinterpret_cast<int*>(bars + 3 * S + 2 * NA + 2);
-  auto stageA = [&](int s) { return base + (size_t)s * C::kStage; };
-  auto stageAl = [&](int s) { return base + (size_t)s * C::kStage + C::kATile; };
-  auto stageBh = [&](int s) { return base + (size_t)s * C::kStage + 2 * C::kATile; };
-  auto stageBl = [&](int s) { return base + (size_t)s * C::kStage + 2 * C::kATile + C::kBTile; };
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + (size_t)SA * C::kATile + (size_t)K * C::kBStage);
+  uint64_t* afull = bars;                            // [SA] A tile landed          (count 1 + tx)
+  uint64_t* aempty = afull + SA;                     // [SA] A tile read            (count kTcWork)
+  uint64_t* bfull = aempty + SA;                     // [K] B tiles landed          (count 1 + tx)
+  uint64_t* conv = bfull + K;                        // [K] A slot written          (count kTcWork)
+  uint64_t* done = conv + K;                         // [K] MMAs of the slot done   (count 1, tcgen05.commit)
+  uint64_t* accf = done + K;                         // [NA] accumulator written    (count 1, tcgen05.commit)
+  uint64_t* acce = accf + NA;                        // [NA] accumulator read       (count kTcWork)
+  uint64_t* fin = acce + NA;                         // every MMA issued has completed (count 1, tcgen05.commit)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(fin + 1);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+  auto stageA = [&](int s) { return base + (size_t)s * C::kATile; };
+  auto stageB = [&](int t) { return base + (size_t)SA * C::kATile + (size_t)t * C::kBStage; };
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int kb0 = blockIdx.y * kb_per;
@@ -185,10 +203,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int row0 = blockIdx.x * kTcBM;    // first Ahat row of this block
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < S; ++s) {
-      bar_init(&full[s], 1);
-      bar_init(&conv[s], kTcWork);
-      bar_init(&empty[s], 1);
+    for (int s = 0; s < SA; ++s) {
+      bar_init(&afull[s], 1);
+      bar_init(&aempty[s], kTcWork);
+    }
+    for (int t = 0; t < K; ++t) {
+      bar_init(&bfull[t], 1);
+      bar_init(&conv[t], kTcWork);
+      bar_init(&done[t], 1);
     }
     for (int b = 0; b < NA; ++b) {
       bar_init(&accf[b], 1);
@@ -200,7 +222,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(tmem_slot)),
-                 "r"(C::kTmemCols)
+                 "r"(kTcTmemCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -211,61 +233,79 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
   if (warp == 0) {
     if (lane == 0) {  // producer
-      int issued = 0;
+      int issued_a = 0, issued_b = 0;
       for (int it = 0; it < nk; ++it) {
-        const int s = it % S;
-        if (it >= S && !bar_wait(&empty[s], ((it / S) - 1) & 1)) {
+        const int s = it % SA, t = it % K;
+        const int kb = kb0 + it;
+        if (it >= SA && !bar_wait(&aempty[s], ((it / SA) - 1) & 1)) {
           atomicExch(abort_flag, 1);
           break;
         }
         if (*(volatile int*)abort_flag) break;
-        bar_expect(&full[s], 2 * C::kBTile + C::kATile);
-        const int kb = kb0 + it;
-        bulk_copy(stageA(s), ahat + ((int64_t)blockIdx.x * nkb + kb) * (C::kATile / 4), C::kATile, &full[s]);
-        bulk_copy(stageBh(s), bh_t + (int64_t)kb * (C::kBTile / 4), C::kBTile, &full[s]);
-        bulk_copy(stageBl(s), bl_t + (int64_t)kb * (C::kBTile / 4), C::kBTile, &full[s]);
-        issued = it + 1;
+        bar_expect(&afull[s], C::kATile);
+        bulk_copy(stageA(s), ahat + ((int64_t)blockIdx.x * nkb + kb) * (C::kATile / 4), C::kATile, &afull[s]);
+        issued_a = it + 1;
+        if (it >= K && !bar_wait(&done[t], ((it / K) - 1) & 1)) {
+          atomicExch(abort_flag, 1);
+          break;
+        }
+        bar_expect(&bfull[t], C::kBStage);
+        bulk_copy(stageB(t), bh_t + (int64_t)kb * (C::kBTile / 4), C::kBTile, &bfull[t]);
+        bulk_copy(stageB(t) + C::kBTile, bl_t + (int64_t)kb * (C::kBTile / 4), C::kBTile, &bfull[t]);
+        issued_b = it + 1;
       }
       // every copy issued has landed before the block's shared memory goes away
-      for (int it = max(0, issued - S); it < issued; ++it) bar_wait(&full[it % S], (it / S) & 1);
+      for (int it = max(0, issued_a - SA); it < issued_a; ++it) bar_wait(&afull[it % SA], (it / SA) & 1);
+      for (int it = max(0, issued_b - K); it < issued_b; ++it) bar_wait(&bfull[it % K], (it / K) & 1);
     }
   } else if (warp == 1) {
     if (lane == 0) {  // MMA issuer
-      // kind::tf32, FP32 accumulator, A and B K-major, N = BN, M = 128
-      const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kTcBM >> 4) << 24);
+      // kind::tf32, FP32 accumulator, A (tensor memory) and B K-major, M = 128, N = BN or 2 BN
+      const uint32_t idesc1 = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kTcBM >> 4) << 24);
+      const uint32_t idesc2 = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)((2 * BN) >> 3) << 17) | ((uint32_t)(kTcBM >> 4) << 24);
       for (int it = 0; it < nk; ++it) {
-        const int s = it % S, q = it / G, b = q % NA;
+        const int t = it % K, q = it / G, b = q % NA;
         const bool first = it % G == 0, last = it % G == G - 1 || it == nk - 1;
-        if (!bar_wait(&conv[s], (it / S) & 1) || (first && q >= NA && !bar_wait(&acce[b], ((q / NA) - 1) & 1))) {
+        if (!bar_wait(&conv[t], (it / K) & 1) || !bar_wait(&bfull[t], (it / K) & 1) ||
+            (first && q >= NA && !bar_wait(&acce[b], ((q / NA) - 1) & 1))) {
           atomicExch(abort_flag, 1);
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t d = tmem + (uint32_t)(b * BN);
-        const uint64_t ah = sw128_desc(stageA(s)), al = sw128_desc(stageAl(s));
-        const uint64_t bh = sw128_desc(stageBh(s)), bl = sw128_desc(stageBl(s));
+        const uint32_t d = tmem + (uint32_t)(b * C::kAccCols);
+        const uint32_t ta = tmem + (uint32_t)(C::kSlotCol0 + t * 64);  // head columns; the tail 32 further
+        const uint64_t bh = sw128_desc(stageB(t)), bl = sw128_desc(stageB(t) + C::kBTile);
 #pragma unroll
         for (int kk = 0; kk < kTcBK / 8; ++kk) {  // 8 TF32 = 32 bytes = 2 descriptor units per step
           const uint64_t o = (uint64_t)(2 * kk);
-          mma_tf32(d, ah + o, bh + o, idesc, (kk > 0 || !first) ? 1u : 0u);
-          mma_tf32(d, ah + o, bl + o, idesc, 1u);
-          mma_tf32(d, al + o, bh + o, idesc, 1u);
+          const uint32_t a_hi = ta + (uint32_t)(8 * kk), a_lo = a_hi + 32;
+          const uint32_t acc = (kk > 0 || !first) ? 1u : 0u;
+          if (C::kMerge) {
+            mma_tf32_ts(d, a_hi, bh + o, idesc2, acc);  // head x [B head | B tail]: columns [0, 2 BN)
+            mma_tf32_ts(d, a_lo, bh + o, idesc1, 1u);   // tail x B head: columns [0, BN)
+          } else {
+            mma_tf32_ts(d, a_hi, bh + o, idesc1, acc);
+            mma_tf32_ts(d, a_hi, bl + o, idesc1, 1u);
+            mma_tf32_ts(d, a_lo, bh + o, idesc1, 1u);
+          }
         }
-        mma_commit(&empty[s]);
+        mma_commit(&done[t]);
         if (last) mma_commit(&accf[b]);
       }
       mma_commit(fin);  // also after an early exit: fires when every MMA above has completed
     }
   } else {
-    // warps 2-9: write each A tile's tail; after each k block, add the
-    // accumulator to registers.  Warps w and w + 4 share tensor-memory lanes
-    // 32 * (w % 4) ..; warp half h keeps the kets [h * BN/4, (h + 1) * BN/4):
-    // their real-part columns and, BN/2 further, their imaginary-part columns.
-    const int ct = threadIdx.x - 64;
+    // warps 2-9: move each A tile into tensor memory (value and tail); after
+    // each group, add the accumulator to registers.  Warps w and w + 4 share
+    // tensor-memory lanes 32 * (w % 4) .. (the A rows of those lanes): warp
+    // half h moves the tile's columns [16 h, 16 h + 16) and keeps the kets
+    // [h * BN/4, (h + 1) * BN/4): their real-part columns and, BN/2 further,
+    // their imaginary-part columns.
     const int q4 = warp & 3;
     const int half = (warp - 2) >> 2;
     constexpr int KQ = BN / 4;  // kets per warp half
     const uint32_t lane_addr = tmem + ((uint32_t)(q4 * 32) << 16);
+    const int r = q4 * 32 + lane;  // A row of this thread = its tensor-memory lane
     float acc_re[KQ], acc_im[KQ];
 #pragma unroll
     for (int c = 0; c < KQ; ++c) acc_re[c] = acc_im[c] = 0.f;
@@ -277,38 +317,62 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         return;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t col = lane_addr + (uint32_t)(b * BN + half * KQ);
+      const uint32_t col = lane_addr + (uint32_t)(b * C::kAccCols + half * KQ);
 #pragma unroll
       for (int c0 = 0; c0 < KQ; c0 += 8) {
         float v[8], w[8];
         tmem_ld8(col + (uint32_t)c0, v);
         tmem_ld8(col + (uint32_t)(BN / 2 + c0), w);
+        if (C::kMerge) {
+          float v2[8], w2[8];
+          tmem_ld8(col + (uint32_t)(BN + c0), v2);
+          tmem_ld8(col + (uint32_t)(BN + BN / 2 + c0), w2);
 #pragma unroll
-        for (int t = 0; t < 8; ++t) {
-          acc_re[c0 + t] += v[t];
-          acc_im[c0 + t] += w[t];
+          for (int u = 0; u < 8; ++u) {
+            v[u] += v2[u];
+            w[u] += w2[u];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          acc_re[c0 + u] += v[u];
+          acc_im[c0 + u] += w[u];
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       bar_arrive(&acce[b]);
     };
     for (int it = 0; it < nk && ok; ++it) {
-      const int s = it % S;
-      if (*(volatile int*)abort_flag || !bar_wait(&full[s], (it / S) & 1)) {
+      const int s = it % SA, t = it % K;
+      // warp-uniform, as the tensor-memory stores below need the whole warp
+      if (!__all_sync(0xffffffffu, !*(volatile int*)abort_flag && bar_wait(&afull[s], (it / SA) & 1) &&
+                                       (it < K || bar_wait(&done[t], ((it / K) - 1) & 1)))) {
         ok = false;
         break;
       }
-      // the MMAs read the raw tile as TF32 (its head, truncated); the tail goes beside it
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // row r, columns [16 half, 16 half + 16): 16-byte chunks 4 half + j of
+      // the swizzled row (chunk c at position c ^ (r mod 8))
       const float4* a = reinterpret_cast<const float4*>(stageA(s));
-      float4* al = reinterpret_cast<float4*>(stageAl(s));
+      float hv[16], tv[16];
 #pragma unroll
-      for (int q = 0; q < C::kATile / 16 / kTcWork; ++q) {
-        const int idx = ct + kTcWork * q;
-        const float4 v = a[idx];
-        al[idx] = make_float4(tf32_tail(v.x), tf32_tail(v.y), tf32_tail(v.z), tf32_tail(v.w));
+      for (int j = 0; j < 4; ++j) {
+        const float4 x = a[r * 8 + ((4 * half + j) ^ (r & 7))];
+        hv[4 * j] = x.x;
+        hv[4 * j + 1] = x.y;
+        hv[4 * j + 2] = x.z;
+        hv[4 * j + 3] = x.w;
       }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      bar_arrive(&conv[s]);
+      bar_arrive(&aempty[s]);  // the stage may be refilled
+#pragma unroll
+      for (int j = 0; j < 16; ++j) tv[j] = tf32_tail(hv[j]);
+      // the MMAs read the value as TF32 (its head, truncated); the tail 32 columns further
+      const uint32_t ta = lane_addr + (uint32_t)(C::kSlotCol0 + t * 64 + 16 * half);
+      tmem_st16(ta, hv);
+      tmem_st16(ta + 32, tv);
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      bar_arrive(&conv[t]);
       if (it % G == 0 && it >= G) drain(it / G - 1);  // the previous group, once this one has begun
     }
     if (ok) drain((nk - 1) / G);  // the last group (the one before it was drained in the loop)
@@ -317,14 +381,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       atomicExch(abort_flag, 1);
       if (lane == 0 && status) atomicOr(status, kTcErrTimeout);
     } else {
-      const int r = q4 * 32 + lane;  // accumulator row = Ahat row row0 + r
       const int64_t i = (int64_t)(row0 + r) >> 1;
       const bool even = (lane & 1) == 0;
 #pragma unroll
-      for (int t = 0; t < KQ; ++t) {
-        const int c = half * KQ + t;
-        const float other = __shfl_xor_sync(0xffffffffu, acc_im[t], 1);
-        const float v = even ? acc_re[t] - other : acc_re[t] + other;  // even lane: Re Y, odd lane: Im Y
+      for (int u = 0; u < KQ; ++u) {
+        const int c = half * KQ + u;
+        const float other = __shfl_xor_sync(0xffffffffu, acc_im[u], 1);
+        const float v = even ? acc_re[u] - other : acc_re[u] + other;  // even lane: Re Y, odd lane: Im Y
         const float w = __shfl_xor_sync(0xffffffffu, v, 1);
         if (even && i < m && c < N) {
           if (part) {
@@ -350,13 +413,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::kTmemCols) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols) : "memory");
   }
 }
 
 // Bhat head and tail: row j = Re X[:, j], row H + j = Im X[:, j] (j < the
-// kets, H = half the tile's BN columns), value and TF32 tail, as swizzled tiles of BN
-// rows x 32 floats, one per k block (zero beyond n).
+// kets, H = half the tile's BN columns), value and TF32 tail, as swizzled tiles
+// of BN rows x 32 floats, one per k block (zero beyond n).
 __global__ void k_tc_split_b(const float2* __restrict__ x, int64_t n, int64_t xes, int64_t xcs, int BN, int64_t nkb,
                              float* __restrict__ bh, float* __restrict__ bl) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;

@@ -1,16 +1,31 @@
-// probe.cu -- qob_probe_peak: the device's FP64 and FP32 fused multiply-add
-// rates, measured with chains of FMAs.
+// probe.cu -- qob_probe_peak / qob_probe_peak_ex: the device's FP64 and FP32
+// fused multiply-add rates, measured with chains of FMAs.
 //
 // The roofline of the ComplexF64 kernels on GB300 is its FP64 pipe, whose rate
 // is far below the FP32 one; this probe measures both on the GPU the library
 // runs on, so the fraction a kernel reaches is taken against a number measured
-// in the same run.  Each thread runs kChains independent chains
-// a = fma(a, b, c) (b, c kernel arguments, so nothing folds), enough chains and
-// resident warps (a full SM: (SMs x 8) blocks of 256 threads) that the FMA
-// latency is covered and the pipe alone bounds the rate; one untimed launch,
+// in the same run.  Each thread runs kChains independent chains of FMAs in one
+// of two forms (k_fma_probe; b, c kernel arguments, so nothing folds), and the
+// form with more lanes per clock counts.  The grid is one
+// full wave: SMs x the blocks of 256 threads the occupancy calculator admits
+// per SM, so no SM idles through a partial second wave.  One untimed launch,
 // then the best of three timed ones, each between two events on a stream of
 // the probe's own.
+//
+// Two figures come out of the best launch:
+//  * the wall rate: FMAs x 2 / event time (TFLOP/s);
+//  * the per-clock rate: each block's first thread reads the SM's cycle
+//    counter (clock64, one counter per SM) before and after its chains, with
+//    the SM it ran on; per SM, FMAs of its blocks / (last end - first start)
+//    gives FMA lanes per SM clock, independent of the clock frequency the
+//    launch ran at.  The cycles per SM over the event time give that frequency.
+// A kernel's fraction of the pipe is then taken at the clock it ran at: lanes
+// per clock x 2 x SMs x its sampled SM clock.
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <map>
+#include <vector>
 
 #include "qob_internal.h"
 
@@ -19,74 +34,146 @@ namespace {
 constexpr int kChains = 16;
 constexpr int kProbeThreads = 256;
 
-template <typename T>
-__global__ void __launch_bounds__(kProbeThreads) k_fma_probe(T* out, int iters, T b, T c) {
-  T a[kChains];
+// FORM 0: a = fma(a, b, c) (the chain runs through the multiplicand);
+// FORM 1: a = fma(x_k, b, a) (through the addend, x_k a register of its own
+// per chain, as in a dot product or a matrix product's inner loop).
+template <typename T, int FORM>
+__global__ void __launch_bounds__(kProbeThreads) k_fma_probe(T* out, long long* stamps, int iters, T b, T c) {
+  T a[kChains], x[kChains];
 #pragma unroll
-  for (int k = 0; k < kChains; ++k) a[k] = (T)(threadIdx.x + k) * c;
+  for (int k = 0; k < kChains; ++k) {
+    a[k] = (T)(threadIdx.x + k) * c;
+    x[k] = (T)(k + 1) * c;
+  }
+  __syncthreads();
+  long long t0 = clock64();
   for (int i = 0; i < iters; ++i) {
 #pragma unroll
-    for (int k = 0; k < kChains; ++k) a[k] = fma(a[k], b, c);
+    for (int k = 0; k < kChains; ++k) a[k] = FORM == 0 ? fma(a[k], b, c) : fma(x[k], b, a[k]);
   }
   T s = 0;
 #pragma unroll
   for (int k = 0; k < kChains; ++k) s += a[k];
   if (s == (T)-1.2345) out[0] = s;  // never true for these arguments; keeps the chains live
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    const long long t1 = clock64();
+    stamps[3 * (size_t)blockIdx.x + 0] = t0;
+    stamps[3 * (size_t)blockIdx.x + 1] = t1;
+    stamps[3 * (size_t)blockIdx.x + 2] = (long long)smid;
+  }
 }
 
-template <typename T>
-double probe(int device, int iters) {
-  int sms = 0;
+struct ProbeResult {
+  double tflops = 0.0;         // wall rate, 2 flops per FMA
+  double lanes_per_clock = 0;  // FMA lanes per SM clock (median over the SMs)
+  double sm_mhz = 0.0;         // SM clock the best launch ran at
+};
+
+template <typename T, int FORM>
+ProbeResult probe_form(int device, int iters) {
+  int sms = 0, per_sm = 0;
   QOB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  QOB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fma_probe<T, FORM>, kProbeThreads, 0));
+  if (per_sm < 1) per_sm = 1;
+  const int blocks = sms * per_sm;
   cudaStream_t s = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   T* out = nullptr;
-  double tflops = 0.0;
+  long long* stamps = nullptr;
+  ProbeResult r;
   QOB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   try {
     QOB_CUDA(cudaEventCreate(&e0));
     QOB_CUDA(cudaEventCreate(&e1));
     QOB_CUDA(cudaMalloc(&out, sizeof(T)));
-    const int blocks = sms * 8;
+    QOB_CUDA(cudaMalloc(&stamps, sizeof(long long) * 3 * (size_t)blocks));
     const T b = (T)0.999, c = (T)1e-3;
-    k_fma_probe<T><<<blocks, kProbeThreads, 0, s>>>(out, iters, b, c);
+    k_fma_probe<T, FORM><<<blocks, kProbeThreads, 0, s>>>(out, stamps, iters, b, c);
     QOB_LAUNCHED();
     float best = 0.f;
+    std::vector<long long> host(3 * (size_t)blocks), keep;
     for (int rep = 0; rep < 3; ++rep) {
       QOB_CUDA(cudaEventRecord(e0, s));
-      k_fma_probe<T><<<blocks, kProbeThreads, 0, s>>>(out, iters, b, c);
+      k_fma_probe<T, FORM><<<blocks, kProbeThreads, 0, s>>>(out, stamps, iters, b, c);
       QOB_LAUNCHED();
       QOB_CUDA(cudaEventRecord(e1, s));
       QOB_CUDA(cudaEventSynchronize(e1));
       float ms = 0.f;
       QOB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      if (rep == 0 || ms < best) best = ms;
+      if (rep == 0 || ms < best) {
+        best = ms;
+        QOB_CUDA(cudaMemcpy(host.data(), stamps, sizeof(long long) * host.size(), cudaMemcpyDeviceToHost));
+        keep = host;
+      }
     }
-    const double fmas = (double)blocks * kProbeThreads * kChains * (double)iters;
-    tflops = 2.0 * fmas / (best * 1e-3) / 1e12;
+    const double per_block = (double)kProbeThreads * kChains * (double)iters;
+    r.tflops = 2.0 * per_block * blocks / (best * 1e-3) / 1e12;
+    // per SM: first start, last end, blocks run
+    std::map<long long, std::pair<std::pair<long long, long long>, int>> span;
+    for (int i = 0; i < blocks; ++i) {
+      const long long t0 = keep[3 * (size_t)i], t1 = keep[3 * (size_t)i + 1], sm = keep[3 * (size_t)i + 2];
+      auto it = span.find(sm);
+      if (it == span.end()) {
+        span[sm] = {{t0, t1}, 1};
+      } else {
+        it->second.first.first = std::min(it->second.first.first, t0);
+        it->second.first.second = std::max(it->second.first.second, t1);
+        it->second.second += 1;
+      }
+    }
+    std::vector<double> rate, cycles;
+    for (const auto& kv : span) {
+      const double cyc = (double)(kv.second.first.second - kv.second.first.first);
+      if (cyc <= 0) continue;
+      rate.push_back(per_block * kv.second.second / cyc);
+      cycles.push_back(cyc);
+    }
+    if (!rate.empty()) {
+      std::sort(rate.begin(), rate.end());
+      std::sort(cycles.begin(), cycles.end());
+      r.lanes_per_clock = rate[rate.size() / 2];
+      r.sm_mhz = cycles.back() / (best * 1e-3) / 1e6;  // the longest SM span over the launch's event time
+    }
   } catch (...) {
     if (out) cudaFree(out);
+    if (stamps) cudaFree(stamps);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     cudaStreamDestroy(s);
     throw;
   }
   QOB_CUDA(cudaFree(out));
+  QOB_CUDA(cudaFree(stamps));
   QOB_CUDA(cudaEventDestroy(e0));
   QOB_CUDA(cudaEventDestroy(e1));
   QOB_CUDA(cudaStreamDestroy(s));
-  return tflops;
+  return r;
+}
+
+// the faster of the two chain forms (by lanes per clock)
+template <typename T>
+ProbeResult probe(int device, int iters) {
+  const ProbeResult r0 = probe_form<T, 0>(device, iters);
+  const ProbeResult r1 = probe_form<T, 1>(device, iters);
+  return r1.lanes_per_clock > r0.lanes_per_clock ? r1 : r0;
 }
 
 }  // namespace
 
-extern "C" int qob_probe_peak(qob_ctx* ctx, int which, double* tflops) {
+extern "C" int qob_probe_peak_ex(qob_ctx* ctx, int which, double* tflops, double* lanes_per_clock,
+                                 double* sm_mhz) {
   if (!ctx) return QOB_ERR_ARG;
   try {
     if (!tflops || (which != 0 && which != 1)) qob::fail(QOB_ERR_ARG, "qob_probe_peak: which must be 0 or 1");
     QOB_CUDA(cudaSetDevice(ctx->c.device));
-    // about 2 ms (FP64) and 1 ms (FP32) per timed launch on GB300
-    *tflops = which == 0 ? probe<double>(ctx->c.device, 512) : probe<float>(ctx->c.device, 8192);
+    // about 2-5 ms (FP64) and 1 ms (FP32) per timed launch on GB300
+    const ProbeResult r = which == 0 ? probe<double>(ctx->c.device, 512) : probe<float>(ctx->c.device, 8192);
+    *tflops = r.tflops;
+    if (lanes_per_clock) *lanes_per_clock = r.lanes_per_clock;
+    if (sm_mhz) *sm_mhz = r.sm_mhz;
     return QOB_OK;
   } catch (const qob::Error& e) {
     ctx->c.err = e.msg;
@@ -95,4 +182,8 @@ extern "C" int qob_probe_peak(qob_ctx* ctx, int which, double* tflops) {
     ctx->c.err = e.what();
     return QOB_ERR_ARG;
   }
+}
+
+extern "C" int qob_probe_peak(qob_ctx* ctx, int which, double* tflops) {
+  return qob_probe_peak_ex(ctx, which, tflops, nullptr, nullptr);
 }

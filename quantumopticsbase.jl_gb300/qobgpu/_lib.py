@@ -48,6 +48,7 @@ SIGNATURES = {
     "qob_destroy": (I, [VP]),
     "qob_last_error": (C.c_char_p, [VP]),
     "qob_probe_peak": (I, [VP, I, DP]),
+    "qob_probe_peak_ex": (I, [VP, I, DP, DP, DP]),
     "qob_set_option": (I, [VP, I, I64]),
     "qob_op_sparse": (I, [VP, I64, I64, I64P, I64P, VP, I, I, C.POINTER(VP)]),
     "qob_op_dense": (I, [VP, I64, I64, VP, I64, I, I, C.POINTER(VP)]),
