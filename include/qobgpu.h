@@ -99,9 +99,11 @@ const char* qob_last_error(qob_ctx* ctx);
 /* Context options (no counterpart in the reference, whose BLAS picks its own
  * kernels).  QOB_OPT_FP64_TENSOR, value 0 (default) or 1: ComplexF64 dense
  * operators and mode products of dense LazyTensor factors whose contracted
- * dimension is at least 64 run on the FP64 tensor cores (DMMA,
- * mma.sync.m8n8k4.f64: four real products per complex 8 x 8 x 4 tile) instead
- * of the FMA kernels; results agree to rounding (1e-15 relative). */
+ * dimension is at least 64, applied to at least 8 kets, run on the FP64 tensor
+ * cores (DMMA, mma.sync.m8n8k4.f64: four real products per complex 8 x 8 x 4
+ * tile) instead of the FMA kernels; results agree to rounding (1e-15
+ * relative).  On GB300 the FMA kernels are faster (about 1.2 against 1.0
+ * TFLOP/s); the option is kept for parts with a faster FP64 tensor pipe. */
 #define QOB_OPT_FP64_TENSOR 1
 /* QOB_OPT_PDL, value 0 (default) or 1: the fused gather kernels are launched
  * with programmatic dependent launch, so that an application's blocks are
@@ -111,11 +113,13 @@ const char* qob_last_error(qob_ctx* ctx);
 #define QOB_OPT_PDL 2
 /* QOB_OPT_FP32_TENSOR, value 0 (default) or 1: ComplexF32 dense operators whose
  * sides are both at least 64 run on the 5th-generation tensor cores
- * (tcgen05.mma kind::tf32 with the accumulator in tensor memory, operand tiles
- * brought into shared memory by bulk asynchronous copies) with every operand
- * split into a TF32 head and tail and three products per tile, which keeps FP32
- * accuracy (relative error ~1e-7); a real, tiled copy of the matrix (the size
- * of the complex one, rounded up to 64 rows x 32 columns) is built on first use. */
+ * (tcgen05.mma kind::tf32; operand tiles brought into shared memory by bulk
+ * asynchronous copies, the matrix's tiles moved on into tensor memory beside
+ * the accumulators) with every operand split into a TF32 head and tail and
+ * three products per k step, which keeps FP32 accuracy (relative error ~1e-7);
+ * a real, tiled copy of the matrix (the size of the complex one, rounded up to
+ * 64 rows x 32 columns) is built on first use.  One block per SM holds the
+ * SM's whole tensor memory for the kernel's duration. */
 #define QOB_OPT_FP32_TENSOR 3
 int qob_set_option(qob_ctx* ctx, int option, int64_t value);
 

@@ -470,7 +470,7 @@ void launch_dense(int precision, const void* a, int64_t m, int64_t n, c128 alpha
                    ff, dmma);
     return;
   }
-  if (dmma && !ff && precision == QOB_C128 && n >= kDmmaMinK) {
+  if (dmma && !ff && precision == QOB_C128 && n >= kDmmaMinK && ncols >= kDmmaMinCols) {
     launch_dense_dmma(a, m, n, alpha, x, xes, xcs, beta, y, yes, ycs, ncols, s, ws, slot);
     return;
   }
@@ -487,7 +487,7 @@ void launch_modek(int precision, const void* a, bool eye, int64_t s1, int64_t do
                   void* y, int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s, bool ff, bool dmma) {
   const int64_t len = s1 * dout * s3;
   if (len == 0 || ncols == 0) return;
-  if (dmma && !ff && !eye && precision == QOB_C128 && din >= kDmmaMinK) {
+  if (dmma && !ff && !eye && precision == QOB_C128 && din >= kDmmaMinK && ncols >= kDmmaMinCols) {
     launch_modek_dmma(a, s1, dout, din, s3, alpha, x, xes, xcs, beta, y, yes, ycs, ncols, s);
     return;
   }

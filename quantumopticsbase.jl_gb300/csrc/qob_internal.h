@@ -449,8 +449,11 @@ void tc_dense_build(TcDense& d, const void* a, int64_t m, int64_t n, cudaStream_
 bool launch_dense_tc(const TcDense& d, c128 alpha, const void* x, int64_t xes, int64_t xcs, c128 beta, void* y,
                      int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s, Workspace* ws, int slot,
                      unsigned* status, int num_sms);
-// contracted dimension from which the FP64 tensor-core option applies
+// contracted dimension and kets from which the FP64 tensor-core option
+// applies (an 8 x 8 x 4 tile covers 8 kets: on one ket the FMA kernels are
+// about 15x faster at n = 4096)
 constexpr int64_t kDmmaMinK = 64;
+constexpr int64_t kDmmaMinCols = 8;
 // Split of ncols vectors of n ComplexF64 elements (element stride es, vector
 // stride cs) into double-float quadruples at the same offsets of out.
 void launch_ff_split(const void* x, int64_t n, int64_t ncols, int64_t es, int64_t cs, void* out, cudaStream_t s);
