@@ -33,11 +33,14 @@
 // memory, add each group's accumulator to registers (see k_tc_cgemm), then
 // run the epilogue; warp 1 owns the tensor memory and one of its threads
 // issues the MMAs (M = 128 rows, N = BN or 2 x BN, K = 8 per instruction).
-// Blocks cover 64 complex rows each and, when that leaves SMs idle, a range of
-// k blocks whose partial products k_tc_reduce adds in order; the grid is one
-// wave (one or two blocks per SM by their shared memory, which also bounds
-// the tensor memory they allocate: all of the SM's, or half of it for up to
-// 16 kets).  Every wait is bounded: a wait that gives up
+// Work is split stream-K style: the (row tile of 64 complex rows, k block)
+// units, row tile major, are cut into equal runs, one per block, so that the
+// grid fills every SM in one wave (one or two blocks per SM by their shared
+// memory, which also bounds the tensor memory they allocate: all of the SM's,
+// or half of it for up to 16 kets).  A block's run holds one or more segments
+// (the part of one row tile's k range in the run); a segment that covers a
+// whole row tile writes y, the others write partial products that
+// k_tc_reduce adds in k order.  Every wait is bounded: a wait that gives up
 // records kTcErrTimeout in the status word, the block drains its copies and
 // MMAs, frees its tensor memory and returns.
 #include <cuda_runtime.h>
@@ -184,8 +187,8 @@ struct TcCfg {
 template <int BN>
 __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
     k_tc_cgemm(const float* __restrict__ ahat, const float* __restrict__ bh_t, const float* __restrict__ bl_t,
-               int64_t m, int N, int nkb, int kb_per, float2* y, int64_t yes, int64_t ycs, float2 alpha, float2 beta,
-               float2* part, unsigned* status) {
+               int64_t m, int N, int nkb, int per, int64_t units, int smax, float2* y, int64_t yes, int64_t ycs,
+               float2 alpha, float2 beta, float2* part, unsigned* status) {
   using C = TcCfg<BN>;
   constexpr int SA = C::kAStages, K = C::kSlots, NA = C::kAcc, G = C::kGroup;
   extern __shared__ __align__(16) unsigned char tc_smem_raw[];
@@ -205,9 +208,13 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
   auto stageB = [&](int t) { return base + (size_t)SA * C::kATile + (size_t)t * C::kBStage; };
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int kb0 = blockIdx.y * kb_per;
-  const int nk = min(nkb - kb0, kb_per);  // >= 1 (the host makes no empty ranges)
-  const int row0 = blockIdx.x * kTcBM;    // first Ahat row of this block
+  const int64_t u0 = (int64_t)blockIdx.x * per;           // first unit of this block
+  const int nk = (int)(units - u0 < (int64_t)per ? units - u0 : (int64_t)per);  // >= 1 (the host makes no empty runs)
+  // The loops below walk the run with (kb, p): the k block of unit it and its
+  // position in its segment; an accumulator group is kGroup k blocks of one
+  // segment (it opens one when p % kGroup == 0, closes one at
+  // p % kGroup == kGroup - 1 or at the segment's end).
+  const int kb_start = (int)(u0 % nkb);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < SA; ++s) {
@@ -241,16 +248,15 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
   if (warp == 0) {
     if (lane == 0) {  // producer
       int issued_a = 0, issued_b = 0;
-      for (int it = 0; it < nk; ++it) {
+      for (int it = 0, kb = kb_start; it < nk; ++it, kb = kb + 1 == nkb ? 0 : kb + 1) {
         const int s = it % SA, t = it % K;
-        const int kb = kb0 + it;
         if (it >= SA && !bar_wait(&aempty[s], ((it / SA) - 1) & 1)) {
           atomicExch(abort_flag, 1);
           break;
         }
         if (*(volatile int*)abort_flag) break;
         bar_expect(&afull[s], C::kATile);
-        bulk_copy(stageA(s), ahat + ((int64_t)blockIdx.x * nkb + kb) * (C::kATile / 4), C::kATile, &afull[s]);
+        bulk_copy(stageA(s), ahat + (u0 + it) * (C::kATile / 4), C::kATile, &afull[s]);  // tile (row tile, kb) = unit
         issued_a = it + 1;
         if (it >= K && !bar_wait(&done[t], ((it / K) - 1) & 1)) {
           atomicExch(abort_flag, 1);
@@ -270,9 +276,17 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
       // kind::tf32, FP32 accumulator, A (tensor memory) and B K-major, M = 128, N = BN or 2 BN
       const uint32_t idesc1 = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kTcBM >> 4) << 24);
       const uint32_t idesc2 = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)((2 * BN) >> 3) << 17) | ((uint32_t)(kTcBM >> 4) << 24);
-      for (int it = 0; it < nk; ++it) {
-        const int t = it % K, q = it / G, b = q % NA;
-        const bool first = it % G == 0, last = it % G == G - 1 || it == nk - 1;
+      int q = -1;  // accumulator group
+      for (int it = 0, kb = kb_start, p = 0; it < nk; ++it) {
+        const bool first = p % G == 0, last = p % G == G - 1 || kb == nkb - 1 || it == nk - 1;
+        if (++kb == nkb) {
+          kb = 0;
+          p = 0;
+        } else {
+          ++p;
+        }
+        if (first) ++q;
+        const int t = it % K, b = q % NA;
         if (!bar_wait(&conv[t], (it / K) & 1) || !bar_wait(&bfull[t], (it / K) & 1) ||
             (first && q >= NA && !bar_wait(&acce[b], ((q / NA) - 1) & 1))) {
           atomicExch(abort_flag, 1);
@@ -349,6 +363,42 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       bar_arrive(&acce[b]);
     };
+    // the segment of row tile mt, its k blocks drained into acc_re / acc_im: y
+    // when it covers the whole row tile, else its partial product; then the
+    // registers start again from zero
+    auto epilogue = [&](int64_t mt, bool whole) {
+      const int il = r >> 1;                          // complex row in the row tile
+      const int64_t i = mt * (kTcBM / 2) + il;
+      const int64_t j = (int64_t)blockIdx.x - (mt * nkb) / per;  // segment index within the row tile
+      const bool even = (lane & 1) == 0;
+#pragma unroll
+      for (int u = 0; u < KQ; ++u) {
+        const int c = half * KQ + u;
+        const float other = __shfl_xor_sync(0xffffffffu, acc_im[u], 1);
+        const float v = even ? acc_re[u] - other : acc_re[u] + other;  // even lane: Re Y, odd lane: Im Y
+        const float w = __shfl_xor_sync(0xffffffffu, v, 1);
+        if (even && i < m && c < N) {
+          if (!whole) {
+            part[((mt * smax + j) * N + c) * (kTcBM / 2) + il] = make_float2(v, w);
+          } else {
+            float2* yp = y + i * yes + (int64_t)c * ycs;
+            float re = alpha.x * v - alpha.y * w;
+            float im = alpha.x * w + alpha.y * v;
+            if (beta.x != 0.f || beta.y != 0.f) {
+              const float2 o = *yp;
+              re = __fmaf_rn(beta.x, o.x, __fmaf_rn(-beta.y, o.y, re));
+              im = __fmaf_rn(beta.x, o.y, __fmaf_rn(beta.y, o.x, im));
+            }
+            *yp = make_float2(re, im);
+          }
+        }
+        acc_re[u] = acc_im[u] = 0.f;
+      }
+    };
+    int q = -1;                                  // accumulator group
+    int64_t seg_tile = u0 / nkb;                 // row tile of the current segment
+    bool seg_from_zero = kb_start == 0;          // the current segment starts at k block 0
+    int kb = kb_start, p = 0;
     for (int it = 0; it < nk && ok; ++it) {
       const int s = it % SA, t = it % K;
       // warp-uniform, as the tensor-memory stores below need the whole warp
@@ -380,38 +430,30 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       bar_arrive(&conv[t]);
-      if (it % G == 0 && it >= G) drain(it / G - 1);  // the previous group, once this one has begun
+      if (p % G == 0) {
+        ++q;
+        if (q > 0) {
+          drain(q - 1);  // the previous group, once this one has begun
+          if (ok && kb == 0 && it > 0) {  // ... which closed the previous segment, a whole row tile's tail
+            epilogue(seg_tile, seg_from_zero);
+            ++seg_tile;
+            seg_from_zero = true;
+          }
+        }
+      }
+      if (++kb == nkb) {
+        kb = 0;
+        p = 0;
+      } else {
+        ++p;
+      }
     }
-    if (ok) drain((nk - 1) / G);  // the last group (the one before it was drained in the loop)
+    if (ok) drain(q);  // the last group
+    if (ok) epilogue(seg_tile, seg_from_zero && kb == 0);  // whole when the run ended at the tile's last k block
     ok = __all_sync(0xffffffffu, ok && !*(volatile int*)abort_flag);
     if (!ok) {
       atomicExch(abort_flag, 1);
       if (lane == 0 && status) atomicOr(status, kTcErrTimeout);
-    } else {
-      const int64_t i = (int64_t)(row0 + r) >> 1;
-      const bool even = (lane & 1) == 0;
-#pragma unroll
-      for (int u = 0; u < KQ; ++u) {
-        const int c = half * KQ + u;
-        const float other = __shfl_xor_sync(0xffffffffu, acc_im[u], 1);
-        const float v = even ? acc_re[u] - other : acc_re[u] + other;  // even lane: Re Y, odd lane: Im Y
-        const float w = __shfl_xor_sync(0xffffffffu, v, 1);
-        if (even && i < m && c < N) {
-          if (part) {
-            part[((int64_t)blockIdx.y * N + c) * m + i] = make_float2(v, w);
-          } else {
-            float2* yp = y + i * yes + (int64_t)c * ycs;
-            float re = alpha.x * v - alpha.y * w;
-            float im = alpha.x * w + alpha.y * v;
-            if (beta.x != 0.f || beta.y != 0.f) {
-              const float2 o = *yp;
-              re = __fmaf_rn(beta.x, o.x, __fmaf_rn(-beta.y, o.y, re));
-              im = __fmaf_rn(beta.x, o.y, __fmaf_rn(beta.y, o.x, im));
-            }
-            *yp = make_float2(re, im);
-          }
-        }
-      }
     }
   }
   // every MMA issued has completed before the tensor memory is freed
@@ -443,15 +485,21 @@ __global__ void k_tc_split_b(const float2* __restrict__ x, int64_t n, int64_t xe
   bl[o_im] = tf32_tail(v.y);
 }
 
-// y[i, c] = alpha * (sum of the k ranges' partial products, in order) + beta * y[i, c]
-__global__ void k_tc_reduce(const float2* __restrict__ part, int kchunks, int64_t m, int N, float2* __restrict__ y,
-                            int64_t yes, int64_t ycs, float2 alpha, float2 beta) {
+// y[i, c] = alpha * (sum of the segments' partial products of i's row tile, in
+// k order) + beta * y[i, c], for row tiles split over more than one block (a
+// row tile that one block covered was written by that block)
+__global__ void k_tc_reduce(const float2* __restrict__ part, int nkb, int per, int smax, int64_t m, int N,
+                            float2* __restrict__ y, int64_t yes, int64_t ycs, float2 alpha, float2 beta) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
   if (i >= m) return;
+  const int64_t mt = i / (kTcBM / 2);
+  const int il = (int)(i % (kTcBM / 2));
+  const int64_t b0 = (mt * nkb) / per, b1 = (mt * nkb + nkb - 1) / per;
+  if (b1 == b0) return;
   float sr = 0.f, si = 0.f;
-  for (int z = 0; z < kchunks; ++z) {
-    const float2 p = part[((int64_t)z * N + c) * m + i];
+  for (int64_t j = 0; j <= b1 - b0; ++j) {
+    const float2 p = part[((mt * smax + j) * N + c) * (kTcBM / 2) + il];
     sr += p.x;
     si += p.y;
   }
@@ -480,21 +528,23 @@ void run_tc(const TcDense& d, int64_t n, const float2* x, int64_t xes, int64_t x
   if (N < BN / 2) QOB_CUDA(cudaMemsetAsync(w, 0, 2 * bbytes, s));
   k_tc_split_b<<<dim3((unsigned)((d.ldk + 255) / 256), (unsigned)N), 256, 0, s>>>(x, n, xes, xcs, BN, nkb, bh, bl);
   QOB_LAUNCHED();
-  const int mt = (int)d.mtiles;
-  // k ranges so that the blocks fill the SMs in one wave (each range at least 4 k blocks)
-  int kchunks = (int)std::max<int64_t>(1, std::min<int64_t>(C::kPerSM * num_sms / std::max(1, mt), nkb / 4));
-  const int kb_per = (int)((nkb + kchunks - 1) / kchunks);
-  kchunks = (int)((nkb + kb_per - 1) / kb_per);
+  const int64_t mt = d.mtiles;
+  // runs of units (row tile, k block): whole row tiles when they fill the SMs,
+  // else equal runs over exactly one wave of blocks (each at least 4 k blocks)
+  const int64_t units = mt * nkb, wave = (int64_t)C::kPerSM * num_sms;
+  const int per = mt >= wave ? (int)nkb : (int)std::max<int64_t>(4, (units + wave - 1) / wave);
+  const int64_t blocks = (units + per - 1) / per;
+  const int smax = (int)((nkb - 1) / per + 2);  // segments of one row tile, at most
   float2* part = nullptr;
-  if (kchunks > 1) part = static_cast<float2*>(ws->get(slot + 1, (size_t)kchunks * N * d.m * sizeof(float2)));
+  if (per % nkb != 0) part = static_cast<float2*>(ws->get(slot + 1, (size_t)mt * smax * N * (kTcBM / 2) * sizeof(float2)));
   auto kern = k_tc_cgemm<BN>;
   QOB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::kSmem));
-  kern<<<dim3((unsigned)mt, (unsigned)kchunks), kTcThreads, C::kSmem, s>>>(
-      static_cast<const float*>(d.ahat.p), bh, bl, d.m, N, (int)nkb, kb_per, y, yes, ycs, alpha, beta, part, status);
+  kern<<<(unsigned)blocks, kTcThreads, C::kSmem, s>>>(static_cast<const float*>(d.ahat.p), bh, bl, d.m, N, (int)nkb, per,
+                                                      units, smax, y, yes, ycs, alpha, beta, part, status);
   QOB_LAUNCHED();
   if (part) {
-    k_tc_reduce<<<dim3((unsigned)((d.m + 127) / 128), (unsigned)N), 128, 0, s>>>(part, kchunks, d.m, N, y, yes, ycs,
-                                                                                alpha, beta);
+    k_tc_reduce<<<dim3((unsigned)((d.m + 127) / 128), (unsigned)N), 128, 0, s>>>(part, (int)nkb, per, smax, d.m, N, y,
+                                                                                yes, ycs, alpha, beta);
     QOB_LAUNCHED();
   }
 }

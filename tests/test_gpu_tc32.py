@@ -5,8 +5,11 @@ against the oracle (the reference's dense mul!, src/operators_dense.jl:394-396,
 restated in FP64), at the ComplexF32 tolerance 1e-5 (relative l2): kets from
 the left in every tile width the kernel has (1 .. 100 kets: 16, 32 and 64 kets
 per pass), rows of an operator from the right, beta = 0 over a NaN-filled
-output, a matrix whose sides are not multiples of the tile sizes, and the
-4096 x 4096 operator on 16 kets; the device status word stays clear.
+output, a matrix whose sides are not multiples of the tile sizes, the
+4096 x 4096 operator on 16 kets (row tiles split over several blocks, partial
+products added in order) and a 19,500 x 64 operator (more row tiles than one
+wave of blocks: every block writes whole row tiles); the device status word
+stays clear.
 """
 import ctypes as C
 
@@ -69,4 +72,15 @@ def test_tc32_dense_4096_on_16_kets(fp32_tensor):
     D = rand_op(rng, b, b)
     X = O.Operator(b, Q.GenericBasis(16), rng.kets_data(4096, 16))
     Y = O.Operator(b, Q.GenericBasis(16), rng.kets_data(4096, 16))
+    check(Y, D, X, AL, BE, TOL32, np.complex64)
+
+
+def test_tc32_dense_tall_whole_row_tiles(fp32_tensor):
+    # 305 row tiles of 64 rows: at least one wave of blocks, so each block takes
+    # whole row tiles (its full k range) and writes y itself, with no reduction
+    rng = Q.Rng(340)
+    bl, br = Q.GenericBasis(19500), Q.GenericBasis(64)
+    D = rand_op(rng, bl, br)
+    X = O.Operator(br, Q.GenericBasis(3), rng.kets_data(64, 3))
+    Y = O.Operator(bl, Q.GenericBasis(3), rng.kets_data(19500, 3))
     check(Y, D, X, AL, BE, TOL32, np.complex64)
