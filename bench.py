@@ -44,7 +44,10 @@ SHAPES = ("128", "256", "P256", "128s4", "256s4", "128s8", "256s8", "128s16", "2
 # staged-tile shapes of qob_op_tune, in its order: (tile bits, kets per thread, ket sets per warp)
 TILE_SHAPES = ((10, 1, 1), (10, 2, 1), (9, 4, 1), (11, 1, 1), (11, 2, 1), (12, 1, 1), (9, 1, 4), (8, 1, 16),
                (8, 2, 8), (9, 2, 4), (10, 1, 4), (7, 2, 16))
-NCANDS = 36 + len(TILE_SHAPES)
+# index-pair shapes of qob_op_tune_ex, in its order: (kets per thread, threads, ket sets per warp)
+PAIR_SHAPES = ((2, 256, 1), (4, 256, 1), (2, 128, 1), (4, 128, 1), (2, 256, 4), (4, 128, 4), (2, 128, 8), (4, 128, 8),
+               (2, 128, 16), (4, 128, 16))
+NCANDS = 36 + len(TILE_SHAPES) + len(PAIR_SHAPES)
 SEED_H = 3
 ORACLE_BUILD = ("oracle/liboref.so, g++ -O3 -ffp-contract=off: every multiply and add rounded separately, as the "
                 "reference's Julia code computes; portable flags (no -march=native), the same binary that checks "
@@ -396,13 +399,22 @@ def run_own(args, rank, world, local_rank):
         v = chosen.value
         ms = {f"{1 << (k // 9)}x{SHAPES[k % 9]}": times[k] for k in range(36)}
         ms.update({f"T{b}:{tc}x256s{ls}": times[36 + i] for i, (b, tc, ls) in enumerate(TILE_SHAPES)})
-        return {"kets_per_thread": v & 0xFF, "tile_bits": (v >> 8) & 0xFF, "threads_per_block": (v >> 16) & 0x3FF,
-                "ket_sets_per_warp": 1 << ((v >> 26) & 0x7), "persistent": bool(v >> 30),
-                "ms_by_shape": ms}
+        ms.update({f"{tc}x{blk}s{ls}p": times[36 + len(TILE_SHAPES) + i] for i, (tc, blk, ls) in enumerate(PAIR_SHAPES)})
+        return {"kets_per_thread": v & 0x7F, "index_pairs": bool((v >> 7) & 1), "tile_bits": (v >> 8) & 0xFF,
+                "threads_per_block": (v >> 16) & 0x3FF, "ket_sets_per_warp": 1 << ((v >> 26) & 0x7),
+                "persistent": bool(v >> 30), "ms_by_shape": ms}
 
     def fix(dt, spec):
         """A launch shape given as <kets per thread>x<threads>[s<ket sets per warp>], P for persistent,
-        or T<tile bits>:<kets per thread>x256[s<ket sets per warp>] for staged tiles."""
+        T<tile bits>:<kets per thread>x256[s<ket sets per warp>] for staged tiles, or a trailing p
+        for two consecutive indices per thread (<kets per thread>x<threads>[s<sets>]p)."""
+        if spec.endswith("p"):
+            kt, rest = spec[:-1].split("x")
+            split = int(rest.split("s")[1]) if "s" in rest else 1
+            block = int(rest.split("s")[0])
+            raise_for(lib.qob_op_set_pairs(ctx.ptr, hd.ptr, L.QOB_LEFT, dtype_code(dt), int(kt), block, split), ctx)
+            return {"kets_per_thread": int(kt), "index_pairs": True, "threads_per_block": block,
+                    "ket_sets_per_warp": split, "persistent": False, "fixed": spec}
         if spec.startswith("T"):
             tb, rest = spec[1:].split(":")
             kt, rest = rest.split("x")
@@ -541,6 +553,9 @@ def kernel_name(scalar, t):
     if t.get("tile_bits"):
         return (f"k_gather_t<{scalar}, real values, {t['kets_per_thread']} kets/thread, real beta> x 256 threads, "
                 f"tiles of 2^{t['tile_bits']} indices, {t['ket_sets_per_warp']} ket sets/warp")
+    if t.get("index_pairs") and scalar in ("double", "float"):
+        return (f"k_gather_j2<{scalar}, real values, {t['kets_per_thread']} kets/thread, real beta> x "
+                f"{t['threads_per_block']} threads, 2 indices/thread, {t['ket_sets_per_warp']} ket sets/warp")
     return "{}<{}, real values, square, {} kets/thread, real beta> x {} threads, {} ket sets/warp".format(
         "k_gather_p" if t["persistent"] else "k_gather_j", scalar, t["kets_per_thread"], t["threads_per_block"],
         t["ket_sets_per_warp"])

@@ -118,8 +118,8 @@ const char* qob_last_error(qob_ctx* ctx);
  * the accumulators) with every operand split into a TF32 head and tail and
  * three products per k step, which keeps FP32 accuracy (relative error ~1e-7);
  * a real, tiled copy of the matrix (the size of the complex one, rounded up to
- * 64 rows x 32 columns) is built on first use.  One block per SM holds the
- * SM's whole tensor memory for the kernel's duration. */
+ * 64 rows x 32 columns) is built on first use.  Each block holds its share of
+ * the SM's tensor memory (all of it, or half for up to 16 kets) while it runs. */
 #define QOB_OPT_FP32_TENSOR 3
 int qob_set_option(qob_ctx* ctx, int option, int64_t value);
 
@@ -225,9 +225,14 @@ int qob_op_prepare(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t* info)
 int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, double* times_ms,
                 int* chosen);
 
-/* qob_op_tune with the length of times_ms given: writes min(times_len, 48)
- * times, the 36 of qob_op_tune followed by the twelve staged-tile shapes
- * (times_ms[36 + i]): blocks of 256 threads that copy tiles of 2^bits
+/* qob_op_tune with the length of times_ms given: writes min(times_len, 58)
+ * times, the 36 of qob_op_tune, the twelve staged-tile shapes
+ * (times_ms[36 + i]) and ten index-pair shapes (times_ms[48 + i], compact
+ * plans on kets from the left in ComplexF64 / ComplexF32: two consecutive
+ * output indices per thread, see qob_op_set_pairs), (vectors per thread,
+ * threads, vector sets per warp) = (2,256,1) (4,256,1) (2,128,1) (4,128,1)
+ * (2,256,4) (4,128,4) (2,128,8) (4,128,8) (2,128,16) (4,128,16); *chosen has
+ * bit 7 set when an index-pair shape won.  The staged tiles: blocks of 256 threads that copy tiles of 2^bits
  * consecutive indices of their kets into shared memory, for (bits, vectors per
  * thread, vector sets per warp) = (10,1,1) (10,2,1) (9,4,1) (11,1,1) (11,2,1)
  * (12,1,1) (9,1,4) (8,1,16) (8,2,8) (9,2,4) (10,1,4) (7,2,16); -1 when not
@@ -251,6 +256,18 @@ int qob_op_set_launch(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors
  * untiled kernel. */
 int qob_op_set_tile(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_per_thread, int lane_split,
                     int tile_bits);
+
+/* Fix an index-pair shape instead of tuning: compact plans (every group one
+ * run of power-of-two subsystems with one entry per row, e.g. spin chains) of
+ * even size, applied in ComplexF64 or ComplexF32 to kets from the left, run
+ * with two consecutive output indices per thread (a group above bit 0 then
+ * serves both with one slot lookup, and a ComplexF32 ket's two inputs arrive in
+ * one 16-byte load); vectors_per_thread 2 or 4, block 128 or 256 threads,
+ * lane_split as above.  Other calls (other plans, dtypes or sides, ComplexF32
+ * vectors not 16-byte aligned or with an odd stride) run the one-index kernel
+ * with the same shape. */
+int qob_op_set_pairs(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_per_thread, int block,
+                     int lane_split);
 
 /* Device status of the context: kernels with bounded waits (the staged-tile
  * gather's wait for its copies) record a wait that gave up, and a library built

@@ -513,7 +513,7 @@ int qob_op_prepare(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t* info)
 }
 
 namespace {
-// The autotuner; writes min(times_len, 48) timings.
+// The autotuner; writes min(times_len, 58) timings.
 int tune_impl(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, double* times_ms, int times_len,
               int* chosen) {
   return guard(ctx, [&] {
@@ -533,10 +533,16 @@ int tune_impl(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, doub
     const int tbits_c[kTileShapes] = {10, 10, 9, 11, 11, 12, 9, 8, 8, 9, 10, 7};
     const int ttc_c[kTileShapes] = {1, 2, 4, 1, 2, 1, 1, 1, 2, 2, 1, 2};
     const int tls_c[kTileShapes] = {1, 1, 1, 1, 1, 1, 4, 16, 8, 4, 4, 16};
-    constexpr int kCands = 4 * kShapes + kTileShapes;
+    // two consecutive indices per thread (compact plans, vectors from the
+    // left, ComplexF64 / ComplexF32): vectors per thread x threads x vector sets per warp
+    constexpr int kPairShapes = 10;
+    const int ptc_c[kPairShapes] = {2, 4, 2, 4, 2, 4, 2, 4, 2, 4};
+    const int pblk_c[kPairShapes] = {256, 256, 128, 128, 256, 128, 128, 128, 128, 128};
+    const int pls_c[kPairShapes] = {1, 1, 1, 1, 4, 4, 8, 8, 16, 16};
+    constexpr int kCands = 4 * kShapes + kTileShapes + kPairShapes;
     double t[kCands];
     for (double& v : t) v = -1.0;
-    int best = 0, best_block = 256, best_split = 1, best_tile = 0;
+    int best = 0, best_block = 256, best_split = 1, best_tile = 0, best_pairs = 0;
     if (P.gather && P.kind == Plan::Kind::Sum) {
       GatherPlan& g = *P.gather;
       const size_t esz = elem_size(dtype);
@@ -563,30 +569,39 @@ int tune_impl(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, doub
       int mbits = 0;
       while ((int64_t(1) << mbits) < g.m) ++mbits;
       const bool tiles_ok = g.fast && g.square && side == QOB_LEFT && (int64_t(1) << mbits) == g.m;
+      const bool pairs_ok = g.fast && g.square && side == QOB_LEFT && g.all_w1 && g.m % 2 == 0 && dtype != QOB_C128X;
       cudaEvent_t e0, e1;
       QOB_CUDA(cudaEventCreate(&e0));
       QOB_CUDA(cudaEventCreate(&e1));
       double best_t = 1e300;
       for (int k = 0; k < kCands; ++k) {
-        int tc, blk, ls, tb = 0;
+        int tc, blk, ls, tb = 0, pr = 0;
         if (k < 4 * kShapes) {
           tc = tiles[k / kShapes];
           blk = blocks[k % kShapes];
           ls = splits[k % kShapes];
           if (tc > ncols || (tc > 1 && side == QOB_RIGHT && ncols > 1)) continue;
           if (ls > 1 && (tc * ls > ncols || side == QOB_RIGHT)) continue;
-        } else {
+        } else if (k < 4 * kShapes + kTileShapes) {
           const int i = k - 4 * kShapes;
           tc = ttc_c[i];
           blk = 256;
           ls = tls_c[i];
           tb = tbits_c[i];
           if (!tiles_ok || tb > mbits || tc * ls > ncols) continue;
+        } else {
+          const int i = k - 4 * kShapes - kTileShapes;
+          tc = ptc_c[i];
+          blk = pblk_c[i];
+          ls = pls_c[i];
+          pr = 1;
+          if (!pairs_ok || tc * ls > ncols) continue;
         }
         g.tc = tc;
         g.block = blk;
         g.lane_split = ls;
         g.tile_bits = tb;
+        g.pairs = pr;
         for (int i = 0; i < 2; ++i)
           apply_plan(ctx->c, P, {1.0, 0.0}, xc(i), xes, xcs, {0.3, 0.0}, yc(i), yes, ycs, ncols, ts, 0);
         const int reps = std::max(8, copies);
@@ -621,12 +636,14 @@ int tune_impl(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, doub
           best_block = blk;
           best_split = ls;
           best_tile = tb;
+          best_pairs = pr;
         }
       }
       g.tc = best;
       g.block = best_block;
       g.lane_split = best_split;
       g.tile_bits = best_tile;
+      g.pairs = best_pairs;
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
     }
@@ -635,8 +652,8 @@ int tune_impl(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, doub
     int lg = 0;
     while ((1 << lg) < best_split) ++lg;
     if (chosen)
-      *chosen = best | (best_tile << 8) | ((best_block < 0 ? -best_block : best_block) << 16) | (lg << 26) |
-                (best_block < 0 ? (1 << 30) : 0);
+      *chosen = best | (best_pairs << 7) | (best_tile << 8) | ((best_block < 0 ? -best_block : best_block) << 16) |
+                (lg << 26) | (best_block < 0 ? (1 << 30) : 0);
   });
 }
 }  // namespace
@@ -666,6 +683,28 @@ int qob_op_set_launch(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors
       P.gather->block = block;
       P.gather->lane_split = lane_split;
       P.gather->tile_bits = 0;
+      P.gather->pairs = 0;
+    }
+  });
+}
+
+int qob_op_set_pairs(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_per_thread, int block,
+                     int lane_split) {
+  return guard(ctx, [&] {
+    if (!ctx || !op || (side != QOB_LEFT && side != QOB_RIGHT)) fail(QOB_ERR_ARG, "qob_op_set_pairs: bad arguments");
+    check_mul_dtype(dtype);
+    if (vectors_per_thread != 2 && vectors_per_thread != 4)
+      fail(QOB_ERR_ARG, "vectors per thread must be 2 or 4 for index pairs");
+    if (block != 128 && block != 256) fail(QOB_ERR_ARG, "block must be 128 or 256");
+    if (lane_split < 1 || lane_split > 32 || (lane_split & (lane_split - 1)) != 0)
+      fail(QOB_ERR_ARG, "lane_split must be 1, 2, 4, 8, 16 or 32");
+    Plan& P = get_plan(ctx->c, op, side, dtype);
+    if (P.gather) {
+      P.gather->tc = vectors_per_thread;
+      P.gather->block = block;
+      P.gather->lane_split = lane_split;
+      P.gather->tile_bits = 0;
+      P.gather->pairs = 1;
     }
   });
 }
@@ -686,6 +725,7 @@ int qob_op_set_tile(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_p
       P.gather->block = 256;
       P.gather->lane_split = lane_split;
       P.gather->tile_bits = tile_bits;
+      P.gather->pairs = 0;
     }
   });
 }

@@ -37,6 +37,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <utility>
 
 #include "qob_internal.h"
@@ -759,6 +760,134 @@ __global__ void __launch_bounds__(256) k_gather_j(GatherView g, SiteTable st,
     if (t < nt) combine<BMODE>(yb + t * vs_y, acc[t].total(), alpha, beta);
 }
 
+// The two inputs of a pair of consecutive elements (the first at an even index):
+// ComplexF32 in one 16-byte load, ComplexF64 in two.
+__device__ __forceinline__ void ld_pair(const float2* p, float2& a, float2& b) {
+  const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+  a = make_float2(q.x, q.y);
+  b = make_float2(q.z, q.w);
+}
+__device__ __forceinline__ void ld_pair(const double2* p, double2& a, double2& b) {
+  a = __ldg(p);
+  b = __ldg(p + 1);
+}
+template <typename R, int VM>
+struct PairsOk {
+  static constexpr bool value = (std::is_same<R, double>::value || std::is_same<R, float>::value) && VM != kComplex;
+};
+
+// Two consecutive output indices per thread (J0 even and J0 + 1), for compact
+// plans on kets (every group one run of power-of-two subsystems, one slot per
+// row).  A group whose run starts above bit 0 maps both indices to the same
+// local row, slot and value and to two consecutive inputs (an even first one),
+// so its descriptor, slot lookup and index arithmetic serve two outputs and
+// a ComplexF32 ket's two inputs arrive in one 16-byte load; the group on bit 0
+// is taken index by index.  Lane split, block order and vector sets as
+// k_gather_j, over pairs.
+template <typename R, int VM, int TC, int BMODE>
+__global__ void __launch_bounds__(256) k_gather_j2(GatherView g, const typename In<R>::T* __restrict__ x, int64_t xcs,
+                                                   typename Cx<R>::T* __restrict__ y, int64_t ycs, int ncols,
+                                                   typename Cx<R>::T alpha, typename Cx<R>::T beta) {
+  using CT = typename Cx<R>::T;
+  using XT = typename In<R>::T;
+  using AT = typename AccOf<R>::T;
+  using ET = typename Ell<R, VM != kComplex>::T;
+  using VT = typename Val<R, VM != kComplex>::T;
+  using DT = typename Val<R, VM == kReal>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  pdl_enter();
+  const ET* ell = stage<ET>(smem_raw, g);
+  const int4* fg = reinterpret_cast<const int4*>(reinterpret_cast<const GGroup*>(smem_raw) + g.ngroups);
+  const int ls = g.lane_split;
+  const int lsh = __ffs(ls) - 1;
+  const int jsh = 5 - lsh;
+  const int lane = threadIdx.x & 31;
+  const int64_t blk = g.jmul == 1u ? (int64_t)blockIdx.x : (int64_t)((blockIdx.x * g.jmul) % gridDim.x);
+  const int64_t pair = blk * (int64_t)(blockDim.x >> lsh) + ((threadIdx.x >> 5) << jsh) + (lane & ((1 << jsh) - 1));
+  if (2 * pair >= g.m) return;
+  const uint32_t J0 = (uint32_t)(2 * pair);
+  const int c0 = blockIdx.y * TC * ls + (lane >> jsh);
+  const int nt = c0 < ncols ? min(TC, (ncols - c0 + ls - 1) >> lsh) : 0;
+  const int64_t vs_x = (int64_t)ls * xcs, vs_y = (int64_t)ls * ycs;
+  const XT* xb = x + (int64_t)c0 * xcs;
+  AT a0[TC], a1[TC];
+  if (g.has_diag) {
+    const DT d0 = static_cast<const DT*>(g.diag)[J0], d1 = static_cast<const DT*>(g.diag)[J0 + 1];
+#pragma unroll
+    for (int t = 0; t < TC; ++t)
+      if (t < nt) {
+        XT u, w;
+        ld_pair(xb + J0 + t * vs_x, u, w);
+        a0[t].set(d0, u);
+        a1[t].set(d1, w);
+      }
+  } else {
+#pragma unroll
+    for (int t = 0; t < TC; ++t) {
+      a0[t].zero();
+      a1[t].zero();
+    }
+  }
+#pragma unroll 4
+  for (int gi = 0; gi < g.ngroups; ++gi) {
+    const int4 f = fg[gi];
+    const bool im = VM == kPhased && f.w != 0;
+    if (f.x == 0) {  // the group on bit 0: each index on its own
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const uint32_t J = J0 + (uint32_t)e;
+        const uint32_t r = J & (uint32_t)f.y;
+        if (kDebugBounds && out_of_range((int64_t)f.z + r, g.ell_slots, g.status)) continue;
+        const ET s = ell[f.z + r];
+        const VT v = Ell<R, VM != kComplex>::v(s);
+        if (kDebugBounds && nz(v) && out_of_range((int64_t)(J - r) + s.col, g.n, g.status)) continue;
+        if (nz(v)) {
+          const XT* xp = xb + ((int64_t)(J - r) + s.col);
+#pragma unroll
+          for (int t = 0; t < TC; ++t)
+            if (t < nt) {
+              AT& acc = e == 0 ? a0[t] : a1[t];
+              if (im)
+                acc.mac_i(v, ld(xp + t * vs_x));
+              else
+                acc.mac(v, ld(xp + t * vs_x));
+            }
+        }
+      }
+    } else {
+      const uint32_t r = (J0 >> f.x) & (uint32_t)f.y;
+      if (kDebugBounds && out_of_range((int64_t)f.z + r, g.ell_slots, g.status)) continue;
+      const ET s = ell[f.z + r];
+      const VT v = Ell<R, VM != kComplex>::v(s);
+      const int64_t p0 = (int64_t)(J0 - (r << f.x)) + s.col;  // even: every offset of the run is
+      if (kDebugBounds && nz(v) && out_of_range(p0 + 1, g.n, g.status)) continue;  // a multiple of 2^f.x
+      if (nz(v)) {
+        const XT* xp = xb + p0;
+#pragma unroll
+        for (int t = 0; t < TC; ++t)
+          if (t < nt) {
+            XT u, w;
+            ld_pair(xp + t * vs_x, u, w);
+            if (im) {
+              a0[t].mac_i(v, u);
+              a1[t].mac_i(v, w);
+            } else {
+              a0[t].mac(v, u);
+              a1[t].mac(v, w);
+            }
+          }
+      }
+    }
+  }
+  CT* yb = y + J0 + (int64_t)c0 * ycs;
+#pragma unroll
+  for (int t = 0; t < TC; ++t)
+    if (t < nt) {
+      combine<BMODE>(yb + t * vs_y, a0[t].total(), alpha, beta);
+      combine<BMODE>(yb + 1 + t * vs_y, a1[t].total(), alpha, beta);
+    }
+}
+
 // The same work as k_gather_j on a grid of exactly (SMs x resident blocks per
 // SM): every block is resident at once, so every SM holds the same number of
 // blocks, and block b takes the b-th equal share of the warp-sized chunks (32
@@ -926,6 +1055,42 @@ void launch_tc(const GatherView& v, const SiteTable& st, int tc, const void* x, 
   }
 }
 
+// k_gather_j2 (pairs of consecutive indices): grid over the m / 2 pairs as
+// launch_j over indices.
+template <typename R, int VM, int TC, int BMODE>
+void launch_j2(const GatherView& v, const void* x, int64_t xcs, void* y, int64_t ycs, int64_t ncols,
+               typename Cx<R>::T a, typename Cx<R>::T b, size_t smem, cudaStream_t s) {
+  using CT = typename Cx<R>::T;
+  using XT = typename In<R>::T;
+  int ls = v.lane_split > 0 ? v.lane_split : 1;
+  while (ls > 1 && (int64_t)TC * ls > ncols) ls >>= 1;
+  auto kern = k_gather_j2<R, VM, TC, BMODE>;
+  allow_smem(kern, smem);
+  const int threads = v.block > 0 ? v.block : kThreads;
+  const int64_t ppb = threads / ls;  // pairs per block
+  const unsigned gx = (unsigned)((v.m / 2 + ppb - 1) / ppb);
+  GatherView w = v;
+  w.lane_split = ls;
+  w.jmul = gx <= 4096 ? chunk_multiplier(gx) : 1;
+  const int64_t per_y = (int64_t)TC * ls;
+  for (int64_t c0 = 0; c0 < ncols; c0 += (int64_t)65535 * per_y) {  // grid.y limit
+    const int64_t nc = std::min<int64_t>(ncols - c0, (int64_t)65535 * per_y);
+    launch_kernel(v.pdl != 0, kern, dim3(gx, (unsigned)((nc + per_y - 1) / per_y)), (unsigned)threads, smem, s, w,
+                  (const XT*)x + c0 * xcs, xcs, (CT*)y + c0 * ycs, ycs, (int)nc, a, b);
+    QOB_LAUNCHED();
+  }
+}
+
+// Whether the pairs kernel can run this call: a compact plan of even size on
+// contiguous vectors, 2 or 4 vectors per thread, and for ComplexF32 16-byte
+// aligned pairs (an even vector stride on a 16-byte aligned base).
+template <typename R>
+bool pairs_fit(const GatherView& v, int tc, const void* x, int64_t xcs) {
+  if (!v.pairs || !v.fast || v.m % 2 != 0 || (tc != 2 && tc != 4)) return false;
+  if (sizeof(typename In<R>::T) == 8 && (((uintptr_t)x & 15) != 0 || (xcs & 1) != 0)) return false;
+  return true;
+}
+
 // Shared memory of one staged-tile block at most (GB300: 227 KB per block)
 constexpr size_t kTileSmemMax = 200 * 1024;
 
@@ -975,6 +1140,15 @@ void dispatch_layout(const GatherView& v, const SiteTable& st, int tc, const voi
           launch_tile_tc<R, VM, BMODE>(t, ttc, x, xcs, y, ycs, ncols, a, b, s);
           return;
         }
+      }
+    }
+    if constexpr (SQUARE && PairsOk<R, VM>::value) {
+      if (v.all_w1 && pairs_fit<R>(v, tc, x, xcs)) {
+        if (tc == 4)
+          launch_j2<R, VM, 4, BMODE>(w, x, xcs, y, ycs, ncols, a, b, smem, s);
+        else
+          launch_j2<R, VM, 2, BMODE>(w, x, xcs, y, ycs, ncols, a, b, smem, s);
+        return;
       }
     }
     if (SQUARE && v.all_w1)

@@ -1083,6 +1083,7 @@ GatherView GatherPlan::view() const {
   v.block = block;
   v.lane_split = lane_split;
   v.tile_bits = tile_bits;
+  v.pairs = pairs;
   v.status = status;
   v.pdl = 0;
   return v;

@@ -185,6 +185,7 @@ struct GatherView {
   uint32_t jmul;
   int32_t lane_split;  // k_gather_j: vector sets per warp (1, 2, 4 or 8; 32/lane_split indices per warp)
   int32_t tile_bits;   // > 0: compact plans on kets use k_gather_t with tiles of 2^tile_bits indices
+  int32_t pairs;       // 1: compact plans on kets use k_gather_j2 (two consecutive indices per thread)
   int32_t pdl;         // 1: launched with programmatic stream serialization (QOB_OPT_PDL)
   unsigned* status;    // the context's device status word (bounded waits that gave up, failed checks)
 };
@@ -264,6 +265,7 @@ struct GatherPlan {
   int block = 0;  // threads per block chosen by qob_op_tune (0: 256; < 0: persistent grid of -block)
   int lane_split = 1;  // vector sets per warp chosen by qob_op_tune
   int tile_bits = 0;   // > 0: staged tiles of 2^tile_bits indices (k_gather_t), chosen by qob_op_tune
+  int pairs = 0;       // 1: two consecutive indices per thread (k_gather_j2), chosen by qob_op_tune
   unsigned* status = nullptr;  // the owning context's device status word
   DeviceBuf dgroups, dvals;  // diagonal sources: groups + local diagonal tables
   int ndgroups = 0;

@@ -64,6 +64,7 @@ SIGNATURES = {
     "qob_op_tune_ex": (I, [VP, VP, I, I, I64, DP, I, C.POINTER(C.c_int)]),
     "qob_op_set_launch": (I, [VP, VP, I, I, I, I, I]),
     "qob_op_set_tile": (I, [VP, VP, I, I, I, I, I]),
+    "qob_op_set_pairs": (I, [VP, VP, I, I, I, I, I]),
     "qob_device_status": (I, [VP, VP, C.POINTER(C.c_uint)]),
     "qob_mul": (I, [VP, I, I, VP, I, D, D, VP, I64, I64, I64, D, D, VP, I64, I64, I64, VP]),
     "qob_mul_host": (I, [VP, I, I, VP, I, D, D, VP, I64, I64, D, D, VP, I64, I64]),
