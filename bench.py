@@ -86,9 +86,9 @@ def parse():
     p.add_argument("--suite", action="store_true", help="secondary workloads, one JSON line each")
     p.add_argument("--only", nargs="*", default=None, help="with --suite: these workloads only")
     p.add_argument("--probe", action="store_true", help="print the device's measured FP64 / FP32 FMA rates")
-    p.add_argument("--pdl", type=int, default=0, choices=[0, 1],
-                   help="time every form with programmatic dependent launch (QOB_OPT_PDL) on; the other setting "
-                        "is timed beside it in the pdl sub-object")
+    p.add_argument("--pdl", type=int, default=1, choices=[0, 1],
+                   help="programmatic dependent launch (QOB_OPT_PDL) for every timed form (default on: the steps "
+                        "measured 1-3 %% faster with it); the other setting is timed beside it in the pdl sub-object")
     p.add_argument("--no-secondary", action="store_true",
                    help="leave out the batched and served sub-objects (used for ncu captures)")
     return p.parse_args()
