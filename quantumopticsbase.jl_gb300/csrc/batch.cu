@@ -28,9 +28,48 @@ namespace qob {
 
 namespace {
 
+// k of an RK4 stage into the stage combination (the arithmetic of
+// k_rk4_stage, element by element): 1: acc = k, tmp = psi + dt/2 k; 2, 3:
+// acc += 2 k, tmp = psi + (dt/2 | dt) k; 4: psi += dt/6 (acc + k)
+template <typename CT, typename S>
+__device__ __forceinline__ void rk4_stage_element(const BatchItemDev& it, int64_t j, CT kv, int stage) {
+  CT* psi = (CT*)it.psi;
+  CT* acc = (CT*)it.acc;
+  CT* tmp = (CT*)it.tmp_out;
+  const S dt = (S)it.dt;
+  if (stage == 1) {
+    const CT p = psi[j];
+    const S c = dt * (S)0.5;
+    acc[j] = kv;
+    CT o;
+    o.x = p.x + c * kv.x;
+    o.y = p.y + c * kv.y;
+    tmp[j] = o;
+  } else if (stage == 2 || stage == 3) {
+    const CT p = psi[j];
+    const S c = stage == 2 ? dt * (S)0.5 : dt;
+    CT a = acc[j];
+    a.x += (S)2 * kv.x;
+    a.y += (S)2 * kv.y;
+    acc[j] = a;
+    CT o;
+    o.x = p.x + c * kv.x;
+    o.y = p.y + c * kv.y;
+    tmp[j] = o;
+  } else {
+    const CT a = acc[j];
+    CT p = psi[j];
+    const S c = dt / (S)6;
+    p.x += c * (a.x + kv.x);
+    p.y += c * (a.y + kv.y);
+    psi[j] = p;
+  }
+}
+
 template <typename R, bool REALV>
 __global__ void __launch_bounds__(256) k_gather_batch(const BatchItemDev* __restrict__ items,
-                                                      const int2* __restrict__ tiles, int ntiles, int tile) {
+                                                      const int2* __restrict__ tiles, int ntiles, int tile,
+                                                      int stage) {
   using CT = typename gather::Cx<R>::T;
   using AT = typename gather::AccOf<R>::T;
   using ET = typename gather::Ell<R, REALV>::T;
@@ -48,6 +87,18 @@ __global__ void __launch_bounds__(256) k_gather_batch(const BatchItemDev* __rest
       AT acc[1];
       gather::accumulate<R, REALV ? gather::kReal : gather::kComplex, true, false, 1>(
           it.v, st, sg, ell, (uint32_t)J, (const CT*)it.x, 1, 0, 1, acc);
+      if (stage != 0) {  // k = alpha * acc, as combine<0> computes it, then the stage combination
+        CT kv;
+        if constexpr (std::is_same<R, gather::DFX>::value || sizeof(R) == 8) {
+          gather::combine<0>(&kv, acc[0].total(), it.alpha, it.beta);
+          rk4_stage_element<CT, double>(it, J, kv, stage);
+        } else {
+          const float2 a = make_float2((float)it.alpha.x, (float)it.alpha.y);
+          gather::combine<0>(&kv, acc[0].total(), a, a);
+          rk4_stage_element<CT, float>(it, J, kv, stage);
+        }
+        continue;
+      }
       CT* yp = (CT*)it.y + J;
       // beta == 0 overwrites y without reading it (NaN in y is ignored)
       const bool bz = it.beta.x == 0.0 && it.beta.y == 0.0;
@@ -122,6 +173,10 @@ void build_tables(Context& ctx, BatchTables& T, const std::vector<BatchSpec>& sp
     d.y = specs[i].y;
     d.alpha = make_double2(specs[i].alpha.re, specs[i].alpha.im);
     d.beta = make_double2(specs[i].beta.re, specs[i].beta.im);
+    d.psi = specs[i].psi;
+    d.acc = specs[i].acc;
+    d.tmp_out = specs[i].tmp_out;
+    d.dt = specs[i].dt;
     const int idx = (int)dev.size();
     dev.push_back(d);
     for (int64_t j0 = 0; j0 < g.m; j0 += tile) tiles.push_back(make_int2(idx, (int)j0));
@@ -145,25 +200,33 @@ void build_tables(Context& ctx, BatchTables& T, const std::vector<BatchSpec>& sp
   T.grid = std::max(1, std::min(T.ntiles, ctx.num_sms * per_sm));
 }
 
-void launch_tables(Context& ctx, const BatchTables& T, const std::vector<BatchSpec>& specs, cudaStream_t s) {
+bool all_fused(const BatchTables& T) {
+  for (bool f : T.fused)
+    if (!f) return false;
+  return true;
+}
+
+void launch_tables(Context& ctx, const BatchTables& T, const std::vector<BatchSpec>& specs, cudaStream_t s,
+                   int stage) {
+  if (stage != 0 && !all_fused(T)) fail(QOB_ERR_STATE, "launch_tables: a fused RK4 stage with items outside the launch");
   if (T.ntiles > 0) {
     const BatchItemDev* it = (const BatchItemDev*)T.items.p;
     const int2* tl = (const int2*)T.tiles.p;
     if (T.ff) {
       if (T.real)
-        k_gather_batch<gather::DFX, true><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile);
+        k_gather_batch<gather::DFX, true><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
       else
-        k_gather_batch<gather::DFX, false><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile);
+        k_gather_batch<gather::DFX, false><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
     } else if (T.prec == QOB_C128) {
       if (T.real)
-        k_gather_batch<double, true><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile);
+        k_gather_batch<double, true><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
       else
-        k_gather_batch<double, false><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile);
+        k_gather_batch<double, false><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
     } else {
       if (T.real)
-        k_gather_batch<float, true><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile);
+        k_gather_batch<float, true><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
       else
-        k_gather_batch<float, false><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile);
+        k_gather_batch<float, false><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
     }
     QOB_LAUNCHED();
   }

@@ -8,20 +8,31 @@
 
 namespace qob {
 
-// One fused item as the persistent kernel reads it.
+// One fused item as the persistent kernel reads it.  With an RK4 stage
+// (launch_tables' stage 1 .. 4) the item's k = alpha * plan * x goes straight
+// into the stage combination of psi, acc and tmp_out instead of into y.
 struct BatchItemDev {
   GatherView v;
   const void* x;
   void* y;
   double2 alpha, beta;
+  void* psi;
+  void* acc;
+  void* tmp_out;
+  double dt;
 };
 
-// One application y = alpha * plan * x + beta * y (one ket, element stride 1).
+// One application y = alpha * plan * x + beta * y (one ket, element stride 1);
+// psi, acc, tmp_out and dt for a fused RK4 stage.
 struct BatchSpec {
   Plan* plan;
   const void* x;
   void* y;
   c128 alpha, beta;
+  void* psi = nullptr;
+  void* acc = nullptr;
+  void* tmp_out = nullptr;
+  double dt = 0.0;
 };
 
 struct BatchTables {
@@ -41,6 +52,11 @@ struct BatchTables {
 Plan& batch_plan(Context& ctx, qob_op* op, int prec);
 bool plan_fusable(const Plan& P);
 void build_tables(Context& ctx, BatchTables& T, const std::vector<BatchSpec>& specs, int prec, int tile);
-void launch_tables(Context& ctx, const BatchTables& T, const std::vector<BatchSpec>& specs, cudaStream_t s);
+// stage 0: y = alpha * plan * x + beta * y for every item; 1 .. 4: the fused
+// items run RK4 stage `stage` with k = alpha * plan * x (every item must be in
+// the fused launch: all_fused)
+void launch_tables(Context& ctx, const BatchTables& T, const std::vector<BatchSpec>& specs, cudaStream_t s,
+                   int stage = 0);
+bool all_fused(const BatchTables& T);
 
 }  // namespace qob

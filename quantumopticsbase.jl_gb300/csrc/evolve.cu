@@ -10,9 +10,12 @@
 //   k2 = -iH tmp,           acc += 2 k2,     tmp = psi + dt/2 k2
 //   k3 = -iH tmp,           acc += 2 k3,     tmp = psi + dt k3
 //   k4 = -iH tmp,           psi += dt/6 (acc + k4)
-// Every application and every stage combination of all states in flight runs
-// as one launch (the batch tables of batch.cu), so a step of many requests of
-// different dimensions costs eight launches.  The optional renormalisation
+// Every application of all states in flight runs as one launch (the batch
+// tables of batch.cu).  When every state's operator is in the fused launch,
+// each application does its stage combination in the same kernel (k stays in
+// registers: four launches per step, and the k buffer serves as the second
+// tmp buffer the stages then alternate with); otherwise the stage
+// combinations run as launches of their own (eight per step).  The optional renormalisation
 // computes |psi| in FP64 with a per-request reduction of fixed order, so a
 // request's result does not depend on which other requests share its launches.
 //
@@ -158,6 +161,11 @@ struct Ensemble {
   int prec = QOB_C128;
   std::vector<BatchSpec> from_psi, from_tmp;  // k = -i H psi  /  k = -i H tmp
   BatchTables g_psi, g_tmp;
+  // fused steps: stage s applies H to its input and combines in place, the
+  // stages' inputs and outputs alternating psi -> tmp -> k -> tmp -> psi
+  bool fused = false;
+  std::vector<BatchSpec> stage_specs[4];
+  BatchTables g_stage[4];
   DeviceBuf stage_items, stage_tiles, partials;
   int stage_ntiles = 0;
   int grid = 1;
@@ -200,8 +208,26 @@ void ensemble_build(Context& ctx, Ensemble& E, const std::vector<EvolveState>& s
     for (int64_t j = 0; j < s.n; j += kStageTile) tiles.push_back(make_int2((int)i, (int)j));
     items.push_back(d);
   }
-  build_tables(ctx, E.g_psi, E.from_psi, prec, 256);
-  build_tables(ctx, E.g_tmp, E.from_tmp, prec, 256);
+  // fused stages when every operator is in the fused launch
+  for (int st = 0; st < 4; ++st) E.stage_specs[st].clear();
+  for (const EvolveState& s : states) {
+    const double dt = s.dt;
+    E.stage_specs[0].push_back({s.plan, s.psi, s.k, {0.0, -1.0}, {0.0, 0.0}, s.psi, s.acc, s.tmp, dt});
+    E.stage_specs[1].push_back({s.plan, s.tmp, s.k, {0.0, -1.0}, {0.0, 0.0}, s.psi, s.acc, s.k, dt});
+    E.stage_specs[2].push_back({s.plan, s.k, s.tmp, {0.0, -1.0}, {0.0, 0.0}, s.psi, s.acc, s.tmp, dt});
+    E.stage_specs[3].push_back({s.plan, s.tmp, s.k, {0.0, -1.0}, {0.0, 0.0}, s.psi, s.acc, nullptr, dt});
+  }
+  E.fused = false;
+  if (!states.empty()) {
+    build_tables(ctx, E.g_stage[0], E.stage_specs[0], prec, 256);
+    E.fused = all_fused(E.g_stage[0]);
+  }
+  if (E.fused) {
+    for (int st = 1; st < 4; ++st) build_tables(ctx, E.g_stage[st], E.stage_specs[st], prec, 256);
+  } else {
+    build_tables(ctx, E.g_psi, E.from_psi, prec, 256);
+    build_tables(ctx, E.g_tmp, E.from_tmp, prec, 256);
+  }
   E.stage_ntiles = (int)tiles.size();
   if (!items.empty()) {
     E.stage_items.upload(items.data(), items.size() * sizeof(StageItemDev));
@@ -220,6 +246,10 @@ void ensemble_step(Context& ctx, Ensemble& E, cudaStream_t s,
   const int2* tl = (const int2*)E.stage_tiles.p;
   for (int mode = 1; mode <= 4; ++mode) {
     if (before_stage) (*before_stage)(mode);
+    if (E.fused) {
+      launch_tables(ctx, E.g_stage[mode - 1], E.stage_specs[mode - 1], s, mode);
+      continue;
+    }
     launch_tables(ctx, mode == 1 ? E.g_psi : E.g_tmp, mode == 1 ? E.from_psi : E.from_tmp, s);
     if (E.prec == QOB_C128)
       k_rk4_stage<double2, double><<<E.grid, 256, 0, s>>>(it, tl, E.stage_ntiles, mode);
