@@ -148,7 +148,7 @@ struct TcCfg {
   static constexpr int kAccCols = kMerge ? 2 * BN : BN;  // columns of one accumulator
   // two blocks per SM for up to 16 kets (each with half the tensor memory and
   // shared memory): one block's MMA issue waits for its own k blocks' copies
-  // and MMAs while the other's MMAs run (40.5 against 45.4 us on n = 4096, 16 kets)
+  // and MMAs while the other's MMAs run (kernel 40.5 against 45.4 us on n = 4096, 16 kets)
   static constexpr int kPerSM = BN <= 32 ? 2 : 1;
   static constexpr int kTmemCols = kTcTmemCols / kPerSM;  // allocated per block
   static constexpr int kAcc = 2;                         // accumulators, used in turn
@@ -167,8 +167,9 @@ struct TcCfg {
   static_assert(kSmem <= 227 * 1024, "shared-memory budget of one block");
 };
 
-// Y[i, c] (complex rows i < m, kets c < N) = alpha * (Ahat Bhat^T combined) + beta * Y,
-// or the block's partial product into part[kz][c][i] when part != null.
+// Y[i, c] (complex rows i < m, kets c < N) = alpha * (Ahat Bhat^T combined) + beta * Y
+// for the segments of the block's run that cover a whole row tile; for the
+// others their partial products, part[row tile][segment][c][row in the tile].
 //
 // Pipeline.  Ahat tiles arrive in a ring of kAStages shared-memory stages; the
 // split warps copy each into a tensor-memory slot (its value, read by the MMA
