@@ -409,7 +409,7 @@ def modek(ctx, stream):
         op = O.LazyTensor(b, b, sites, facs, 0.3)
         h = handle(ctx, op)
         n = len(b)
-        for tdt, npdt, code, label in _modes(dmma=True):
+        for tdt, npdt, code, label in _modes(dmma=True, tc32=True):
             for ncols in (1, 16):
                 x = _cols(n, ncols, tdt, 61)
                 y = _cols(n, ncols, tdt, 62)

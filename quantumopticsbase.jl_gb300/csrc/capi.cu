@@ -133,7 +133,7 @@ void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, i
       const void* src = x;
       int64_t ses = xes, scs = xcs;
       for (size_t k = 0; k < nst; ++k) {
-        const ModekStep& st = mk.steps[k];
+        ModekStep& st = mk.steps[k];
         std::vector<int64_t> next = cur;
         next[st.site] = st.dout;
         const int64_t s1 = prod_range(cur, 0, st.site), s3 = prod_range(cur, st.site + 1, cur.size());
@@ -148,14 +148,35 @@ void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, i
           launch_ff_split(src, len_in, ncols, ses, scs, xs, s);
           sin = xs;
         }
+        // ComplexF32 dense factors on the tensor cores: one product with the
+        // (before, after, ket) index triples as columns, contracted dimension din
+        const bool tc = ctx.fp32_tensor && P.precision == QOB_C64 && !ffs && !st.eye && st.din >= kDmmaMinK &&
+                        st.dout >= kDmmaMinK;
+        auto mode_product = [&](c128 bk, void* out, int64_t oes, int64_t ocs) {
+          if (tc) {
+            if (!st.tc.ready) tc_dense_build(st.tc, st.a.p, st.dout, st.din, s);
+            TcColMap xm, ym;
+            xm.s1 = ym.s1 = s1;
+            xm.s3 = ym.s3 = s3;
+            xm.sa = ses;
+            xm.sb = s1 * st.din * ses;
+            xm.st = scs;
+            ym.sa = oes;
+            ym.sb = s1 * st.dout * oes;
+            ym.st = ocs;
+            launch_gemm_tc(st.tc, ak, sin, s1 * ses, xm, bk, out, s1 * oes, ym, s1 * s3 * ncols, s, &ctx.ws, ws + 3,
+                           static_cast<unsigned*>(ctx.status.p), ctx.num_sms);
+          } else {
+            launch_modek(P.precision, st.a.p, st.eye, s1, st.dout, st.din, s3, ak, sin, ses, scs, bk, out, oes, ocs,
+                         ncols, s, ffs, ctx.fp64_tensor);
+          }
+        };
         if (k + 1 == nst) {
-          launch_modek(P.precision, st.a.p, st.eye, s1, st.dout, st.din, s3, ak, sin, ses, scs, b, y, yes,
-                       ycs, ncols, s, ffs, ctx.fp64_tensor);
+          mode_product(b, y, yes, ycs);
         } else {
           const int64_t len = prod_range(next, 0, next.size());
           void* t = ctx.ws.get(ws + (k % 2), (size_t)len * ncols * esz);
-          launch_modek(P.precision, st.a.p, st.eye, s1, st.dout, st.din, s3, ak, sin, ses, scs, zero, t, 1,
-                       len, ncols, s, ffs, ctx.fp64_tensor);
+          mode_product(zero, t, 1, len);
           src = t;
           ses = 1;
           scs = len;

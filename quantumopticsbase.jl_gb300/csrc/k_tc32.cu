@@ -97,6 +97,39 @@ __device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t b
 }
 // float offset of element (row r, column k) inside a swizzled tile of 32-float rows
 __host__ __device__ __forceinline__ int swz(int r, int k) { return r * 32 + ((((k >> 2) ^ (r & 7)) << 2) | (k & 3)); }
+// element offset of column c of a column map (no division for a plain stride;
+// 32-bit divisions: column counts and the map's extents stay below 2^31)
+__host__ __device__ __forceinline__ int64_t tc_col_offset(const TcColMap& m, int64_t c) {
+  if (m.s1 == 1 && m.s3 == 1) return c * m.st;
+  const uint32_t cc = (uint32_t)c, s1 = (uint32_t)m.s1, s3 = (uint32_t)m.s3;
+  const uint32_t a = cc % s1, q = cc / s1;
+  return (int64_t)a * m.sa + (int64_t)(q % s3) * m.sb + (int64_t)(q / s3) * m.st;
+}
+// Consecutive columns of a column map: the offset of column c, then of c + 1, ...
+struct TcColCursor {
+  int64_t a, b, off;
+  __device__ __forceinline__ TcColCursor(const TcColMap& m, int64_t c) {
+    const uint32_t cc = (uint32_t)c, s1 = (uint32_t)m.s1, s3 = (uint32_t)m.s3;
+    a = cc % s1;
+    const uint32_t q = cc / s1;
+    b = q % s3;
+    off = a * m.sa + b * m.sb + (int64_t)(q / s3) * m.st;
+  }
+  __device__ __forceinline__ void next(const TcColMap& m) {
+    if (++a < m.s1) {
+      off += m.sa;
+      return;
+    }
+    a = 0;
+    off -= (m.s1 - 1) * m.sa;
+    if (++b < m.s3) {
+      off += m.sb;
+      return;
+    }
+    b = 0;
+    off += m.st - (m.s3 - 1) * m.sb;
+  }
+};
 // Shared-memory matrix descriptor of a K-major tile with the 128-byte swizzle:
 // start address, stride between 8-row groups 1024 bytes, descriptor version 1.
 __device__ __forceinline__ uint64_t sw128_desc(const void* tile) {
@@ -185,11 +218,14 @@ struct TcCfg {
 // The tensor cores' own accumulation (which does not round to nearest) then
 // spans 64 terms only, which keeps the FP32 accuracy of the ComplexF32 mode
 // for long rows (the error does not grow with n).
-template <int BN>
+// COLS: more than one column tile or a column map other than one stride
+// (mode products); without it the kernel keeps one column tile and y's
+// columns one stride apart, which the common dense case compiles leaner for.
+template <int BN, bool COLS>
 __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
     k_tc_cgemm(const float* __restrict__ ahat, const float* __restrict__ bh_t, const float* __restrict__ bl_t,
-               int64_t m, int N, int nkb, int per, int64_t units, int smax, float2* y, int64_t yes, int64_t ycs,
-               float2 alpha, float2 beta, float2* part, unsigned* status) {
+               int64_t m, int mt, int64_t ncols, int nkb, int per, int64_t units, int smax, float2* y, int64_t yes,
+               TcColMap ym, float2 alpha, float2 beta, float2* part, unsigned* status) {
   using C = TcCfg<BN>;
   constexpr int SA = C::kAStages, K = C::kSlots, NA = C::kAcc, G = C::kGroup;
   extern __shared__ __align__(16) unsigned char tc_smem_raw[];
@@ -249,7 +285,10 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
   if (warp == 0) {
     if (lane == 0) {  // producer
       int issued_a = 0, issued_b = 0;
-      for (int it = 0, kb = kb_start; it < nk; ++it, kb = kb + 1 == nkb ? 0 : kb + 1) {
+      int64_t rt = u0 / nkb;                  // combined row tile: column tile * mt + row tile
+      int mti = (int)(rt % mt);               // row tile
+      int64_t ct = rt / mt;                   // column tile
+      for (int it = 0, kb = kb_start; it < nk; ++it) {
         const int s = it % SA, t = it % K;
         if (it >= SA && !bar_wait(&aempty[s], ((it / SA) - 1) & 1)) {
           atomicExch(abort_flag, 1);
@@ -257,16 +296,24 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
         }
         if (*(volatile int*)abort_flag) break;
         bar_expect(&afull[s], C::kATile);
-        bulk_copy(stageA(s), ahat + (u0 + it) * (C::kATile / 4), C::kATile, &afull[s]);  // tile (row tile, kb) = unit
+        bulk_copy(stageA(s), ahat + ((int64_t)mti * nkb + kb) * (C::kATile / 4), C::kATile, &afull[s]);
         issued_a = it + 1;
         if (it >= K && !bar_wait(&done[t], ((it / K) - 1) & 1)) {
           atomicExch(abort_flag, 1);
           break;
         }
         bar_expect(&bfull[t], C::kBStage);
-        bulk_copy(stageB(t), bh_t + (int64_t)kb * (C::kBTile / 4), C::kBTile, &bfull[t]);
-        bulk_copy(stageB(t) + C::kBTile, bl_t + (int64_t)kb * (C::kBTile / 4), C::kBTile, &bfull[t]);
+        const int64_t bt = ((COLS ? ct * nkb : 0) + kb) * (C::kBTile / 4);  // the column tile's Bhat tile of k block kb
+        bulk_copy(stageB(t), bh_t + bt, C::kBTile, &bfull[t]);
+        bulk_copy(stageB(t) + C::kBTile, bl_t + bt, C::kBTile, &bfull[t]);
         issued_b = it + 1;
+        if (++kb == nkb) {
+          kb = 0;
+          if (++mti == mt) {
+            mti = 0;
+            ++ct;
+          }
+        }
       }
       // every copy issued has landed before the block's shared memory goes away
       for (int it = max(0, issued_a - SA); it < issued_a; ++it) bar_wait(&afull[it % SA], (it / SA) & 1);
@@ -367,22 +414,25 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
     // the segment of row tile mt, its k blocks drained into acc_re / acc_im: y
     // when it covers the whole row tile, else its partial product; then the
     // registers start again from zero
-    auto epilogue = [&](int64_t mt, bool whole) {
+    auto epilogue = [&](int64_t rt, bool whole) {
       const int il = r >> 1;                          // complex row in the row tile
-      const int64_t i = mt * (kTcBM / 2) + il;
-      const int64_t j = (int64_t)blockIdx.x - (mt * nkb) / per;  // segment index within the row tile
+      const uint32_t rt32 = (uint32_t)rt;             // units (rt * nkb) stay below 2^31 (the host checks)
+      const int64_t i = (int64_t)(rt32 % (uint32_t)mt) * (kTcBM / 2) + il;
+      const int64_t c0 = (int64_t)(rt32 / (uint32_t)mt) * (BN / 2);  // first column of the column tile
+      const int64_t j = (int64_t)blockIdx.x - (int64_t)((rt32 * (uint32_t)nkb) / (uint32_t)per);  // segment in the row tile
       const bool even = (lane & 1) == 0;
+      TcColCursor cur(ym, COLS ? c0 + half * KQ : 0);  // y offset of this thread's first column (COLS)
 #pragma unroll
       for (int u = 0; u < KQ; ++u) {
         const int c = half * KQ + u;
         const float other = __shfl_xor_sync(0xffffffffu, acc_im[u], 1);
         const float v = even ? acc_re[u] - other : acc_re[u] + other;  // even lane: Re Y, odd lane: Im Y
         const float w = __shfl_xor_sync(0xffffffffu, v, 1);
-        if (even && i < m && c < N) {
+        if (even && i < m && c0 + c < ncols) {
           if (!whole) {
-            part[((mt * smax + j) * N + c) * (kTcBM / 2) + il] = make_float2(v, w);
+            part[((rt * smax + j) * (BN / 2) + c) * (kTcBM / 2) + il] = make_float2(v, w);
           } else {
-            float2* yp = y + i * yes + (int64_t)c * ycs;
+            float2* yp = y + i * yes + (COLS ? cur.off : (int64_t)c * ym.st);
             float re = alpha.x * v - alpha.y * w;
             float im = alpha.x * w + alpha.y * v;
             if (beta.x != 0.f || beta.y != 0.f) {
@@ -394,6 +444,7 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
           }
         }
         acc_re[u] = acc_im[u] = 0.f;
+        if (COLS) cur.next(ym);
       }
     };
     int q = -1;                                  // accumulator group
@@ -467,85 +518,105 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
   }
 }
 
-// Bhat head and tail: row j = Re X[:, j], row H + j = Im X[:, j] (j < the
-// kets, H = half the tile's BN columns), value and TF32 tail, as swizzled tiles
-// of BN rows x 32 floats, one per k block (zero beyond n).
-__global__ void k_tc_split_b(const float2* __restrict__ x, int64_t n, int64_t xes, int64_t xcs, int BN, int64_t nkb,
-                             float* __restrict__ bh, float* __restrict__ bl) {
+// Bhat head and tail of the ncols columns (x's column c at element offset
+// tc_col_offset(xm, c), elements k * xes apart) in column tiles of H = BN / 2
+// columns: in tile ct, row j = Re X[:, ct * H + j], row H + j = Im X[:, ct * H + j],
+// value and TF32 tail, as swizzled tiles of BN rows x 32 floats, tile
+// (ct, k block) at float offset (ct * nkb + k block) * BN * 32 (zero beyond n).
+template <int BN>
+__global__ void k_tc_split_b(const float2* __restrict__ x, int64_t n, int64_t xes, TcColMap xm, int64_t ncols,
+                             int64_t nkb, float* __restrict__ bh, float* __restrict__ bl) {
+  constexpr int H = BN / 2;
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
   if (k >= nkb * kTcBK) return;
-  float2 v = make_float2(0.f, 0.f);
-  if (k < n) v = x[k * xes + (int64_t)j * xcs];
-  const int64_t tile = (k / kTcBK) * (int64_t)BN * kTcBK;
   const int kk = (int)(k % kTcBK);
-  const int64_t o_re = tile + swz(j, kk), o_im = tile + swz(BN / 2 + j, kk);
-  bh[o_re] = v.x;  // read as TF32 by the MMA: its truncated head
-  bl[o_re] = tf32_tail(v.x);
-  bh[o_im] = v.y;
-  bl[o_im] = tf32_tail(v.y);
+  for (uint32_t cg = blockIdx.y; cg < (uint32_t)ncols; cg += gridDim.y) {
+    float2 v = make_float2(0.f, 0.f);
+    if (k < n) v = x[k * xes + tc_col_offset(xm, cg)];
+    const uint32_t ct = cg / H;
+    const int j = (int)(cg % H);
+    const int64_t tile = ((int64_t)ct * nkb + k / kTcBK) * (int64_t)BN * kTcBK;
+    const int64_t o_re = tile + swz(j, kk), o_im = tile + swz(H + j, kk);
+    bh[o_re] = v.x;  // read as TF32 by the MMA: its truncated head
+    bl[o_re] = tf32_tail(v.x);
+    bh[o_im] = v.y;
+    bl[o_im] = tf32_tail(v.y);
+  }
 }
 
-// y[i, c] = alpha * (sum of the segments' partial products of i's row tile, in
-// k order) + beta * y[i, c], for row tiles split over more than one block (a
-// row tile that one block covered was written by that block)
-__global__ void k_tc_reduce(const float2* __restrict__ part, int nkb, int per, int smax, int64_t m, int N,
-                            float2* __restrict__ y, int64_t yes, int64_t ycs, float2 alpha, float2 beta) {
+// y[i, c] = alpha * (sum of the segments' partial products of (i, c)'s
+// combined row tile, in k order) + beta * y[i, c], for the row tiles split over
+// more than one block (a row tile that one block covered was written by that
+// block); c's column tile is c / H, its combined row tile column tile * mt + i / 64.
+template <int BN>
+__global__ void k_tc_reduce(const float2* __restrict__ part, int mt, int nkb, int per, int smax, int64_t m,
+                            int64_t ncols, float2* __restrict__ y, int64_t yes, TcColMap ym, float2 alpha,
+                            float2 beta) {
+  constexpr int H = BN / 2;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int c = blockIdx.y;
   if (i >= m) return;
-  const int64_t mt = i / (kTcBM / 2);
   const int il = (int)(i % (kTcBM / 2));
-  const int64_t b0 = (mt * nkb) / per, b1 = (mt * nkb + nkb - 1) / per;
-  if (b1 == b0) return;
-  float sr = 0.f, si = 0.f;
-  for (int64_t j = 0; j <= b1 - b0; ++j) {
-    const float2 p = part[((mt * smax + j) * N + c) * (kTcBM / 2) + il];
-    sr += p.x;
-    si += p.y;
+  const uint32_t mti = (uint32_t)(i / (kTcBM / 2));
+  for (uint32_t cg = blockIdx.y; cg < (uint32_t)ncols; cg += gridDim.y) {
+    const uint32_t rt = (cg / H) * (uint32_t)mt + mti;  // units (rt * nkb) stay below 2^31 (the host checks)
+    const int c = (int)(cg % H);
+    const uint32_t b0 = (rt * (uint32_t)nkb) / (uint32_t)per, b1 = (rt * (uint32_t)nkb + nkb - 1) / (uint32_t)per;
+    if (b1 == b0) continue;
+    float sr = 0.f, si = 0.f;
+    for (uint32_t j = 0; j <= b1 - b0; ++j) {
+      const float2 p = part[(((int64_t)rt * smax + j) * H + c) * (kTcBM / 2) + il];
+      sr += p.x;
+      si += p.y;
+    }
+    float2* yp = y + i * yes + tc_col_offset(ym, cg);
+    float re = alpha.x * sr - alpha.y * si;
+    float im = alpha.x * si + alpha.y * sr;
+    if (beta.x != 0.f || beta.y != 0.f) {
+      const float2 o = *yp;
+      re = __fmaf_rn(beta.x, o.x, __fmaf_rn(-beta.y, o.y, re));
+      im = __fmaf_rn(beta.x, o.y, __fmaf_rn(beta.y, o.x, im));
+    }
+    *yp = make_float2(re, im);
   }
-  float2* yp = y + i * yes + (int64_t)c * ycs;
-  float re = alpha.x * sr - alpha.y * si;
-  float im = alpha.x * si + alpha.y * sr;
-  if (beta.x != 0.f || beta.y != 0.f) {
-    const float2 o = *yp;
-    re = __fmaf_rn(beta.x, o.x, __fmaf_rn(-beta.y, o.y, re));
-    im = __fmaf_rn(beta.x, o.y, __fmaf_rn(beta.y, o.x, im));
-  }
-  *yp = make_float2(re, im);
 }
 
 template <int BN>
-void run_tc(const TcDense& d, int64_t n, const float2* x, int64_t xes, int64_t xcs, int N, float2* y, int64_t yes,
-            int64_t ycs, float2 alpha, float2 beta, Workspace* ws, int slot, cudaStream_t s, unsigned* status,
-            int num_sms) {
+void run_tc(const TcDense& d, const float2* x, int64_t xes, const TcColMap& xm, int64_t ncols, float2* y,
+            int64_t yes, const TcColMap& ym, float2 alpha, float2 beta, Workspace* ws, int slot, cudaStream_t s,
+            unsigned* status, int num_sms) {
   using C = TcCfg<BN>;
+  constexpr int H = BN / 2;
   const int64_t nkb = d.ldk / kTcBK;
-  // split vectors: head and tail tiles of Bhat (rows N .. BN/2 - 1 and BN/2 + N .. BN - 1 stay zero)
-  const size_t bbytes = (size_t)nkb * C::kBTile;
+  const int64_t ncolt = (ncols + H - 1) / H;
+  // split vectors: head and tail tiles of Bhat (the rows of a last column tile's missing columns stay zero)
+  const size_t bbytes = (size_t)ncolt * nkb * C::kBTile;
   char* w = static_cast<char*>(ws->get(slot, 2 * bbytes + 256));
   float* bh = reinterpret_cast<float*>(w);
   float* bl = reinterpret_cast<float*>(w + bbytes);
-  if (N < BN / 2) QOB_CUDA(cudaMemsetAsync(w, 0, 2 * bbytes, s));
-  k_tc_split_b<<<dim3((unsigned)((d.ldk + 255) / 256), (unsigned)N), 256, 0, s>>>(x, n, xes, xcs, BN, nkb, bh, bl);
+  if (ncols % H != 0) QOB_CUDA(cudaMemsetAsync(w, 0, 2 * bbytes, s));
+  const unsigned gy = (unsigned)std::min<int64_t>(ncols, 65535);
+  k_tc_split_b<BN><<<dim3((unsigned)((d.ldk + 255) / 256), gy), 256, 0, s>>>(x, d.n, xes, xm, ncols, nkb, bh, bl);
   QOB_LAUNCHED();
   const int64_t mt = d.mtiles;
-  // runs of units (row tile, k block): whole row tiles when they fill the SMs,
-  // else equal runs over exactly one wave of blocks (each at least 4 k blocks)
-  const int64_t units = mt * nkb, wave = (int64_t)C::kPerSM * num_sms;
-  const int per = mt >= wave ? (int)nkb : (int)std::max<int64_t>(4, (units + wave - 1) / wave);
+  // units (column tile, row tile, k block), in that order of significance:
+  // whole row tiles when they fill the SMs, else equal runs over exactly one
+  // wave of blocks (each at least 4 k blocks)
+  const int64_t rtiles = ncolt * mt, units = rtiles * nkb, wave = (int64_t)C::kPerSM * num_sms;
+  const int per = rtiles >= wave ? (int)nkb : (int)std::max<int64_t>(4, (units + wave - 1) / wave);
   const int64_t blocks = (units + per - 1) / per;
   const int smax = (int)((nkb - 1) / per + 2);  // segments of one row tile, at most
   float2* part = nullptr;
-  if (per % nkb != 0) part = static_cast<float2*>(ws->get(slot + 1, (size_t)mt * smax * N * (kTcBM / 2) * sizeof(float2)));
-  auto kern = k_tc_cgemm<BN>;
+  if (per % nkb != 0)
+    part = static_cast<float2*>(ws->get(slot + 1, (size_t)rtiles * smax * H * (kTcBM / 2) * sizeof(float2)));
+  const bool cols = ncolt > 1 || ym.s1 != 1 || ym.s3 != 1;
+  auto kern = cols ? k_tc_cgemm<BN, true> : k_tc_cgemm<BN, false>;
   QOB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::kSmem));
-  kern<<<(unsigned)blocks, kTcThreads, C::kSmem, s>>>(static_cast<const float*>(d.ahat.p), bh, bl, d.m, N, (int)nkb, per,
-                                                      units, smax, y, yes, ycs, alpha, beta, part, status);
+  kern<<<(unsigned)blocks, kTcThreads, C::kSmem, s>>>(static_cast<const float*>(d.ahat.p), bh, bl, d.m, (int)mt, ncols,
+                                                      (int)nkb, per, units, smax, y, yes, ym, alpha, beta, part, status);
   QOB_LAUNCHED();
   if (part) {
-    k_tc_reduce<<<dim3((unsigned)((d.m + 127) / 128), (unsigned)N), 128, 0, s>>>(part, (int)nkb, per, smax, d.m, N, y,
-                                                                                yes, ycs, alpha, beta);
+    k_tc_reduce<BN><<<dim3((unsigned)((d.m + 127) / 128), gy), 128, 0, s>>>(part, (int)mt, (int)nkb, per, smax, d.m,
+                                                                           ncols, y, yes, ym, alpha, beta);
     QOB_LAUNCHED();
   }
 }
@@ -583,23 +654,33 @@ void tc_dense_build(TcDense& d, const void* a, int64_t m, int64_t n, cudaStream_
   d.ready = true;
 }
 
+bool launch_gemm_tc(const TcDense& d, c128 alpha, const void* x, int64_t xes, const TcColMap& xm, c128 beta,
+                    void* y, int64_t yes, const TcColMap& ym, int64_t ncols, cudaStream_t s, Workspace* ws, int slot,
+                    unsigned* status, int num_sms) {
+  if (!d.ready || ncols < 1) return false;
+  // (column tile, row tile, k block) units and column indices are counted in 32 bits
+  if (ncols >= ((int64_t)1 << 31) ||
+      (int64_t)(d.mtiles * ((ncols + 15) / 16)) > ((int64_t)1 << 31) / (d.ldk / kTcBK))
+    fail(QOB_ERR_UNSUPPORTED, "tensor-core product: too many tiles");
+  const float2 a = make_float2((float)alpha.re, (float)alpha.im), b = make_float2((float)beta.re, (float)beta.im);
+  const float2* xc = static_cast<const float2*>(x);
+  float2* yc = static_cast<float2*>(y);
+  if (ncols <= 16)
+    run_tc<32>(d, xc, xes, xm, ncols, yc, yes, ym, a, b, ws, slot, s, status, num_sms);
+  else if (ncols <= 32)
+    run_tc<64>(d, xc, xes, xm, ncols, yc, yes, ym, a, b, ws, slot, s, status, num_sms);
+  else  // column tiles of 64 (BN = 128 rows of Bhat), all in one launch
+    run_tc<128>(d, xc, xes, xm, ncols, yc, yes, ym, a, b, ws, slot, s, status, num_sms);
+  return true;
+}
+
 bool launch_dense_tc(const TcDense& d, c128 alpha, const void* x, int64_t xes, int64_t xcs, c128 beta, void* y,
                      int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s, Workspace* ws, int slot,
                      unsigned* status, int num_sms) {
-  if (!d.ready || ncols < 1) return false;
-  const float2 a = make_float2((float)alpha.re, (float)alpha.im), b = make_float2((float)beta.re, (float)beta.im);
-  for (int64_t c0 = 0; c0 < ncols; c0 += 64) {  // up to 64 kets per pass (BN = 128 columns)
-    const int N = (int)std::min<int64_t>(64, ncols - c0);
-    const float2* xc = static_cast<const float2*>(x) + c0 * xcs;
-    float2* yc = static_cast<float2*>(y) + c0 * ycs;
-    if (N <= 16)
-      run_tc<32>(d, d.n, xc, xes, xcs, N, yc, yes, ycs, a, b, ws, slot, s, status, num_sms);
-    else if (N <= 32)
-      run_tc<64>(d, d.n, xc, xes, xcs, N, yc, yes, ycs, a, b, ws, slot, s, status, num_sms);
-    else
-      run_tc<128>(d, d.n, xc, xes, xcs, N, yc, yes, ycs, a, b, ws, slot, s, status, num_sms);
-  }
-  return true;
+  TcColMap xm, ym;  // kets: column c at c * (column stride)
+  xm.st = xcs;
+  ym.st = ycs;
+  return launch_gemm_tc(d, alpha, x, xes, xm, beta, y, yes, ym, ncols, s, ws, slot, status, num_sms);
 }
 
 }  // namespace qob

@@ -293,6 +293,14 @@ struct TcDense {
   bool ready = false;
 };
 
+// Columns of a tensor-core product's operand: column c = a + s1 * (b + s3 * t)
+// sits at element offset a * sa + b * sb + t * st (a dense operator's kets:
+// s1 = s3 = 1, st = the ket stride; a mode product: a and b index the
+// subsystems before and after the contracted one, t the ket).
+struct TcColMap {
+  int64_t s1 = 1, s3 = 1, sa = 0, sb = 0, st = 0;
+};
+
 // Dense full-space term (GEMM / GEMV pass) or a mode-k sequence.
 struct DensePass {
   TermCoef coef;
@@ -307,6 +315,7 @@ struct ModekStep {
   int64_t dout, din;
   DeviceBuf a;  // dout x din column-major
   bool eye = false;
+  TcDense tc;   // ComplexF32 plans: the tensor-core form (QOB_OPT_FP32_TENSOR)
 };
 struct ModekPass {
   TermCoef coef;
@@ -451,6 +460,12 @@ void tc_dense_build(TcDense& d, const void* a, int64_t m, int64_t n, cudaStream_
 bool launch_dense_tc(const TcDense& d, c128 alpha, const void* x, int64_t xes, int64_t xcs, c128 beta, void* y,
                      int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s, Workspace* ws, int slot,
                      unsigned* status, int num_sms);
+// The same with general column maps (xm, ym) over ncols columns, elements xes /
+// yes apart along the contracted / output dimension: mode products of
+// ComplexF32 dense LazyTensor factors.
+bool launch_gemm_tc(const TcDense& d, c128 alpha, const void* x, int64_t xes, const TcColMap& xm, c128 beta,
+                    void* y, int64_t yes, const TcColMap& ym, int64_t ncols, cudaStream_t s, Workspace* ws, int slot,
+                    unsigned* status, int num_sms);
 // contracted dimension and kets from which the FP64 tensor-core option
 // applies (an 8 x 8 x 4 tile covers 8 kets: on one ket the FMA kernels are
 // about 15x faster at n = 4096)

@@ -8,8 +8,12 @@ per pass), rows of an operator from the right, beta = 0 over a NaN-filled
 output, a matrix whose sides are not multiples of the tile sizes, the
 4096 x 4096 operator on 16 kets (row tiles split over several blocks, partial
 products added in order) and a 19,500 x 64 operator (more row tiles than one
-wave of blocks: every block writes whole row tiles); the device status word
-stays clear.
+wave of blocks: every block writes whole row tiles); and the mode products of
+dense LazyTensor factors of 64 or more (the reference's _tp_matmul_first! /
+_mid! / _last!, src/operators_lazytensor.jl:281-428) with the factor on the
+first, a middle and the last subsystem, on 1, 16 and 100 kets, from the left
+and on the rows of an operator from the right; the device status word stays
+clear.
 """
 import ctypes as C
 
@@ -84,3 +88,26 @@ def test_tc32_dense_tall_whole_row_tiles(fp32_tensor):
     X = O.Operator(br, Q.GenericBasis(3), rng.kets_data(64, 3))
     Y = O.Operator(bl, Q.GenericBasis(3), rng.kets_data(19500, 3))
     check(Y, D, X, AL, BE, TOL32, np.complex64)
+
+
+def _dense_factor(rng, d):
+    return O.Operator(Q.GenericBasis(d), Q.GenericBasis(d),
+                      np.asfortranarray(rng.complex_normal(d * d).reshape(d, d, order="F")))
+
+
+@pytest.mark.parametrize("dims,sites,ncols", [(d, s, c) for d, s in (((80, 3, 70), (1, 3)), ((5, 96, 7), (2,)),
+                                                                       ((9, 72), (2,)), ((66, 4), (1,)))
+                                               for c in (1, 16, 100)] + [((200, 3, 200), (1, 3), 16)])
+def test_tc32_mode_products(fp32_tensor, dims, sites, ncols):
+    rng = Q.Rng(360 + len(dims) + ncols + dims[0])
+    b = Q.tensor_basis(*[Q.GenericBasis(d) for d in dims])
+    facs = tuple(_dense_factor(rng, dims[s - 1]) for s in sites)
+    op = O.LazyTensor(b, b, sites, facs, 0.3 - 0.1j)
+    n = len(b)
+    X = O.Operator(b, Q.GenericBasis(ncols), rng.kets_data(n, ncols))
+    Y = O.Operator(b, Q.GenericBasis(ncols), rng.kets_data(n, ncols))
+    check(Y, op, X, AL, BE, TOL32, np.complex64)
+    if ncols == 16 and len(dims) == 3 and dims[0] < 100:
+        R = O.Operator(Q.GenericBasis(5), b, np.asfortranarray(rng.complex_normal(5 * n).reshape(5, n, order="F")))
+        Z = O.Operator(Q.GenericBasis(5), b, np.asfortranarray(rng.complex_normal(5 * n).reshape(5, n, order="F")))
+        check(Z, R, op, AL, BE, TOL32, np.complex64)
