@@ -112,7 +112,8 @@ const char* qob_last_error(qob_ctx* ctx);
  * applications, e.g. replayed steps. */
 #define QOB_OPT_PDL 2
 /* QOB_OPT_FP32_TENSOR, value 0 (default) or 1: ComplexF32 dense operators whose
- * sides are both at least 64 run on the 5th-generation tensor cores
+ * sides are both at least 64, and the mode products of ComplexF32 dense
+ * LazyTensor factors of at least 64 x 64, run on the 5th-generation tensor cores
  * (tcgen05.mma kind::tf32; operand tiles brought into shared memory by bulk
  * asynchronous copies, the matrix's tiles moved on into tensor memory beside
  * the accumulators) with every operand split into a TF32 head and tail and
