@@ -553,7 +553,7 @@ def kernel_name(scalar, t):
     if t.get("tile_bits"):
         return (f"k_gather_t<{scalar}, real values, {t['kets_per_thread']} kets/thread, real beta> x 256 threads, "
                 f"tiles of 2^{t['tile_bits']} indices, {t['ket_sets_per_warp']} ket sets/warp")
-    if t.get("index_pairs") and scalar in ("double", "float"):
+    if t.get("index_pairs"):
         return (f"k_gather_j2<{scalar}, real values, {t['kets_per_thread']} kets/thread, real beta> x "
                 f"{t['threads_per_block']} threads, 2 indices/thread, {t['ket_sets_per_warp']} ket sets/warp")
     return "{}<{}, real values, square, {} kets/thread, real beta> x {} threads, {} ket sets/warp".format(

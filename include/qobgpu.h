@@ -229,7 +229,7 @@ int qob_op_tune(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, do
 /* qob_op_tune with the length of times_ms given: writes min(times_len, 58)
  * times, the 36 of qob_op_tune, the twelve staged-tile shapes
  * (times_ms[36 + i]) and ten index-pair shapes (times_ms[48 + i], compact
- * plans on kets from the left in ComplexF64 / ComplexF32: two consecutive
+ * plans on kets from the left: two consecutive
  * output indices per thread, see qob_op_set_pairs), (vectors per thread,
  * threads, vector sets per warp) = (2,256,1) (4,256,1) (2,128,1) (4,128,1)
  * (2,256,4) (4,128,4) (2,128,8) (4,128,8) (2,128,16) (4,128,16); *chosen has
@@ -260,7 +260,8 @@ int qob_op_set_tile(qob_ctx* ctx, qob_op* op, int side, int dtype, int vectors_p
 
 /* Fix an index-pair shape instead of tuning: compact plans (every group one
  * run of power-of-two subsystems with one entry per row, e.g. spin chains) of
- * even size, applied in ComplexF64 or ComplexF32 to kets from the left, run
+ * even size, applied to kets from the left (ComplexF64, ComplexF32 or
+ * double-float), run
  * with two consecutive output indices per thread (a group above bit 0 then
  * serves both with one slot lookup, and a ComplexF32 ket's two inputs arrive in
  * one 16-byte load); vectors_per_thread 2 or 4, block 128 or 256 threads,

@@ -555,7 +555,7 @@ int tune_impl(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, doub
     const int ttc_c[kTileShapes] = {1, 2, 4, 1, 2, 1, 1, 1, 2, 2, 1, 2};
     const int tls_c[kTileShapes] = {1, 1, 1, 1, 1, 1, 4, 16, 8, 4, 4, 16};
     // two consecutive indices per thread (compact plans, vectors from the
-    // left, ComplexF64 / ComplexF32): vectors per thread x threads x vector sets per warp
+    // left): vectors per thread x threads x vector sets per warp
     constexpr int kPairShapes = 10;
     const int ptc_c[kPairShapes] = {2, 4, 2, 4, 2, 4, 2, 4, 2, 4};
     const int pblk_c[kPairShapes] = {256, 256, 128, 128, 256, 128, 128, 128, 128, 128};
@@ -590,7 +590,7 @@ int tune_impl(qob_ctx* ctx, qob_op* op, int side, int dtype, int64_t ncols, doub
       int mbits = 0;
       while ((int64_t(1) << mbits) < g.m) ++mbits;
       const bool tiles_ok = g.fast && g.square && side == QOB_LEFT && (int64_t(1) << mbits) == g.m;
-      const bool pairs_ok = g.fast && g.square && side == QOB_LEFT && g.all_w1 && g.m % 2 == 0 && dtype != QOB_C128X;
+      const bool pairs_ok = g.fast && g.square && side == QOB_LEFT && g.all_w1 && g.m % 2 == 0;
       cudaEvent_t e0, e1;
       QOB_CUDA(cudaEventCreate(&e0));
       QOB_CUDA(cudaEventCreate(&e1));

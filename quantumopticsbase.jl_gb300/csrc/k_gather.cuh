@@ -761,7 +761,7 @@ __global__ void __launch_bounds__(256) k_gather_j(GatherView g, SiteTable st,
 }
 
 // The two inputs of a pair of consecutive elements (the first at an even index):
-// ComplexF32 in one 16-byte load, ComplexF64 in two.
+// ComplexF32 in one 16-byte load, ComplexF64 (and its double-float split) in two.
 __device__ __forceinline__ void ld_pair(const float2* p, float2& a, float2& b) {
   const float4 q = __ldg(reinterpret_cast<const float4*>(p));
   a = make_float2(q.x, q.y);
@@ -771,9 +771,14 @@ __device__ __forceinline__ void ld_pair(const double2* p, double2& a, double2& b
   a = __ldg(p);
   b = __ldg(p + 1);
 }
+__device__ __forceinline__ void ld_pair(const float4* p, float4& a, float4& b) {  // double-float (hi, lo) pairs
+  a = __ldg(p);
+  b = __ldg(p + 1);
+}
 template <typename R, int VM>
 struct PairsOk {
-  static constexpr bool value = (std::is_same<R, double>::value || std::is_same<R, float>::value) && VM != kComplex;
+  static constexpr bool value =
+      (std::is_same<R, double>::value || std::is_same<R, float>::value || std::is_same<R, DF>::value) && VM != kComplex;
 };
 
 // Two consecutive output indices per thread (J0 even and J0 + 1), for compact
