@@ -312,11 +312,7 @@ def particle(ctx, stream):
     return {"workload": "particle", "results": out}
 
 
-def served(ctx, stream, nreq=192, rate=2000.0, seed=50, preload=False):
-    """Requests of 100 RK4 steps on a server with a worker thread: Poisson
-    arrivals at `rate` per second (latency from submission to completion), or
-    with preload, all requests queued before the worker starts (the engine's
-    sustained rate with a full queue, timed from the start)."""
+def served(ctx, stream, nreq=192, rate=2000.0, seed=50):
     from qobgpu.evolution import Server
 
     rng = Rng(seed)
@@ -333,18 +329,12 @@ def served(ctx, stream, nreq=192, rate=2000.0, seed=50, preload=False):
             S.submit(H, np.zeros(len(H.basis_l)), 1, 1e-3)
         while S.step():
             pass
+        S.start()
         ids = []
-        if preload:
-            for k in range(nreq):
-                ids.append(S.submit(pool[picks[k]], psis[k], 100, 1e-3))
-            t0 = time.perf_counter()
-            S.start()
-        else:
-            S.start()
-            t0 = time.perf_counter()
-            for k in range(nreq):
-                ids.append(S.submit(pool[picks[k]], psis[k], 100, 1e-3))
-                time.sleep(gaps[k])
+        t0 = time.perf_counter()
+        for k in range(nreq):
+            ids.append(S.submit(pool[picks[k]], psis[k], 100, 1e-3))
+            time.sleep(gaps[k])
         for i in ids:
             S.wait(i, 600.0)
         wall = time.perf_counter() - t0
