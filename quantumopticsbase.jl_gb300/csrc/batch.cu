@@ -66,7 +66,10 @@ __device__ __forceinline__ void rk4_stage_element(const BatchItemDev& it, int64_
   }
 }
 
-template <typename R, bool REALV>
+// RK4 instantiates the fused-stage epilogue (stage 1..4 at run time); the
+// plain instantiation keeps the y = alpha k + beta y epilogue alone, so the
+// batched product does not carry the stage code's registers and branches.
+template <typename R, bool REALV, bool RK4>
 __global__ void __launch_bounds__(256) k_gather_batch(const BatchItemDev* __restrict__ items,
                                                       const int2* __restrict__ tiles, int ntiles, int tile,
                                                       int stage) {
@@ -87,7 +90,7 @@ __global__ void __launch_bounds__(256) k_gather_batch(const BatchItemDev* __rest
       AT acc[1];
       gather::accumulate<R, REALV ? gather::kReal : gather::kComplex, true, false, 1>(
           it.v, st, sg, ell, (uint32_t)J, (const CT*)it.x, 1, 0, 1, acc);
-      if (stage != 0) {  // k = alpha * acc, as combine<0> computes it, then the stage combination
+      if constexpr (RK4) {  // k = alpha * acc, as combine<0> computes it, then the stage combination
         CT kv;
         if constexpr (std::is_same<R, gather::DFX>::value || sizeof(R) == 8) {
           gather::combine<0>(&kv, acc[0].total(), it.alpha, it.beta);
@@ -97,23 +100,23 @@ __global__ void __launch_bounds__(256) k_gather_batch(const BatchItemDev* __rest
           gather::combine<0>(&kv, acc[0].total(), a, a);
           rk4_stage_element<CT, float>(it, J, kv, stage);
         }
-        continue;
-      }
-      CT* yp = (CT*)it.y + J;
-      // beta == 0 overwrites y without reading it (NaN in y is ignored)
-      const bool bz = it.beta.x == 0.0 && it.beta.y == 0.0;
-      if constexpr (std::is_same<R, gather::DFX>::value || sizeof(R) == 8) {
-        if (bz)
-          gather::combine<0>(yp, acc[0].total(), it.alpha, it.beta);
-        else
-          gather::combine<2>(yp, acc[0].total(), it.alpha, it.beta);
       } else {
-        const float2 a = make_float2((float)it.alpha.x, (float)it.alpha.y);
-        const float2 b = make_float2((float)it.beta.x, (float)it.beta.y);
-        if (bz)
-          gather::combine<0>(yp, acc[0].total(), a, b);
-        else
-          gather::combine<2>(yp, acc[0].total(), a, b);
+        CT* yp = (CT*)it.y + J;
+        // beta == 0 overwrites y without reading it (NaN in y is ignored)
+        const bool bz = it.beta.x == 0.0 && it.beta.y == 0.0;
+        if constexpr (std::is_same<R, gather::DFX>::value || sizeof(R) == 8) {
+          if (bz)
+            gather::combine<0>(yp, acc[0].total(), it.alpha, it.beta);
+          else
+            gather::combine<2>(yp, acc[0].total(), it.alpha, it.beta);
+        } else {
+          const float2 a = make_float2((float)it.alpha.x, (float)it.alpha.y);
+          const float2 b = make_float2((float)it.beta.x, (float)it.beta.y);
+          if (bz)
+            gather::combine<0>(yp, acc[0].total(), a, b);
+          else
+            gather::combine<2>(yp, acc[0].total(), a, b);
+        }
       }
     }
   }
@@ -126,10 +129,34 @@ size_t ell_size(int prec, bool real) {
   return real ? sizeof(EllF) : sizeof(EllC);
 }
 
+template <bool RK4>
 const void* batch_kernel(int prec, bool real, bool ff) {
-  if (ff) return real ? (const void*)k_gather_batch<gather::DFX, true> : (const void*)k_gather_batch<gather::DFX, false>;
-  return prec == QOB_C128 ? (real ? (const void*)k_gather_batch<double, true> : (const void*)k_gather_batch<double, false>)
-                          : (real ? (const void*)k_gather_batch<float, true> : (const void*)k_gather_batch<float, false>);
+  if (ff)
+    return real ? (const void*)k_gather_batch<gather::DFX, true, RK4> : (const void*)k_gather_batch<gather::DFX, false, RK4>;
+  return prec == QOB_C128
+             ? (real ? (const void*)k_gather_batch<double, true, RK4> : (const void*)k_gather_batch<double, false, RK4>)
+             : (real ? (const void*)k_gather_batch<float, true, RK4> : (const void*)k_gather_batch<float, false, RK4>);
+}
+
+template <bool RK4>
+void launch_batch(const BatchTables& T, const BatchItemDev* it, const int2* tl, cudaStream_t s, int stage) {
+  const int grid = RK4 ? T.grid_rk4 : T.grid;
+  if (T.ff) {
+    if (T.real)
+      k_gather_batch<gather::DFX, true, RK4><<<grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
+    else
+      k_gather_batch<gather::DFX, false, RK4><<<grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
+  } else if (T.prec == QOB_C128) {
+    if (T.real)
+      k_gather_batch<double, true, RK4><<<grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
+    else
+      k_gather_batch<double, false, RK4><<<grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
+  } else {
+    if (T.real)
+      k_gather_batch<float, true, RK4><<<grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
+    else
+      k_gather_batch<float, false, RK4><<<grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
+  }
 }
 
 }  // namespace
@@ -188,16 +215,19 @@ void build_tables(Context& ctx, BatchTables& T, const std::vector<BatchSpec>& sp
     T.items.upload(dev.data(), dev.size() * sizeof(BatchItemDev));
     T.tiles.upload(tiles.data(), tiles.size() * sizeof(int2));
   }
-  // persistent grid: as many 256-thread blocks as are resident at once
-  int per_sm = 1;
-  if (T.ntiles > 0) {
-    const void* kern = batch_kernel(prec, T.real, T.ff);
+  // persistent grids: as many 256-thread blocks as are resident at once
+  auto resident = [&](const void* kern) {
+    int n = 1;
     if (T.smem > 48 * 1024)
       QOB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T.smem));
-    QOB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, T.smem));
-    per_sm = std::max(per_sm, 1);
+    QOB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, 256, T.smem));
+    return std::max(1, std::min(T.ntiles, ctx.num_sms * std::max(n, 1)));
+  };
+  T.grid = T.grid_rk4 = 1;
+  if (T.ntiles > 0) {
+    T.grid = resident(batch_kernel<false>(prec, T.real, T.ff));
+    T.grid_rk4 = resident(batch_kernel<true>(prec, T.real, T.ff));
   }
-  T.grid = std::max(1, std::min(T.ntiles, ctx.num_sms * per_sm));
 }
 
 bool all_fused(const BatchTables& T) {
@@ -212,22 +242,10 @@ void launch_tables(Context& ctx, const BatchTables& T, const std::vector<BatchSp
   if (T.ntiles > 0) {
     const BatchItemDev* it = (const BatchItemDev*)T.items.p;
     const int2* tl = (const int2*)T.tiles.p;
-    if (T.ff) {
-      if (T.real)
-        k_gather_batch<gather::DFX, true><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
-      else
-        k_gather_batch<gather::DFX, false><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
-    } else if (T.prec == QOB_C128) {
-      if (T.real)
-        k_gather_batch<double, true><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
-      else
-        k_gather_batch<double, false><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
-    } else {
-      if (T.real)
-        k_gather_batch<float, true><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
-      else
-        k_gather_batch<float, false><<<T.grid, 256, T.smem, s>>>(it, tl, T.ntiles, T.tile, stage);
-    }
+    if (stage != 0)
+      launch_batch<true>(T, it, tl, s, stage);
+    else
+      launch_batch<false>(T, it, tl, s, stage);
     QOB_LAUNCHED();
   }
   for (size_t i = 0; i < specs.size(); ++i) {  // items outside the fused launch

@@ -45,7 +45,8 @@ struct BatchTables {
   bool real = true;
   bool ff = false;  // double-float items (ComplexF64 data): the kernel splits x as it loads
   size_t smem = 0;
-  int grid = 1;
+  int grid = 1;      // persistent grid of the plain product
+  int grid_rk4 = 1;  // and of the fused RK4 stages
 };
 
 // The LEFT-side plan of an operator, compiled or refreshed on demand (capi.cu).
