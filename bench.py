@@ -737,7 +737,7 @@ def main():
     if args.suite:
         from bench_suite import run_suite
 
-        return run_suite(local_rank, args.only)
+        return run_suite(local_rank, args.only, args.pdl)
     if args.probe:
         return print(json.dumps(probe_peaks(local_rank)), flush=True)
     run_own(args, rank, world, local_rank)

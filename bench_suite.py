@@ -458,15 +458,19 @@ WORKLOADS = ("jc512", "sparse4096", "rho_h8", "lindblad", "particle", "modek", "
              "host_link")
 
 
-def run_suite(device: int = 0, only=None):
-    """Run the workloads (all, or the names in `only`), one JSON line each."""
+def run_suite(device: int = 0, only=None, pdl: int = 1):
+    """Run the workloads (all, or the names in `only`), one JSON line each,
+    with programmatic dependent launch on (pdl = 1, as the headline bench) or
+    off."""
     import torch
 
     ctx = get_context(device)
+    raise_for(L.lib().qob_set_option(ctx.ptr, L.QOB_OPT_PDL, int(pdl)), ctx)
     stream = torch.cuda.Stream(device)
     names = [w for w in WORKLOADS if not only or w in only]
     for fn in (globals()[w] for w in names):
         t0 = time.perf_counter()
         line = fn(ctx, stream)
         line["seconds"] = time.perf_counter() - t0
+        line["pdl"] = bool(pdl)
         print(json.dumps(line), flush=True)

@@ -105,11 +105,13 @@ const char* qob_last_error(qob_ctx* ctx);
  * relative).  On GB300 the FMA kernels are faster (about 1.2 against 1.0
  * TFLOP/s); the option is kept for parts with a faster FP64 tensor pipe. */
 #define QOB_OPT_FP64_TENSOR 1
-/* QOB_OPT_PDL, value 0 (default) or 1: the fused gather kernels are launched
- * with programmatic dependent launch, so that an application's blocks are
- * scheduled while the previous kernel on the stream finishes (each waits for
- * that kernel's completion before it touches memory).  Shortens back-to-back
- * applications, e.g. replayed steps. */
+/* QOB_OPT_PDL, value 0 (default) or 1: the fused gather kernels, and the
+ * split, GEMM and reduce kernels of the tensor-core path (QOB_OPT_FP32_TENSOR),
+ * are launched with programmatic dependent launch, so that an application's
+ * blocks are scheduled while the previous kernel on the stream finishes (each
+ * waits for that kernel's completion before it touches memory; the GEMM sets up
+ * its barriers and tensor memory first).  Shortens back-to-back applications,
+ * e.g. replayed steps. */
 #define QOB_OPT_PDL 2
 /* QOB_OPT_FP32_TENSOR, value 0 (default) or 1: ComplexF32 dense operators whose
  * sides are both at least 64, and the mode products of ComplexF32 dense

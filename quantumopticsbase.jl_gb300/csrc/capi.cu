@@ -114,7 +114,7 @@ void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, i
       if (ctx.fp32_tensor && P.precision == QOB_C64 && !P.ff && d.m >= kDmmaMinK && d.n >= kDmmaMinK) {
         if (!d.tc.ready) tc_dense_build(d.tc, d.a.p, d.m, d.n, s);
         launch_dense_tc(d.tc, ad, xin, xes, xcs, b, y, yes, ycs, ncols, s, &ctx.ws, ws,
-                        static_cast<unsigned*>(ctx.status.p), ctx.num_sms);
+                        static_cast<unsigned*>(ctx.status.p), ctx.num_sms, ctx.pdl);
       } else {
         launch_dense(P.precision, d.a.p, d.m, d.n, ad, xin, xes, xcs, b, y, yes, ycs, ncols, s, &ctx.ws, ws, P.ff,
                      ctx.fp64_tensor);
@@ -165,7 +165,7 @@ void apply_plan(Context& ctx, Plan& P, c128 alpha, const void* x, int64_t xes, i
             ym.sb = s1 * st.dout * oes;
             ym.st = ocs;
             launch_gemm_tc(st.tc, ak, sin, s1 * ses, xm, bk, out, s1 * oes, ym, s1 * s3 * ncols, s, &ctx.ws, ws + 3,
-                           static_cast<unsigned*>(ctx.status.p), ctx.num_sms);
+                           static_cast<unsigned*>(ctx.status.p), ctx.num_sms, ctx.pdl);
           } else {
             launch_modek(P.precision, st.a.p, st.eye, s1, st.dout, st.din, s3, ak, sin, ses, scs, bk, out, oes, ocs,
                          ncols, s, ffs, ctx.fp64_tensor);

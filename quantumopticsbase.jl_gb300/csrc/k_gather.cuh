@@ -40,6 +40,7 @@
 #include <type_traits>
 #include <utility>
 
+#include "launch.cuh"
 #include "qob_internal.h"
 
 namespace qob {
@@ -188,38 +189,6 @@ __device__ __forceinline__ bool nz(double2 v) {
 __device__ __forceinline__ bool nz(float2 v) { return ((__float_as_uint(v.x) | __float_as_uint(v.y)) << 1) != 0u; }
 __device__ __forceinline__ bool nz(float4 v) {
   return ((__float_as_uint(v.x) | __float_as_uint(v.y) | __float_as_uint(v.z) | __float_as_uint(v.w)) << 1) != 0u;
-}
-
-// Programmatic dependent launch: a gather launched with the programmatic
-// stream-serialization attribute may start while the previous kernel of the
-// stream finishes; it waits here, before its first access to memory, until that
-// kernel has completed and its writes are visible, and lets the next such
-// launch start in turn.  Without the attribute both are no-ops.
-__device__ __forceinline__ void pdl_enter() {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
-// A launch with the programmatic stream-serialization attribute when pdl is set
-// (the kernels call pdl_enter first), else an ordinary one.
-template <typename... KArgs, typename... Args>
-void launch_kernel(bool pdl, void (*kernel)(KArgs...), dim3 grid, unsigned threads, size_t smem, cudaStream_t s,
-                   Args&&... args) {
-  if (!pdl) {
-    kernel<<<grid, threads, smem, s>>>(std::forward<Args>(args)...);
-    return;
-  }
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = dim3(threads);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  QOB_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
 }
 
 // FP64 accumulator: plain fused multiply-adds.

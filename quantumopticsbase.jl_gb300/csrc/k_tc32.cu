@@ -47,6 +47,7 @@
 
 #include <algorithm>
 
+#include "launch.cuh"
 #include "qob_internal.h"
 
 namespace qob {
@@ -281,6 +282,9 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
+  // with programmatic dependent launch the set-up above overlaps the split
+  // kernel; nothing in global memory is touched before this point
+  pdl_enter();
 
   if (warp == 0) {
     if (lane == 0) {  // producer
@@ -527,6 +531,7 @@ template <int BN>
 __global__ void k_tc_split_b(const float2* __restrict__ x, int64_t n, int64_t xes, TcColMap xm, int64_t ncols,
                              int64_t nkb, float* __restrict__ bh, float* __restrict__ bl) {
   constexpr int H = BN / 2;
+  pdl_enter();
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= nkb * kTcBK) return;
   const int kk = (int)(k % kTcBK);
@@ -553,6 +558,7 @@ __global__ void k_tc_reduce(const float2* __restrict__ part, int mt, int nkb, in
                             int64_t ncols, float2* __restrict__ y, int64_t yes, TcColMap ym, float2 alpha,
                             float2 beta) {
   constexpr int H = BN / 2;
+  pdl_enter();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= m) return;
   const int il = (int)(i % (kTcBM / 2));
@@ -583,7 +589,7 @@ __global__ void k_tc_reduce(const float2* __restrict__ part, int mt, int nkb, in
 template <int BN>
 void run_tc(const TcDense& d, const float2* x, int64_t xes, const TcColMap& xm, int64_t ncols, float2* y,
             int64_t yes, const TcColMap& ym, float2 alpha, float2 beta, Workspace* ws, int slot, cudaStream_t s,
-            unsigned* status, int num_sms) {
+            unsigned* status, int num_sms, bool pdl) {
   using C = TcCfg<BN>;
   constexpr int H = BN / 2;
   const int64_t nkb = d.ldk / kTcBK;
@@ -595,7 +601,8 @@ void run_tc(const TcDense& d, const float2* x, int64_t xes, const TcColMap& xm, 
   float* bl = reinterpret_cast<float*>(w + bbytes);
   if (ncols % H != 0) QOB_CUDA(cudaMemsetAsync(w, 0, 2 * bbytes, s));
   const unsigned gy = (unsigned)std::min<int64_t>(ncols, 65535);
-  k_tc_split_b<BN><<<dim3((unsigned)((d.ldk + 255) / 256), gy), 256, 0, s>>>(x, d.n, xes, xm, ncols, nkb, bh, bl);
+  launch_kernel(pdl, k_tc_split_b<BN>, dim3((unsigned)((d.ldk + 255) / 256), gy), 256u, 0, s, x, d.n, xes, xm, ncols,
+                nkb, bh, bl);
   QOB_LAUNCHED();
   const int64_t mt = d.mtiles;
   // units (column tile, row tile, k block), in that order of significance:
@@ -611,12 +618,13 @@ void run_tc(const TcDense& d, const float2* x, int64_t xes, const TcColMap& xm, 
   const bool cols = ncolt > 1 || ym.s1 != 1 || ym.s3 != 1;
   auto kern = cols ? k_tc_cgemm<BN, true> : k_tc_cgemm<BN, false>;
   QOB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::kSmem));
-  kern<<<(unsigned)blocks, kTcThreads, C::kSmem, s>>>(static_cast<const float*>(d.ahat.p), bh, bl, d.m, (int)mt, ncols,
-                                                      (int)nkb, per, units, smax, y, yes, ym, alpha, beta, part, status);
+  launch_kernel(pdl, kern, dim3((unsigned)blocks), (unsigned)kTcThreads, C::kSmem, s,
+                static_cast<const float*>(d.ahat.p), (const float*)bh, (const float*)bl, d.m, (int)mt, ncols, (int)nkb,
+                per, units, smax, y, yes, ym, alpha, beta, part, status);
   QOB_LAUNCHED();
   if (part) {
-    k_tc_reduce<BN><<<dim3((unsigned)((d.m + 127) / 128), gy), 128, 0, s>>>(part, (int)mt, (int)nkb, per, smax, d.m,
-                                                                           ncols, y, yes, ym, alpha, beta);
+    launch_kernel(pdl, k_tc_reduce<BN>, dim3((unsigned)((d.m + 127) / 128), gy), 128u, 0, s, (const float2*)part,
+                  (int)mt, (int)nkb, per, smax, d.m, ncols, y, yes, ym, alpha, beta);
     QOB_LAUNCHED();
   }
 }
@@ -656,7 +664,7 @@ void tc_dense_build(TcDense& d, const void* a, int64_t m, int64_t n, cudaStream_
 
 bool launch_gemm_tc(const TcDense& d, c128 alpha, const void* x, int64_t xes, const TcColMap& xm, c128 beta,
                     void* y, int64_t yes, const TcColMap& ym, int64_t ncols, cudaStream_t s, Workspace* ws, int slot,
-                    unsigned* status, int num_sms) {
+                    unsigned* status, int num_sms, bool pdl) {
   if (!d.ready || ncols < 1) return false;
   // (column tile, row tile, k block) units and column indices are counted in 32 bits
   if (ncols >= ((int64_t)1 << 31) ||
@@ -666,21 +674,21 @@ bool launch_gemm_tc(const TcDense& d, c128 alpha, const void* x, int64_t xes, co
   const float2* xc = static_cast<const float2*>(x);
   float2* yc = static_cast<float2*>(y);
   if (ncols <= 16)
-    run_tc<32>(d, xc, xes, xm, ncols, yc, yes, ym, a, b, ws, slot, s, status, num_sms);
+    run_tc<32>(d, xc, xes, xm, ncols, yc, yes, ym, a, b, ws, slot, s, status, num_sms, pdl);
   else if (ncols <= 32)
-    run_tc<64>(d, xc, xes, xm, ncols, yc, yes, ym, a, b, ws, slot, s, status, num_sms);
+    run_tc<64>(d, xc, xes, xm, ncols, yc, yes, ym, a, b, ws, slot, s, status, num_sms, pdl);
   else  // column tiles of 64 (BN = 128 rows of Bhat), all in one launch
-    run_tc<128>(d, xc, xes, xm, ncols, yc, yes, ym, a, b, ws, slot, s, status, num_sms);
+    run_tc<128>(d, xc, xes, xm, ncols, yc, yes, ym, a, b, ws, slot, s, status, num_sms, pdl);
   return true;
 }
 
 bool launch_dense_tc(const TcDense& d, c128 alpha, const void* x, int64_t xes, int64_t xcs, c128 beta, void* y,
                      int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s, Workspace* ws, int slot,
-                     unsigned* status, int num_sms) {
+                     unsigned* status, int num_sms, bool pdl) {
   TcColMap xm, ym;  // kets: column c at c * (column stride)
   xm.st = xcs;
   ym.st = ycs;
-  return launch_gemm_tc(d, alpha, x, xes, xm, beta, y, yes, ym, ncols, s, ws, slot, status, num_sms);
+  return launch_gemm_tc(d, alpha, x, xes, xm, beta, y, yes, ym, ncols, s, ws, slot, status, num_sms, pdl);
 }
 
 }  // namespace qob

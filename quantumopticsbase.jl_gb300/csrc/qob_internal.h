@@ -456,16 +456,18 @@ void launch_modek_dmma(const void* A, int64_t s1, int64_t dout, int64_t din, int
                        cudaStream_t s);
 void tc_dense_build(TcDense& d, const void* a, int64_t m, int64_t n, cudaStream_t s);
 // y = alpha * A x + beta * y for ComplexF32 vectors on the tensor cores;
-// false when d is not built.  Workspace slots slot, slot + 1.
+// false when d is not built.  Workspace slots slot, slot + 1.  pdl: the
+// split, GEMM and reduce kernels are launched with programmatic dependent
+// launch (QOB_OPT_PDL).
 bool launch_dense_tc(const TcDense& d, c128 alpha, const void* x, int64_t xes, int64_t xcs, c128 beta, void* y,
                      int64_t yes, int64_t ycs, int64_t ncols, cudaStream_t s, Workspace* ws, int slot,
-                     unsigned* status, int num_sms);
+                     unsigned* status, int num_sms, bool pdl = false);
 // The same with general column maps (xm, ym) over ncols columns, elements xes /
 // yes apart along the contracted / output dimension: mode products of
 // ComplexF32 dense LazyTensor factors.
 bool launch_gemm_tc(const TcDense& d, c128 alpha, const void* x, int64_t xes, const TcColMap& xm, c128 beta,
                     void* y, int64_t yes, const TcColMap& ym, int64_t ncols, cudaStream_t s, Workspace* ws, int slot,
-                    unsigned* status, int num_sms);
+                    unsigned* status, int num_sms, bool pdl = false);
 // contracted dimension and kets from which the FP64 tensor-core option
 // applies (an 8 x 8 x 4 tile covers 8 kets: on one ket the FMA kernels are
 // about 15x faster at n = 4096)

@@ -111,3 +111,80 @@ def test_tc32_mode_products(fp32_tensor, dims, sites, ncols):
         R = O.Operator(Q.GenericBasis(5), b, np.asfortranarray(rng.complex_normal(5 * n).reshape(5, n, order="F")))
         Z = O.Operator(Q.GenericBasis(5), b, np.asfortranarray(rng.complex_normal(5 * n).reshape(5, n, order="F")))
         check(Z, R, op, AL, BE, TOL32, np.complex64)
+
+
+@pytest.mark.parametrize("which", ["dense", "mode_products"])
+def test_tc32_pdl_keeps_chained_applications_ordered(fp32_tensor, which):
+    """QOB_OPT_PDL on the tensor-core path: the split, GEMM and reduce kernels
+    of each application are launched with programmatic dependent launch (the
+    GEMM's set-up overlaps the split, every kernel waits for its predecessor
+    before touching memory).  A chain y1 = A x, y2 = A y1, y3 = A y2 of
+    ComplexF32 applications recorded into a CUDA graph and replayed equals the
+    oracle's chain at the ComplexF32 tolerance and is bitwise equal to the same
+    chain without PDL; a dense 1024 x 1024 operator on 16 kets (row tiles split
+    over several blocks, partial products reduced) and two 200 x 200 mode
+    products on a 200 x 3 x 200 basis (two split -> GEMM -> reduce chains per
+    application)."""
+    import torch
+
+    import oracle as OR
+    from helpers import rel_l2
+    from qobgpu import _lib as L
+    from qobgpu.device import dtype_code, get_context, handle, raise_for
+
+    rng = Q.Rng(380)
+    if which == "dense":
+        b = Q.GenericBasis(1024)
+        op = rand_op(rng, b, b)
+        alpha = 1.0 / 32.0
+    else:
+        b = Q.tensor_basis(Q.GenericBasis(200), Q.GenericBasis(3), Q.GenericBasis(200))
+        op = O.LazyTensor(b, b, (1, 3), (_dense_factor(rng, 200), _dense_factor(rng, 200)), 1.0)
+        alpha = 1.0 / 200.0
+    n, k = len(b), 16
+    X = rng.kets_data(n, k)
+    node = OR.build_node(op)
+    ref = [np.asfortranarray(X.astype(np.complex64).astype(np.complex128))]
+    for _ in range(3):
+        r = np.zeros_like(ref[-1])
+        OR.mul_kets_threaded(node, alpha, np.asfortranarray(ref[-1]), 0.0, r, 8)
+        ref.append(r)
+    lib = L.lib()
+    ctx = get_context(0)
+    hd = handle(ctx, op)
+    code = dtype_code(np.complex64)
+    stream = torch.cuda.Stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    outs = {}
+    try:
+        for pdl in (0, 1):
+            raise_for(lib.qob_set_option(ctx.ptr, L.QOB_OPT_PDL, pdl), ctx)
+            bufs = [torch.as_tensor(np.ascontiguousarray(X.T), device="cuda:0").to(torch.complex64).t()]
+            bufs += [torch.zeros(k, n, dtype=torch.complex64, device="cuda:0").t() for _ in range(3)]
+
+            def chain():
+                for i in range(3):
+                    raise_for(lib.qob_mul(ctx.ptr, L.QOB_LEFT, 0, hd.ptr, code, alpha, 0.0,
+                                          C.c_void_p(bufs[i].data_ptr()), n, k, n, 0.0, 0.0,
+                                          C.c_void_p(bufs[i + 1].data_ptr()), n, k, n, sp), ctx)
+
+            torch.cuda.synchronize()
+            chain()  # direct launches (builds the tiled matrix on first use)
+            stream.synchronize()
+            g = C.c_void_p()
+            raise_for(lib.qob_graph_begin(ctx.ptr, sp), ctx)
+            chain()
+            raise_for(lib.qob_graph_end(ctx.ptr, sp, C.byref(g)), ctx)
+            for t in bufs[1:]:
+                t.zero_()
+            torch.cuda.synchronize()
+            for _ in range(3):
+                raise_for(lib.qob_graph_launch(ctx.ptr, g, sp), ctx)
+            stream.synchronize()
+            lib.qob_graph_free(ctx.ptr, g)
+            outs[pdl] = [t.cpu().numpy().astype(np.complex128) for t in bufs[1:]]
+    finally:
+        raise_for(lib.qob_set_option(ctx.ptr, L.QOB_OPT_PDL, 0), ctx)
+    for i in range(3):
+        assert rel_l2(outs[1][i], ref[i + 1]) < TOL32, (i, rel_l2(outs[1][i], ref[i + 1]))
+        assert np.array_equal(outs[1][i], outs[0][i])
