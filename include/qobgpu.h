@@ -111,7 +111,8 @@ const char* qob_last_error(qob_ctx* ctx);
  * blocks are scheduled while the previous kernel on the stream finishes (each
  * waits for that kernel's completion before it touches memory; the GEMM sets up
  * its barriers and tensor memory first).  Shortens back-to-back applications,
- * e.g. replayed steps. */
+ * e.g. replayed steps; a grid of far fewer blocks than SMs may run slower with
+ * it, its blocks placed on the SMs that the previous kernel frees first. */
 #define QOB_OPT_PDL 2
 /* QOB_OPT_FP32_TENSOR, value 0 (default) or 1: ComplexF32 dense operators whose
  * sides are both at least 64, and the mode products of ComplexF32 dense
