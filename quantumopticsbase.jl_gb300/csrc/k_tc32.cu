@@ -1,6 +1,6 @@
 // k_tc32.cu -- ComplexF32 dense operator times vectors on the 5th-generation
-// tensor cores (tcgen05.mma kind::tf32, accumulator in tensor memory, operand
-// tiles brought in by TMA), for mul! on a DenseOperator
+// tensor cores (tcgen05.mma kind::tf32, accumulator and A operand in tensor
+// memory, B tiles brought in by bulk copies), for mul! on a DenseOperator
 // (src/operators_dense.jl:394-396, BLAS cgemm in the reference).
 //
 // The complex product is one real GEMM.  The operator is stored (built on
@@ -11,8 +11,8 @@
 // memory as tiles (128 rows x 32 floats of Ahat, BN rows x 32 floats of Bhat),
 // each tile one contiguous block laid out exactly as the MMA reads it from
 // shared memory (rows of 128 bytes, 16-byte chunk c of row r at position
-// c ^ (r mod 8): the 128-byte swizzle), so a stage arrives with one bulk copy
-// per operand (cp.async.bulk) that streams a contiguous block.  Then
+// c ^ (r mod 8): the 128-byte swizzle), so a B stage arrives with one bulk
+// copy per tile (cp.async.bulk) that streams a contiguous block.  Then
 // D = Ahat Bhat^T (2m x 2N, FP32 in tensor memory) gives
 //   Re Y[i, c] = D[2i, c] - D[2i+1, N+c],   Im Y[i, c] = D[2i+1, c] + D[2i, N+c]
 // (in the kernel the imaginary rows of Bhat start at BN / 2, BN = the tile's
@@ -24,20 +24,20 @@
 // turn: within 2^-20 |x|), and D = Ahi Bhi + Ahi Blo + Alo Bhi (three products
 // per k step, two MMAs when B's head and tail tiles are one operand of twice
 // the columns; the dropped Alo Blo is below 2^-20 of the product): about 1e-6
-// relative.  Each Ahat tile is moved from shared memory into tensor memory
-// as it arrives, value and tail side by side, and the MMAs read A from there;
-// the tails of Bhat are made once per call, beside its values.
+// relative.  Each Ahat tile is loaded from global memory into registers and
+// stored into tensor memory, value and tail side by side, and the MMAs read A
+// from there; the tails of Bhat are made once per call, beside its values.
 //
-// Block (320 threads): warp 0 issues the bulk copies (a ring of Ahat tiles and
-// a ring of Bhat head / tail tiles); warps 2-9 move each Ahat tile into tensor
-// memory, add each group's accumulator to registers (see k_tc_cgemm), then
-// run the epilogue; warp 1 owns the tensor memory and one of its threads
-// issues the MMAs (M = 128 rows, N = BN or 2 x BN, K = 8 per instruction).
+// Block (320 threads): warp 0 issues the bulk copies of the ring of Bhat head /
+// tail tiles; warps 2-9 load each Ahat tile (one k block ahead) and store it
+// into tensor memory, add each group's accumulator to registers (see
+// k_tc_cgemm), then run the epilogue; warp 1 owns the tensor memory and one of
+// its threads issues the MMAs (M = 128 rows, N = BN or 2 x BN, K = 8 per
+// instruction).
 // Work is split stream-K style: the (row tile of 64 complex rows, k block)
 // units, row tile major, are cut into equal runs, one per block, so that the
-// grid fills every SM in one wave (one or two blocks per SM by their shared
-// memory, which also bounds the tensor memory they allocate: all of the SM's,
-// or half of it for up to 16 kets).  A block's run holds one or more segments
+// grid fills every SM in one wave (two blocks per SM for up to 16 kets, each
+// with half of the SM's tensor memory, else one with all of it).  A block's run holds one or more segments
 // (the part of one row tile's k range in the run); a segment that covers a
 // whole row tile writes y, the others write partial products that
 // k_tc_reduce adds in k order.  Every wait is bounded: a wait that gives up
@@ -192,26 +192,33 @@ struct TcCfg {
   static constexpr int kATile = kTcBM * kTcBK * 4;       // 16 KB
   static constexpr int kBTile = BN * kTcBK * 4;
   static constexpr int kBStage = 2 * kBTile;             // B head tile, then B tail tile
-  static constexpr int kAStages = BN <= 32 ? 5 : (BN <= 64 ? 8 : 5);
+  static constexpr int kAStages = BN <= 32 ? 5 : (BN <= 64 ? 8 : 5);  // A ring (ARING)
   static constexpr int kBarBytes = 512;
-  static constexpr size_t kSmem = 1024 /* alignment */ + (size_t)kAStages * kATile + (size_t)kSlots * kBStage + kBarBytes;
+  static constexpr size_t smem(bool aring) {
+    return 1024 /* alignment */ + (aring ? (size_t)kAStages * kATile : 0) + (size_t)kSlots * kBStage + kBarBytes;
+  }
   static_assert(kSlotCol0 + 64 * kSlots <= kTmemCols, "tensor-memory budget");
-  static_assert(kPerSM * (kSmem + 1024) <= 228 * 1024, "shared memory of kPerSM blocks on one SM");
+  static_assert(kPerSM * (smem(true) + 1024) <= 228 * 1024, "shared memory of kPerSM blocks on one SM");
   static_assert(8 * (2 * kAStages + 3 * kSlots + 2 * kAcc + 1) + 8 <= kBarBytes, "barrier area");
-  static_assert(kSmem <= 227 * 1024, "shared-memory budget of one block");
+  static_assert(smem(true) <= 227 * 1024, "shared-memory budget of one block");
 };
 
 // Y[i, c] (complex rows i < m, kets c < N) = alpha * (Ahat Bhat^T combined) + beta * Y
 // for the segments of the block's run that cover a whole row tile; for the
 // others their partial products, part[row tile][segment][c][row in the tile].
 //
-// Pipeline.  Ahat tiles arrive in a ring of kAStages shared-memory stages; the
-// split warps copy each into a tensor-memory slot (its value, read by the MMA
-// as the TF32 head, and its tail: 32 + 32 columns) and release the stage at
-// once, so that ring turns over at the speed of the copies, not of the MMAs.
-// The Bhat tiles of a k block and the tensor-memory slot share an index in a
-// second ring of kSlots, released by the MMAs' commit.  The MMAs read A from
-// tensor memory and B from shared memory.
+// Pipeline.  The split warps store each Ahat tile into a tensor-memory slot:
+// its value, read by the MMA as the TF32 head, and its tail, 32 + 32 columns.
+// They take the tile from a ring of kAStages shared-memory stages filled by
+// bulk copies (ARING: a matrix streamed once from memory, larger than half
+// the L2, which these copies stream fastest; each stage released as soon as
+// it is read), or load it themselves from global memory into registers two
+// k blocks ahead (a matrix read from L2, as the mode products and the smaller
+// operators re-read theirs, where 16-byte loads that each cover 512 bytes of
+// a warp are faster).  The Bhat tiles of a k block, brought into shared
+// memory by bulk copies, and the tensor-memory slot share an index in a ring
+// of kSlots, released by the MMAs' commit.  The MMAs read A from tensor
+// memory and B from shared memory.
 //
 // Accumulation: each group of kGroup k blocks (64 terms) starts a fresh
 // accumulator in tensor memory, kAcc of them used in turn; the split warps
@@ -222,13 +229,13 @@ struct TcCfg {
 // COLS: more than one column tile or a column map other than one stride
 // (mode products); without it the kernel keeps one column tile and y's
 // columns one stride apart, which the common dense case compiles leaner for.
-template <int BN, bool COLS>
+template <int BN, bool COLS, bool ARING>
 __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
     k_tc_cgemm(const float* __restrict__ ahat, const float* __restrict__ bh_t, const float* __restrict__ bl_t,
                int64_t m, int mt, int64_t ncols, int nkb, int per, int64_t units, int smax, float2* y, int64_t yes,
                TcColMap ym, float2 alpha, float2 beta, float2* part, unsigned* status) {
   using C = TcCfg<BN>;
-  constexpr int SA = C::kAStages, K = C::kSlots, NA = C::kAcc, G = C::kGroup;
+  constexpr int SA = ARING ? C::kAStages : 0, K = C::kSlots, NA = C::kAcc, G = C::kGroup;
   extern __shared__ __align__(16) unsigned char tc_smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)tc_smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* bars = reinterpret_cast<uint64_t*>(base + (size_t)SA * C::kATile + (size_t)K * C::kBStage);
@@ -287,21 +294,25 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
   pdl_enter();
 
   if (warp == 0) {
-    if (lane == 0) {  // producer
+    if (lane == 0) {  // producer: the B tiles, and the A tiles with ARING
       int issued_a = 0, issued_b = 0;
       int64_t rt = u0 / nkb;                  // combined row tile: column tile * mt + row tile
       int mti = (int)(rt % mt);               // row tile
       int64_t ct = rt / mt;                   // column tile
       for (int it = 0, kb = kb_start; it < nk; ++it) {
-        const int s = it % SA, t = it % K;
-        if (it >= SA && !bar_wait(&aempty[s], ((it / SA) - 1) & 1)) {
-          atomicExch(abort_flag, 1);
-          break;
+        const int t = it % K;
+        if constexpr (ARING) {
+          const int s = it % SA;
+          if (it >= SA && !bar_wait(&aempty[s], ((it / SA) - 1) & 1)) {
+            atomicExch(abort_flag, 1);
+            break;
+          }
+          if (*(volatile int*)abort_flag) break;
+          bar_expect(&afull[s], C::kATile);
+          bulk_copy(stageA(s), ahat + ((int64_t)mti * nkb + kb) * (C::kATile / 4), C::kATile, &afull[s]);
+          issued_a = it + 1;
         }
         if (*(volatile int*)abort_flag) break;
-        bar_expect(&afull[s], C::kATile);
-        bulk_copy(stageA(s), ahat + ((int64_t)mti * nkb + kb) * (C::kATile / 4), C::kATile, &afull[s]);
-        issued_a = it + 1;
         if (it >= K && !bar_wait(&done[t], ((it / K) - 1) & 1)) {
           atomicExch(abort_flag, 1);
           break;
@@ -455,34 +466,74 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<BN>::kPerSM)
     int64_t seg_tile = u0 / nkb;                 // row tile of the current segment
     bool seg_from_zero = kb_start == 0;          // the current segment starts at k block 0
     int kb = kb_start, p = 0;
+    // row r, columns [16 half, 16 half + 16) of a tile: four 16-byte loads j,
+    // each of the warp's a run of 512 bytes (the tile order of a_slot), from
+    // the shared-memory stage (ARING) or from global memory, where the tile
+    // of unit (row tile mti, k block kb) starts at float4 (mti * nkb + kb) * 1024
+    const int aoff = (q4 * 2 + half) * 4 * 32 + lane;
+    const float4* __restrict__ arow = reinterpret_cast<const float4*>(ahat) + aoff;
+    // direct loads: two tiles in flight, units it + 1 (nx) and it + 2 (nx2), while unit it is stored
+    int fmti = (int)((uint32_t)seg_tile % (uint32_t)mt), fkb = kb_start;  // the unit last loaded
+    auto load = [&](float4 (&v)[4]) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) v[j] = __ldg(arow + ((int64_t)fmti * nkb + fkb) * (C::kATile / 16) + 32 * j);
+    };
+    auto advance = [&] {
+      if (++fkb == nkb) {
+        fkb = 0;
+        if (++fmti == mt) fmti = 0;
+      }
+    };
+    float4 nx[4], nx2[4];
+    if constexpr (!ARING) {
+      load(nx);
+      if (nk > 1) {
+        advance();
+        load(nx2);
+      }
+    }
     for (int it = 0; it < nk && ok; ++it) {
-      const int s = it % SA, t = it % K;
+      const int s = ARING ? it % SA : 0, t = it % K;
+      float hv[16];
+      if constexpr (!ARING) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          hv[4 * j] = nx[j].x;
+          hv[4 * j + 1] = nx[j].y;
+          hv[4 * j + 2] = nx[j].z;
+          hv[4 * j + 3] = nx[j].w;
+          nx[j] = nx2[j];
+        }
+        if (it + 2 < nk) {  // the unit after next, loaded while this one is stored
+          advance();
+          load(nx2);
+        }
+      }
       // warp-uniform, as the tensor-memory stores below need the whole warp
-      if (!__all_sync(0xffffffffu, !*(volatile int*)abort_flag && bar_wait(&afull[s], (it / SA) & 1) &&
+      if (!__all_sync(0xffffffffu, !*(volatile int*)abort_flag && (!ARING || bar_wait(&afull[s], (it / SA) & 1)) &&
                                        (it < K || bar_wait(&done[t], ((it / K) - 1) & 1)))) {
         ok = false;
         break;
       }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      // row r, columns [16 half, 16 half + 16): 16-byte chunks 4 half + j of
-      // the swizzled row (chunk c at position c ^ (r mod 8))
-      const float4* a = reinterpret_cast<const float4*>(stageA(s));
-      float hv[16], tv[16];
+      if constexpr (ARING) {
+        const float4* a = reinterpret_cast<const float4*>(stageA(s)) + aoff;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const float4 x = a[r * 8 + ((4 * half + j) ^ (r & 7))];
-        hv[4 * j] = x.x;
-        hv[4 * j + 1] = x.y;
-        hv[4 * j + 2] = x.z;
-        hv[4 * j + 3] = x.w;
+        for (int j = 0; j < 4; ++j) {
+          const float4 x = a[32 * j];
+          hv[4 * j] = x.x;
+          hv[4 * j + 1] = x.y;
+          hv[4 * j + 2] = x.z;
+          hv[4 * j + 3] = x.w;
+        }
+        bar_arrive(&aempty[s]);  // the stage may be refilled
       }
-      bar_arrive(&aempty[s]);  // the stage may be refilled
-#pragma unroll
-      for (int j = 0; j < 16; ++j) tv[j] = tf32_tail(hv[j]);
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       // the MMAs read the value as TF32 (its head, truncated); the tail 32 columns further
       const uint32_t ta = lane_addr + (uint32_t)(C::kSlotCol0 + t * 64 + 16 * half);
       tmem_st16(ta, hv);
-      tmem_st16(ta + 32, tv);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) hv[j] = tf32_tail(hv[j]);
+      tmem_st16(ta + 32, hv);
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       bar_arrive(&conv[t]);
@@ -616,9 +667,13 @@ void run_tc(const TcDense& d, const float2* x, int64_t xes, const TcColMap& xm, 
   if (per % nkb != 0)
     part = static_cast<float2*>(ws->get(slot + 1, (size_t)rtiles * smax * H * (kTcBM / 2) * sizeof(float2)));
   const bool cols = ncolt > 1 || ym.s1 != 1 || ym.s3 != 1;
-  auto kern = cols ? k_tc_cgemm<BN, true> : k_tc_cgemm<BN, false>;
-  QOB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::kSmem));
-  launch_kernel(pdl, kern, dim3((unsigned)blocks), (unsigned)kTcThreads, C::kSmem, s,
+  // the A ring for a matrix streamed once from memory (one column tile, larger
+  // than half the L2), direct loads for one read from L2
+  const bool aring = !cols && d.stream_a;
+  auto kern = cols ? k_tc_cgemm<BN, true, false> : aring ? k_tc_cgemm<BN, false, true> : k_tc_cgemm<BN, false, false>;
+  const size_t smem = C::smem(aring);
+  QOB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  launch_kernel(pdl, kern, dim3((unsigned)blocks), (unsigned)kTcThreads, smem, s,
                 static_cast<const float*>(d.ahat.p), (const float*)bh, (const float*)bl, d.m, (int)mt, ncols, (int)nkb,
                 per, units, smax, y, yes, ym, alpha, beta, part, status);
   QOB_LAUNCHED();
@@ -629,9 +684,20 @@ void run_tc(const TcDense& d, const float2* x, int64_t xes, const TcColMap& xm, 
   }
 }
 
+// Position of element (row rr, column kk) in an Ahat tile: the order in which
+// the split warps load it.  Warp half h of the warps that own tensor-memory
+// lanes 32 q .. 32 q + 31 loads columns [16 h, 16 h + 16) of those rows as
+// four 16-byte loads j (columns 16 h + 4 j .. + 3), lane l for row 32 q + l, so
+// that each load of a warp reads 512 consecutive bytes.
+__device__ __forceinline__ int a_slot(int rr, int kk) {
+  const int q = rr >> 5, l = rr & 31, h = kk >> 4, jj = (kk >> 2) & 3, e = kk & 3;
+  return ((((q * 2 + h) * 4 + jj) * 32 + l) << 2) + e;
+}
+
 // Ahat of the stored ComplexF32 matrix (column-major m x n, on the device) as
-// swizzled 128 x 32 tiles, tile (t, b) at float offset (t * nkb + b) * 4096:
-// row 2i = Re A[i, :], row 2i + 1 = Im A[i, :]; zero beyond the matrix.
+// 128 x 32 tiles, tile (t, b) at float offset (t * nkb + b) * 4096, each in the
+// order the split warps of k_tc_cgemm load it (a_slot): row 2i = Re A[i, :],
+// row 2i + 1 = Im A[i, :]; zero beyond the matrix.
 __global__ void k_tc_build_ahat(const float2* __restrict__ a, int64_t m, int64_t n, int64_t nkb, float* __restrict__ ah) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // complex row
   const int64_t k = blockIdx.y;
@@ -641,8 +707,8 @@ __global__ void k_tc_build_ahat(const float2* __restrict__ a, int64_t m, int64_t
   const int64_t r = 2 * i;  // Ahat row of the real part; the imaginary part is the next row of the same tile
   const int64_t tile = ((r / kTcBM) * nkb + k / kTcBK) * (int64_t)(kTcBM * kTcBK);
   const int rr = (int)(r % kTcBM), kk = (int)(k % kTcBK);
-  ah[tile + swz(rr, kk)] = v.x;
-  ah[tile + swz(rr + 1, kk)] = v.y;
+  ah[tile + a_slot(rr, kk)] = v.x;
+  ah[tile + a_slot(rr + 1, kk)] = v.y;
 }
 
 }  // namespace
@@ -655,6 +721,10 @@ void tc_dense_build(TcDense& d, const void* a, int64_t m, int64_t n, cudaStream_
   if (d.ldk > 65535) fail(QOB_ERR_UNSUPPORTED, "tensor-core dense path: more than 65535 columns");
   const int64_t nkb = d.ldk / kTcBK;
   d.ahat.alloc((size_t)d.mtiles * nkb * kTcBM * kTcBK * sizeof(float));
+  int dev = 0, l2 = 0;
+  QOB_CUDA(cudaGetDevice(&dev));
+  QOB_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
+  d.stream_a = d.ahat.bytes > (size_t)l2 / 2;
   const int64_t mpad = d.mtiles * kTcBM / 2;
   k_tc_build_ahat<<<dim3((unsigned)((mpad + 127) / 128), (unsigned)d.ldk), 128, 0, s>>>(
       static_cast<const float2*>(a), m, n, nkb, static_cast<float*>(d.ahat.p));

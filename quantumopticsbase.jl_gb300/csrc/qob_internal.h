@@ -290,6 +290,7 @@ struct GatherPlan {
 struct TcDense {
   int64_t m = 0, n = 0, ldk = 0, mtiles = 0;
   DeviceBuf ahat;
+  bool stream_a = false;  // the tiled matrix is larger than half the L2 (streamed from memory on each call)
   bool ready = false;
 };
 
