@@ -89,6 +89,8 @@ def parse():
     p.add_argument("--pdl", type=int, default=1, choices=[0, 1],
                    help="programmatic dependent launch (QOB_OPT_PDL) for every timed form (default on: the steps "
                         "measured 1-3 %% faster with it); the other setting is timed beside it in the pdl sub-object")
+    p.add_argument("--batch-tile", type=int, default=None, choices=[128, 256, 512, 1024],
+                   help="with --suite: fix the uneven batch's tile length instead of tuning it (for profiling)")
     p.add_argument("--no-secondary", action="store_true",
                    help="leave out the batched and served sub-objects (used for ncu captures)")
     return p.parse_args()
@@ -737,7 +739,7 @@ def main():
     if args.suite:
         from bench_suite import run_suite
 
-        return run_suite(local_rank, args.only, args.pdl)
+        return run_suite(local_rank, args.only, args.pdl, args.batch_tile)
     if args.probe:
         return print(json.dumps(probe_peaks(local_rank)), flush=True)
     run_own(args, rank, world, local_rank)

@@ -194,7 +194,10 @@ def rho_h8(ctx, stream):
     return {"workload": "rho_h8", "results": out}
 
 
-def cavities256(ctx, stream):
+def cavities256(ctx, stream, tile=None):
+    """256 uneven two-mode cavities in one persistent launch; the tile length
+    tuned (qob_batch_tune), or fixed to `tile` (the tuned 256 under a
+    profiler, whose replays would time the tuner's candidates differently)."""
     import torch
 
     from qobgpu.evolution import Batch
@@ -212,7 +215,11 @@ def cavities256(ctx, stream):
             x = _cols(dims[k], 1, tdt, 10 + k).contiguous()
             y = _cols(dims[k], 1, tdt, 20 + k).contiguous()
             b.add(H, x, y, 0.7 - 0.2j, 0.3)
-        chosen, times = b.tune()
+        if tile:
+            b.set_tile(tile)
+            chosen = tile
+        else:
+            chosen, times = b.tune()
         ms = _timed_graph(ctx, stream, lambda sp: raise_for(L.lib().qob_batch_run(ctx.ptr, b.ptr, sp), ctx), reps=50)
         s = 16 if npdt == np.complex128 else 8
         bytes_ = 3 * sum(dims) * s
@@ -458,10 +465,11 @@ WORKLOADS = ("jc512", "sparse4096", "rho_h8", "lindblad", "particle", "modek", "
              "host_link")
 
 
-def run_suite(device: int = 0, only=None, pdl: int = 1):
+def run_suite(device: int = 0, only=None, pdl: int = 1, batch_tile=None):
     """Run the workloads (all, or the names in `only`), one JSON line each,
     with programmatic dependent launch on (pdl = 1, as the headline bench) or
-    off."""
+    off; batch_tile fixes the persistent batch's tile length instead of
+    tuning it."""
     import torch
 
     ctx = get_context(device)
@@ -470,7 +478,7 @@ def run_suite(device: int = 0, only=None, pdl: int = 1):
     names = [w for w in WORKLOADS if not only or w in only]
     for fn in (globals()[w] for w in names):
         t0 = time.perf_counter()
-        line = fn(ctx, stream)
+        line = fn(ctx, stream, batch_tile) if fn is cavities256 and batch_tile else fn(ctx, stream)
         line["seconds"] = time.perf_counter() - t0
         line["pdl"] = bool(pdl)
         print(json.dumps(line), flush=True)

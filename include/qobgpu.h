@@ -404,6 +404,9 @@ int qob_apply_batched(qob_ctx* ctx, int dtype, int n, qob_op* const* ops, const 
 /* Time tile lengths 128 / 256 / 512 / 1024 (times_ms[0..3]) and keep the
  * fastest; runs the batch 28 times, so the outputs are overwritten. */
 int qob_batch_tune(qob_ctx* ctx, qob_batch* batch, double* times_ms, int* chosen);
+/* Set the tile length (128, 256, 512 or 1024 output indices) without timing,
+ * e.g. to the one a previous qob_batch_tune chose; QOB_ERR_ARG otherwise. */
+int qob_batch_set_tile(qob_ctx* ctx, qob_batch* batch, int tile);
 /* info[0] items, [1] items in the fused launch, [2] tiles, [3] tile length,
  * [4] blocks of the persistent grid. */
 int qob_batch_info(qob_ctx* ctx, qob_batch* batch, int64_t* info);

@@ -374,6 +374,15 @@ int qob_batch_tune(qob_ctx* ctx, qob_batch* b, double* times_ms, int* chosen) {
   });
 }
 
+int qob_batch_set_tile(qob_ctx* ctx, qob_batch* b, int tile) {
+  return bguard(ctx, [&] {
+    if (!b) qob::fail(QOB_ERR_ARG, "null batch");
+    if (tile != 128 && tile != 256 && tile != 512 && tile != 1024)
+      qob::fail(QOB_ERR_ARG, "qob_batch_set_tile: tile must be 128, 256, 512 or 1024");
+    rebuild(ctx, b, tile);
+  });
+}
+
 int qob_batch_info(qob_ctx* ctx, qob_batch* b, int64_t* info) {
   return bguard(ctx, [&] {
     if (!b || !info) qob::fail(QOB_ERR_ARG, "qob_batch_info: bad arguments");

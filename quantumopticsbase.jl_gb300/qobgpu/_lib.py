@@ -81,6 +81,7 @@ SIGNATURES = {
     "qob_batch_run": (I, [VP, VP, VP]),
     "qob_batch_tune": (I, [VP, VP, DP, C.POINTER(C.c_int)]),
     "qob_batch_info": (I, [VP, VP, I64P]),
+    "qob_batch_set_tile": (I, [VP, VP, I]),
     "qob_batch_free": (I, [VP, VP]),
     "qob_rk4": (I, [VP, VP, I, VP, I64, D, I, I, VP]),
     "qob_apply_batched": (I, [VP, I, I, C.POINTER(VP), C.POINTER(VP), C.POINTER(VP), DP, DP, VP]),

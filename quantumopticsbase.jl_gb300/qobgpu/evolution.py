@@ -58,6 +58,10 @@ class Batch:
         raise_for(L.lib().qob_batch_tune(self.ctx.ptr, self.ptr, t, C.byref(ch)), self.ctx)
         return ch.value, list(t)
 
+    def set_tile(self, tile: int):
+        """Fix the tile length (128, 256, 512 or 1024) without timing."""
+        raise_for(L.lib().qob_batch_set_tile(self.ctx.ptr, self.ptr, int(tile)), self.ctx)
+
     def info(self):
         v = (C.c_int64 * 5)()
         raise_for(L.lib().qob_batch_info(self.ctx.ptr, self.ptr, v), self.ctx)

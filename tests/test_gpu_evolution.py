@@ -110,6 +110,43 @@ def test_uneven_batch_matches_oracle(dtype, tol):
 
 
 @pytest.mark.parametrize("dtype,tol", [(np.complex128, 1e-12), (np.complex64, 1e-5)])
+def test_batch_set_tile_every_length_matches_oracle(dtype, tol):
+    """qob_batch_set_tile fixes the persistent launch's tile length without
+    timing: every allowed length (128 .. 1024 output indices, so tiles that
+    cover several items' ends and items longer than one tile) gives the oracle's
+    result, qob_batch_info reports the length and tile count, and a length
+    outside the four is refused with QOB_ERR_ARG."""
+    import torch
+
+    from qobgpu import _lib as L
+    from qobgpu.evolution import Batch
+
+    models = cavity_models(12, seed=17)
+    rng = Q.Rng(18)
+    data = []
+    for H in models:
+        n = len(H.basis_l)
+        data.append((H, rng.ket_data(n), rng.ket_data(n)))
+    ref = [OR.mul(Q.Ket(H.basis_l, y), H, Q.Ket(H.basis_r, x), 0.7 - 0.2j, 0.3) for H, x, y in data]
+    for tile in (128, 256, 512, 1024):
+        b = Batch(dtype)
+        ys = []
+        for H, x, y in data:
+            yd = torch.as_tensor(y.astype(dtype), device="cuda:0")
+            b.add(H, torch.as_tensor(x.astype(dtype), device="cuda:0"), yd, 0.7 - 0.2j, 0.3)
+            ys.append(yd)
+        b.set_tile(tile)
+        info = b.info()
+        assert info["tile"] == tile
+        assert info["tiles"] == sum(-(-len(H.basis_l) // tile) for H, _, _ in data)
+        b.run()
+        torch.cuda.synchronize()
+        for yd, r in zip(ys, ref):
+            assert rel_l2(yd.cpu().numpy().astype(np.complex128), r) < tol, tile
+    assert L.lib().qob_batch_set_tile(b.ctx.ptr, b.ptr, 300) == L.QOB_ERR_ARG
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, 1e-12), (np.complex64, 1e-5)])
 def test_rk4_matches_host_rk4(dtype, tol):
     import torch
 
