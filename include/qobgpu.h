@@ -472,8 +472,10 @@ int qob_rk4_td(qob_ctx* ctx, qob_op* H, int dtype, void* psi, int64_t n, double 
  * queued request is admitted when fewer than max_active run and its device
  * memory (4 state vectors) fits both mem_budget and the free device memory;
  * requests larger than mem_budget are rejected (status -QOB_ERR_OOM).  A step
- * of every active request is eight batched launches, recorded once per set of
- * active requests into a CUDA graph and replayed; an engine iteration on the
+ * of every active request is four batched launches (each RK4 stage's
+ * combination done in the batched gather's epilogue; eight, the combinations
+ * apart, when an operator does not compile into the fused gather), recorded
+ * once per set of active requests into a CUDA graph and replayed; an engine iteration on the
  * worker thread (qob_server_start / _stop) runs up to 16 steps (4 while
  * requests wait, never past a request's last step), qob_server_step runs one.
  * Requests that arrive while others run join at the next iteration.  A
