@@ -113,8 +113,8 @@ def test_tc32_mode_products(fp32_tensor, dims, sites, ncols):
         check(Z, R, op, AL, BE, TOL32, np.complex64)
 
 
-@pytest.mark.parametrize("which", ["dense", "mode_products"])
-def test_tc32_pdl_keeps_chained_applications_ordered(fp32_tensor, which):
+@pytest.mark.parametrize("which,k", [("dense", 16), ("dense", 7), ("mode_products", 16)])
+def test_tc32_pdl_keeps_chained_applications_ordered(fp32_tensor, which, k):
     """QOB_OPT_PDL on the tensor-core path: the split, GEMM and reduce kernels
     of each application are launched with programmatic dependent launch (the
     GEMM's set-up overlaps the split, every kernel waits for its predecessor
@@ -122,9 +122,10 @@ def test_tc32_pdl_keeps_chained_applications_ordered(fp32_tensor, which):
     ComplexF32 applications recorded into a CUDA graph and replayed equals the
     oracle's chain at the ComplexF32 tolerance and is bitwise equal to the same
     chain without PDL; a dense 1024 x 1024 operator on 16 kets (row tiles split
-    over several blocks, partial products reduced) and two 200 x 200 mode
-    products on a 200 x 3 x 200 basis (two split -> GEMM -> reduce chains per
-    application)."""
+    over several blocks, partial products reduced), the same on 7 kets (a
+    ragged column tile: the split's buffers are cleared by a memset that the
+    split launch follows) and two 200 x 200 mode products on a 200 x 3 x 200
+    basis (two split -> GEMM -> reduce chains per application)."""
     import torch
 
     import oracle as OR
@@ -141,7 +142,7 @@ def test_tc32_pdl_keeps_chained_applications_ordered(fp32_tensor, which):
         b = Q.tensor_basis(Q.GenericBasis(200), Q.GenericBasis(3), Q.GenericBasis(200))
         op = O.LazyTensor(b, b, (1, 3), (_dense_factor(rng, 200), _dense_factor(rng, 200)), 1.0)
         alpha = 1.0 / 200.0
-    n, k = len(b), 16
+    n = len(b)
     X = rng.kets_data(n, k)
     node = OR.build_node(op)
     ref = [np.asfortranarray(X.astype(np.complex64).astype(np.complex128))]
