@@ -377,10 +377,13 @@ void launch_axpby(int precision, const void* x, int64_t xes, int64_t xcs, c128 a
 
 namespace {
 // k ranges per dense product: enough blocks for about eight per SM (fine
-// enough that the last wave is short), each range at least 64 columns long
+// enough that the last wave is short), sixteen for one ket per thread (a
+// stream of the matrix, latency-bound: twice the warps in flight), each range
+// at least 64 columns long
 int dense_kchunks(int64_t m, int64_t n, int64_t ncols, int tc) {
   const int64_t blocks = ((m + 127) / 128) * ((ncols + tc - 1) / tc);
-  int64_t kch = (1216 + blocks - 1) / blocks;
+  const int64_t target = tc == 1 ? 2432 : 1216;
+  int64_t kch = (target + blocks - 1) / blocks;
   kch = std::min<int64_t>(kch, std::max<int64_t>(1, n / 64));
   return (int)std::max<int64_t>(1, std::min<int64_t>(kch, 65535));
 }
